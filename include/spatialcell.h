@@ -1,0 +1,289 @@
+/*
+ * spatialcell.h -- C ABI of libspatialcell, the sm_103a (GB300) per-step
+ * simulation hot path of spatial_cell_sim.
+ *
+ * The reference (justgos/spatial-cell, spatial_cell_sim) has no library
+ * interface: its step is the body of main() (spatial_cell_sim/src/main.cu:347-700)
+ * launching CUDA kernels on process-global state (__constant__ d_Config,
+ * config.cuh:102).  This header is the boundary a driver binds instead:
+ *
+ *   reference                                     this ABI
+ *   -------------------------------------------   ------------------------------
+ *   Config(Json::Value)  config.cuh:46-75         sc_config, sc_config_load_json
+ *   loadParticleTypeInfo chemistry.cuh:10-33      sc_types_load_json
+ *   flattenParticleTypeInfo chemistry.cuh:38-51   (id-indexed sc_type_info[])
+ *   loadComplexificationInfo interactions.cuh:17-54   sc_rules_load_json
+ *   flattenComplexificationInfo / partnerMap...   sc_create (builds both)
+ *     interactions.cuh:59-145
+ *   setupParticles -> DoubleBuffer copyToDevice   sc_load_state
+ *     setup/setup.cuh:17-253, memory.cuh:256
+ *   initial sort + removeInterfering + complexify(-1)  sc_prepare
+ *     main.cu:284-338
+ *   one iteration of the step loop main.cu:347-661    sc_step
+ *   single kernels of that loop                   sc_run_phase
+ *   reduceParticles + persistFrame                sc_reduce_frame
+ *     dynamics.cuh:824-844, main.cu:95-126
+ *   FileStorage writeHeader / writeFrame          sc_frames_write_header / _frame
+ *     storage.cuh:22-39
+ *
+ * Conventions: every function returns 0 on success and a negative SC_E_*
+ * code on failure; sc_last_error() gives the message.  A sim owns all of its
+ * device memory and one CUDA stream; calls on one sim must come from one host
+ * thread at a time, different sims are independent.  Layouts below are the
+ * reference's structs byte for byte (types.cuh:167-300, NUM_METABOLITES = 10).
+ */
+#ifndef SPATIALCELL_H
+#define SPATIALCELL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SC_MAX_ACTIVE_INTERACTIONS 8  /* constants.cuh:18 */
+#define SC_AOS_NUM_METABOLITES 10     /* constants.cuh:15 */
+#define SC_REDUCED_NUM_METABOLITES 4  /* constants.cuh:16 */
+#define SC_PARTICLE_FLAG_ACTIVE 0x1   /* constants.cuh:23 */
+#define SC_INTERACTION_TYPE_CHAIN 1
+#define SC_INTERACTION_GROUP_FORWARD 10
+#define SC_INTERACTION_GROUP_BACKWARD 11
+#define SC_PARTICLE_TYPE_LIPID 0
+#define SC_PARTICLE_TYPE_METABOLIC 1000
+#define SC_HYDROPHYLIC 0
+#define SC_HYDROPHOBIC 1
+#define SC_POLAR 2
+
+/* Status codes */
+#define SC_OK 0
+#define SC_E_INVALID (-1)  /* bad argument, config or table */
+#define SC_E_CUDA (-2)     /* CUDA runtime error */
+#define SC_E_OOM (-3)      /* device allocation failed */
+#define SC_E_IO (-4)       /* file open / read / write failed */
+#define SC_E_PARSE (-5)    /* malformed JSON */
+#define SC_E_DEVICE (-6)   /* a kernel reported an error (bounded wait expired, bounds) */
+#define SC_E_STATE (-7)    /* call out of order (e.g. step before load) */
+
+/* ParticleInteraction, types.cuh:167-171 (12 bytes) */
+typedef struct sc_interaction {
+    int32_t type;
+    int32_t group;
+    int32_t partner_id;
+} sc_interaction;
+
+/* Particle, types.cuh:173-222 (256 bytes). */
+typedef struct sc_particle {
+    int32_t id;                        /*   0 */
+    int32_t type;                      /*   4 */
+    int32_t flags;                     /*   8 */
+    int8_t state;                      /*  12 */
+    int8_t _pad0[3];
+    int32_t last_state_change_step;    /*  16 */
+    float radius;                      /*  20 */
+    int8_t hydrophobic;                /*  24 */
+    int8_t _pad1[3];
+    float pos[3];                      /*  28 */
+    float _pad2[2];
+    float rot[4];                      /*  48 */
+    float velocity[3];                 /*  64 */
+    float pos_noise[3];                /*  76 */
+    float _pad3[2];
+    float angular_velocity[4];         /*  96 */
+    float angular_noise[4];            /* 112 */
+    int32_t n_active_interactions;     /* 128 */
+    sc_interaction interactions[SC_MAX_ACTIVE_INTERACTIONS]; /* 132 */
+    int32_t scheduled_polymerization;  /* 228 */
+    float _pad4[2];
+    float debug_vector[4];             /* 240 */
+} sc_particle;
+
+/* MetabolicParticle, types.cuh:224-242 (304 bytes). */
+typedef struct sc_metabolic_particle {
+    sc_particle p;                               /*   0 */
+    float metabolites[SC_AOS_NUM_METABOLITES];   /* 256 */
+    float _pad[2];
+} sc_metabolic_particle;
+
+/* ReducedParticle, types.cuh:244-287 (36 bytes); halves are IEEE binary16. */
+typedef struct sc_reduced_particle {
+    int32_t id;
+    int32_t type;
+    int32_t flags;        /* flags | (state & 0xF) << 16 */
+    uint16_t radius;
+    uint16_t pos[3];
+    uint16_t rot[4];
+    uint16_t debug_vector[4];
+} sc_reduced_particle;
+
+/* ReducedMetabolicParticle, types.cuh:289-300 (44 bytes). */
+typedef struct sc_reduced_metabolic_particle {
+    sc_reduced_particle p;
+    uint16_t metabolites[SC_REDUCED_NUM_METABOLITES];
+} sc_reduced_metabolic_particle;
+
+/* MinimalParticleTypeInfo, types.cuh:16-32 (8 bytes); id-indexed table. */
+typedef struct sc_type_info {
+    float radius;
+    int8_t hydrophobic;
+    int8_t _pad[3];
+} sc_type_info;
+
+/* ParticleInteractionInfo, types.cuh:55-126 (96 bytes). */
+typedef struct sc_rule {
+    int32_t id;                          /*  0 */
+    int32_t group;                       /*  4 */
+    int32_t first_partner_type;          /*  8 */
+    int8_t first_partner_state;          /* 12 */
+    int8_t _pad0[3];
+    int32_t second_partner_type;         /* 16 */
+    int8_t second_partner_state;         /* 20 */
+    uint8_t propagate_state;             /* 21 */
+    uint8_t set_state;                   /* 22 */
+    uint8_t wait_for_state;              /* 23 */
+    uint8_t wait_for_alignment;          /* 24 */
+    uint8_t only_via_transition;         /* 25 */
+    uint8_t _pad1[2];
+    int32_t transition_to;               /* 28 */
+    int32_t polymerize;                  /* 32 */
+    uint8_t break_after_transition;      /* 36 */
+    uint8_t _pad2[11];
+    float relative_orientation[4];       /* 48 */
+    float orientation_alignment_threshold; /* 64 */
+    float relative_position[3];          /* 68 */
+    float position_alignment_threshold;  /* 80 */
+    float _pad3[3];
+} sc_rule;
+
+/* config.json (spatial_cell_sim/config.json, config.cuh:15-75) plus
+ * extension keys whose defaults reproduce the reference. */
+typedef struct sc_config {
+    int32_t num_particles;            /* particle capacity */
+    int32_t num_metabolic_particles;  /* metabolic particle capacity */
+    int32_t steps;
+    float sim_size;
+    float max_interaction_distance;
+    float max_diffusion_distance;
+    float grid_cell_size;
+    float movement_noise_scale;
+    float rotation_noise_scale;
+    float metabolite_movement_noise_scale;
+    float velocity_decay;
+    float angular_velocity_decay;
+    int32_t noise_coordination_steps;
+    int32_t relaxation_steps;
+    int32_t metabolite_diffusion_steps;
+    int32_t persist_every_nth_frame;
+    int32_t report_every_nth_frame;
+    /* extensions */
+    int32_t num_metabolites;  /* simulated species S, 1..10 (reference: 10) */
+    int32_t _reserved;
+    uint64_t seed;            /* Philox key of the Brownian noise */
+} sc_config;
+
+/* Counters of a sim (the reference's nActiveParticles, lastActiveParticle,
+ * nextParticleId and nActiveMetabolicParticles buffers, main.cu:244-253). */
+typedef struct sc_counters {
+    int32_t n_active_particles;
+    int32_t n_active_metabolic_particles;
+    int32_t next_particle_id;
+    int32_t step;
+    int64_t kernel_launches;   /* kernels this sim has launched so far */
+    int32_t device_error;      /* sticky kernel-side error code, 0 if none */
+    int32_t _reserved;
+} sc_counters;
+
+/* Phases for sc_run_phase: one reference kernel (or kernel pair) each. */
+enum sc_phase {
+    SC_PHASE_SORT_PARTICLES = 0,      /* updateGridAndSort<Particle>, grid.cuh:111-139 */
+    SC_PHASE_SORT_METABOLIC = 1,      /* updateGridAndSort<MetabolicParticle> */
+    SC_PHASE_MOVE_BROWNIAN = 2,       /* move + brownianMovementAndRotation<Particle>, main.cu:375-395 */
+    SC_PHASE_MOVE_BROWNIAN_METAB = 3, /* moveMetabolicParticles + brownian<Metabolic>, main.cu:402-419 */
+    SC_PHASE_COORDINATE_NOISE = 4,    /* coordinateNoise, fraction = arg / noiseCoordinationSteps */
+    SC_PHASE_APPLY_NOISE = 5,         /* applyNoise<Particle> + applyNoise<Metabolic> */
+    SC_PHASE_RELAX = 6,               /* relax, dynamics.cuh:405-822 */
+    SC_PHASE_RELAX_METAB = 7,         /* relaxMetabolicParticles, metabolites.cuh:140-264 */
+    SC_PHASE_RELAX_PARTNERS = 8,      /* relaxMetabolicParticlePartners, metabolites.cuh:266-350 */
+    SC_PHASE_APPLY_VELOCITIES = 9,    /* applyVelocities x2 (fraction 0.45) */
+    SC_PHASE_COMPLEXIFY = 10,         /* complexify, interactions.cuh:216-346 */
+    SC_PHASE_TRANSITION = 11,         /* transitionInteractions, interactions.cuh:349-555 */
+    SC_PHASE_POLYMERIZE = 12,         /* polymerize, interactions.cuh:558-740 */
+    SC_PHASE_DIFFUSE = 13,            /* diffuseMetabolites, metabolites.cuh:352-431 */
+    SC_PHASE_REMOVE_INTERFERING = 14, /* removeInterferingMetabolicParticles, metabolites.cuh:18-88 */
+    SC_PHASE_END_STEP = 15            /* step counter += 1 */
+};
+
+typedef struct sc_sim sc_sim;
+
+/* ---- configuration and tables (host only) ---- */
+/* Reference defaults (spatial_cell_sim/config.json) plus extension defaults. */
+void sc_config_defaults(sc_config *cfg);
+/* Parses config.json (Config(Json::Value), config.cuh:46-64).  Missing keys
+ * keep the values already in *cfg. */
+int sc_config_load_json(const char *path, sc_config *cfg);
+/* Derived grid values of config.cuh:65-74 (cells per axis rounded up to a
+ * power of two, at least 2). */
+int sc_config_grid(const sc_config *cfg, int32_t *n_grid_cells, int32_t *n_grid_bits);
+/* large-molecules.json -> id-indexed table (chemistry.cuh:10-51).  Writes
+ * max(type)+1 entries (missing ids zero) if they fit in capacity; *n_types
+ * always receives the required count. */
+int sc_types_load_json(const char *path, sc_type_info *out, int32_t capacity, int32_t *n_types);
+/* complexification.json -> rule list in file order (interactions.cuh:17-54),
+ * with jsoncpp's defaults and its null handling (an explicit null reads as 0). */
+int sc_rules_load_json(const char *path, sc_rule *out, int32_t capacity, int32_t *n_rules);
+
+/* ---- simulation ---- */
+/* Creates a sim on the current CUDA device.  types: id-indexed, n_types
+ * entries.  rules: any order; the first of duplicate ids wins. */
+int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types,
+              const sc_rule *rules, int32_t n_rules, sc_sim **out);
+void sc_destroy(sc_sim *sim);
+/* Message of the last failure of this sim (sim == NULL: of the last failed
+ * call that had no sim). */
+const char *sc_last_error(const sc_sim *sim);
+
+/* Uploads a reference-layout state.  particles[0..n) and metabolic[0..nm) are
+ * the set-up items; the rest of capacity is zero (inactive), as the
+ * reference's memset host buffers are.  n and nm become the active counters
+ * (nActiveParticles, nActiveMetabolicParticles); step is the loop counter of
+ * the next step; next_particle_id the id the next polymerised monomer gets. */
+int sc_load_state(sc_sim *sim, const sc_particle *particles, int32_t n,
+                  const sc_metabolic_particle *metabolic, int32_t nm,
+                  int32_t step, int32_t next_particle_id);
+/* main.cu:284-338: sort both sets, removeInterferingMetabolicParticles, and
+ * the initial complexify (step -1). */
+int sc_prepare(sc_sim *sim);
+/* Runs n_steps iterations of the step loop (main.cu:347-661) asynchronously
+ * on the sim's stream. */
+int sc_step(sc_sim *sim, int32_t n_steps);
+/* Runs one phase of the loop (for differential testing). */
+int sc_run_phase(sc_sim *sim, int32_t phase, int32_t arg);
+/* Waits for the sim's stream and reports kernel-side errors. */
+int sc_sync(sc_sim *sim);
+
+/* Downloads the state in the reference layout, capacity-sized buffers (either
+ * may be NULL).  Interaction slots at and beyond n_active_interactions are
+ * written as zero. */
+int sc_export_state(sc_sim *sim, sc_particle *particles, sc_metabolic_particle *metabolic);
+/* Sort results of the last sort: which = 0 particles, 1 metabolic.
+ * ranges: 2 * cells uint32 in the reference's gridRanges layout ([start, end)
+ * per cell, zero for empty cells); perm: capacity entries, the pre-sort slot
+ * of every sorted slot.  Either may be NULL. */
+int sc_export_grid(sc_sim *sim, int32_t which, uint32_t *ranges, uint32_t *perm);
+int sc_get_counters(sc_sim *sim, sc_counters *out);
+/* The frames.dat payload of the current state (reduceParticles on the
+ * counters' ranges, zero beyond), into capacity-sized host buffers. */
+int sc_reduce_frame(sc_sim *sim, sc_reduced_particle *particles,
+                    sc_reduced_metabolic_particle *metabolic);
+
+/* ---- frames.dat (storage.cuh:9-44) ---- */
+int sc_frames_write_header(void *file /* FILE* */, const sc_config *cfg);
+int sc_frames_write_frame(void *file /* FILE* */, const sc_config *cfg,
+                          const sc_reduced_particle *particles,
+                          const sc_reduced_metabolic_particle *metabolic);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPATIALCELL_H */

@@ -1,0 +1,144 @@
+"""ctypes drivers of the CPU oracle libraries (TEST INFRASTRUCTURE ONLY).
+
+``OracleEngine("port")`` drives oracle/_build/libscport.so (the CPU
+restatement); ``OracleEngine("ref")`` drives oracle/_ref/libscref.so (the
+reference's own kernels compiled for the host).  Both expose the same calls
+as the product's C ABI, so a test can run one scenario through all of them.
+"""
+import ctypes
+
+import numpy as np
+
+from spatial_cell_gb300 import abi
+
+from . import build
+
+_LIBS = {}
+
+_SIGS = {
+    "create": (ctypes.c_void_p, [ctypes.POINTER(abi.Config), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_int]),
+    "destroy": (None, [ctypes.c_void_p]),
+    "load_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int]),
+    "run_phase": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "prepare": (ctypes.c_int, [ctypes.c_void_p]),
+    "step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "export_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "export_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "get_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(abi.Counters)]),
+    "reduce_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+}
+
+
+def load(kind):
+    """Loads (building first if needed) the 'port' or 'ref' library."""
+    if kind in _LIBS:
+        return _LIBS[kind]
+    if kind == "port":
+        path, prefix = build.build_port(), "scp_"
+    elif kind == "ref":
+        path, prefix = build.build_ref(), "oref_"
+        if path is None:
+            raise FileNotFoundError("the reference tree is not present; the reference harness cannot be built")
+    else:
+        raise ValueError(kind)
+    lib = ctypes.CDLL(path)
+    fns = {}
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, prefix + name)
+        f.restype = res
+        f.argtypes = args
+        fns[name] = f
+    if kind == "port":
+        lib.scp_set_threads.argtypes = [ctypes.c_int]
+        lib.scp_max_threads.restype = ctypes.c_int
+        fns["set_threads"] = lib.scp_set_threads
+        fns["max_threads"] = lib.scp_max_threads
+    if kind == "ref":
+        lib.oref_load_tables.restype = ctypes.c_int
+        lib.oref_load_tables.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p] * 4
+        lib.oref_load_config.restype = ctypes.c_int
+        lib.oref_load_config.argtypes = [ctypes.c_char_p, ctypes.POINTER(abi.Config), ctypes.c_void_p,
+                                         ctypes.c_void_p]
+        fns["load_tables"] = lib.oref_load_tables
+        fns["load_config"] = lib.oref_load_config
+    _LIBS[kind] = (lib, fns)
+    return _LIBS[kind]
+
+
+class OracleEngine:
+    def __init__(self, kind, cfg, types, rules):
+        self.kind = kind
+        self.lib, self.f = load(kind)
+        self.cfg = cfg
+        self.types = np.ascontiguousarray(types, dtype=abi.TYPE_INFO_DTYPE)
+        self.rules = np.ascontiguousarray(rules, dtype=abi.RULE_DTYPE)
+        self.h = self.f["create"](ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules),
+                                  len(self.rules))
+        if not self.h:
+            raise ValueError("oracle rejected the configuration")
+        self.n_grid, self.bits, self.cells = abi.grid_dims(cfg)
+
+    def close(self):
+        if self.h:
+            self.f["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{self.kind}: {what} failed ({rc})")
+
+    def load_state(self, particles, metabolic, step=0, next_particle_id=None):
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        m = np.ascontiguousarray(metabolic, abi.METABOLIC_DTYPE)
+        if next_particle_id is None:
+            next_particle_id = len(p)
+        self._check(self.f["load_state"](self.h, abi.ptr(p), len(p), abi.ptr(m), len(m), step, next_particle_id),
+                    "load_state")
+
+    def run_phase(self, phase, arg=0):
+        self._check(self.f["run_phase"](self.h, phase, arg), f"phase {phase}")
+
+    def prepare(self):
+        self._check(self.f["prepare"](self.h), "prepare")
+
+    def step(self, n=1):
+        self._check(self.f["step"](self.h, n), "step")
+
+    def export_state(self):
+        p = np.zeros(self.cfg.num_particles, abi.PARTICLE_DTYPE)
+        m = np.zeros(self.cfg.num_metabolic_particles, abi.METABOLIC_DTYPE)
+        self._check(self.f["export_state"](self.h, abi.ptr(p), abi.ptr(m)), "export_state")
+        return p, m
+
+    def export_grid(self, which):
+        r = np.zeros(self.cells * 2, np.uint32)
+        cap = self.cfg.num_metabolic_particles if which else self.cfg.num_particles
+        perm = np.zeros(max(cap, 1), np.uint32)
+        self._check(self.f["export_grid"](self.h, which, abi.ptr(r), abi.ptr(perm)), "export_grid")
+        return r, perm[:cap]
+
+    def counters(self):
+        c = abi.Counters()
+        self._check(self.f["get_counters"](self.h, ctypes.byref(c)), "get_counters")
+        return c
+
+    def reduce_frame(self):
+        rp = np.zeros(self.cfg.num_particles, abi.REDUCED_DTYPE)
+        rm = np.zeros(self.cfg.num_metabolic_particles, abi.REDUCED_METABOLIC_DTYPE)
+        self._check(self.f["reduce_frame"](self.h, abi.ptr(rp), abi.ptr(rm)), "reduce_frame")
+        return rp, rm
+
+
+def set_threads(n):
+    lib, f = load("port")
+    f["set_threads"](n)
+
+
+def max_threads():
+    lib, f = load("port")
+    return f["max_threads"]()

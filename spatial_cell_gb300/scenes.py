@@ -1,0 +1,268 @@
+"""Synthetic workloads in the reference's state layout.
+
+No dataset is involved anywhere in the reference: its scene is generated in
+code (spatial_cell_sim/src/setup/setup.cuh:17-253).  These generators build
+seeded states with the shapes, sizes and value ranges of the workloads this
+project measures, in the reference's own ``Particle`` / ``MetabolicParticle``
+layout, plus small scenes that exercise every branch of the step (chains,
+rule bonds with transitions and polymerisation, test bonds, lipids).
+"""
+import numpy as np
+
+from . import abi
+
+LIPID, DUMMY, TYPE_A, TYPE_B = 0, 1, 2, 3
+METABOLIC = abi.PARTICLE_TYPE_METABOLIC
+
+
+def random_quaternions(rng, n):
+    """Uniform random unit quaternions (Shoemake's method, as math.cuh:264-277)."""
+    u, v, w = rng.random(n), rng.random(n), rng.random(n)
+    su, su1 = np.sqrt(u), np.sqrt(1.0 - u)
+    q = np.stack([su1 * np.sin(2 * np.pi * v), su1 * np.cos(2 * np.pi * v),
+                  su * np.sin(2 * np.pi * w), su * np.cos(2 * np.pi * w)], axis=1)
+    return q.astype(np.float32)
+
+
+def blank_particles(n, dtype=abi.PARTICLE_DTYPE):
+    """Particle(...) defaults of types.cuh:192-221 (active, identity rotations)."""
+    p = np.zeros(n, dtype)
+    p["flags"] = abi.PARTICLE_FLAG_ACTIVE
+    p["last_state_change_step"] = -1
+    p["rot"][:, 3] = 1.0
+    p["angular_velocity"][:, 3] = 1.0
+    p["angular_noise"][:, 3] = 1.0
+    p["scheduled_polymerization"] = -1
+    return p
+
+
+def baseline_types():
+    """Type table of the measured workloads: lipid r=1.0 (polar), dummy r=2.0,
+    A and B r=2.5, metabolite carrier (type 1000) r=2.5; id-indexed."""
+    t = np.zeros(METABOLIC + 1, abi.TYPE_INFO_DTYPE)
+    t[LIPID] = (1.0, abi.POLAR)
+    t[DUMMY] = (2.0, abi.HYDROPHYLIC)
+    t[TYPE_A] = (2.5, abi.HYDROPHYLIC)
+    t[TYPE_B] = (2.5, abi.HYDROPHYLIC)
+    t[METABOLIC] = (2.5, abi.HYDROPHYLIC)
+    return t
+
+
+def rule(rid, first, second, group=None, first_state=-1, second_state=-1, set_state=1, wait_for_state=1,
+         wait_for_alignment=1, only_via_transition=0, transition_to=-1, polymerize=-1, break_after=0,
+         rel_ori=(0.0, 0.0, 0.0, 1.0), rel_pos=(0.0, 0.0, 0.0), ori_thr=0.8, pos_thr=0.8):
+    """One complexification rule with the loader defaults of interactions.cuh:33-49."""
+    r = np.zeros(1, abi.RULE_DTYPE)
+    r["id"] = rid
+    r["group"] = rid if group is None else group
+    r["first_partner_type"] = first
+    r["second_partner_type"] = second
+    r["first_partner_state"] = first_state
+    r["second_partner_state"] = second_state
+    r["set_state"] = set_state
+    r["wait_for_state"] = wait_for_state
+    r["wait_for_alignment"] = wait_for_alignment
+    r["only_via_transition"] = only_via_transition
+    r["transition_to"] = transition_to
+    r["polymerize"] = polymerize
+    r["break_after_transition"] = break_after
+    r["relative_orientation"] = rel_ori
+    r["relative_position"] = rel_pos
+    r["orientation_alignment_threshold"] = ori_thr
+    r["position_alignment_threshold"] = pos_thr
+    return r
+
+
+def baseline_rules():
+    """A + B bind when their centres pass the interaction cube (alignment gates
+    left open): one rule, group = id so each particle holds one such bond."""
+    return rule(1001, TYPE_A, TYPE_B, rel_pos=(0.0, 5.0, 0.0), ori_thr=-2.0, pos_thr=-100.0)
+
+
+def uniform_particles(rng, n, box, types, fractions=((LIPID, 0.4), (DUMMY, 0.4), (TYPE_A, 0.1), (TYPE_B, 0.1))):
+    p = blank_particles(n)
+    counts = [int(n * f) for _, f in fractions]
+    counts[1] += n - sum(counts)
+    kinds = np.concatenate([np.full(c, t, np.int32) for (t, _), c in zip(fractions, counts)])
+    kinds = rng.permutation(kinds)
+    p["id"] = np.arange(n, dtype=np.int32)
+    p["type"] = kinds
+    p["radius"] = types["radius"][kinds]
+    p["hydrophobic"] = types["hydrophobic"][kinds]
+    p["pos"] = (rng.random((n, 3)) * box).astype(np.float32)
+    p["rot"] = random_quaternions(rng, n)
+    return p
+
+
+def uniform_metabolic(rng, nm, box, types, species):
+    m = blank_particles(nm, abi.METABOLIC_DTYPE)
+    m["id"] = np.arange(nm, dtype=np.int32)
+    m["type"] = METABOLIC
+    m["radius"] = types["radius"][METABOLIC]
+    m["hydrophobic"] = types["hydrophobic"][METABOLIC]
+    m["pos"] = (rng.random((nm, 3)) * box).astype(np.float32)
+    m["rot"] = random_quaternions(rng, nm)
+    amounts = np.zeros((nm, abi.AOS_NUM_METABOLITES), np.float32)
+    # species 0 seeded as in metabolite_setup.cuh:13-28, the others random
+    amounts[:, 0] = np.where(m["pos"][:, 0] < box * 0.2, 100.0, 0.0)
+    if species > 1:
+        amounts[:, 1:species] = (rng.random((nm, species - 1)) * 10.0).astype(np.float32)
+    m["metabolites"] = amounts
+    return m
+
+
+# Measured workloads.  Each is (particles, metabolic particles, box nm, cell nm, seed).
+WORKLOADS = {
+    "plain_small": dict(n=65536, nm=131072, box=200.0, seed=1),
+    "plain_large": dict(n=2097152, nm=8388608, box=635.0, seed=2),
+}
+
+
+def workload_config(name, **overrides):
+    w = WORKLOADS[name]
+    kw = dict(num_particles=w["n"], num_metabolic_particles=w["nm"], sim_size=w["box"], grid_cell_size=6.0,
+              max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=w["seed"],
+              steps=200 if name == "plain_small" else 1000)
+    kw.update(overrides)
+    return abi.make_config(**kw)
+
+
+def build_workload(name, **overrides):
+    """Config, tables and initial state of a measured workload."""
+    cfg = workload_config(name, **overrides)
+    rng = np.random.default_rng(cfg.seed)
+    types = baseline_types()
+    rules = baseline_rules()
+    p = uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
+    m = uniform_metabolic(rng, cfg.num_metabolic_particles, cfg.sim_size, types, cfg.num_metabolites)
+    return cfg, types, rules, p, m
+
+
+# ---------------------------------------------------------------------------
+# Small scenes for differential testing: every branch of the step.
+# ---------------------------------------------------------------------------
+CHAIN_A, CHAIN_B, CHAIN_C = 40, 41, 42   # chain monomer types
+CTRL, MONO = 50, 51                       # polymerising controller and its monomer
+HALF_A, HALF_B = 60, 61                   # transition / break-after pair
+
+
+def test_types():
+    t = baseline_types()
+    for ty, r, h in [(CHAIN_A, 0.75, 0), (CHAIN_B, 0.75, 0), (CHAIN_C, 0.8, 1), (CTRL, 2.0, 0), (MONO, 1.0, 0),
+                     (HALF_A, 1.5, 1), (HALF_B, 1.7, 0)]:
+        t[ty] = (r, h)
+    return t
+
+
+def test_rules():
+    """Rules reaching every path of complexify / transitionInteractions /
+    polymerize: alignment gates, states, groups, transitions that set state,
+    break-after-transition, and a polymerising transition."""
+    rs = [
+        # A+B with real alignment gates
+        rule(1001, TYPE_A, TYPE_B, rel_pos=(0.0, 4.0, 1.0), rel_ori=(0.0, 0.38268343, 0.0, 0.92387953),
+             ori_thr=-0.3, pos_thr=-1.5, transition_to=1002),
+        # formed only by transition; sets states, then breaks after aligning
+        rule(1002, TYPE_A, TYPE_B, group=1001, first_state=1, second_state=2, only_via_transition=1,
+             transition_to=1003, rel_pos=(0.0, 4.0, 1.0), ori_thr=-0.5, pos_thr=-2.0),
+        rule(1003, TYPE_A, TYPE_B, group=1001, only_via_transition=1, break_after=1, rel_pos=(0.0, 4.0, 1.0)),
+        # homotypic rule without group (may be granted twice)
+        rule(1010, HALF_A, HALF_A, group=-1, rel_pos=(0.0, 3.0, 0.0), ori_thr=-1.0, pos_thr=-3.0),
+        # HALF_A + HALF_B with state requirement
+        rule(1011, HALF_A, HALF_B, first_state=0, second_state=-1, rel_pos=(3.2, 0.0, 0.0), ori_thr=-0.8,
+             pos_thr=-3.0, transition_to=1012),
+        rule(1012, HALF_A, HALF_B, group=1011, first_state=3, second_state=-1, only_via_transition=1,
+             wait_for_alignment=0, rel_pos=(3.2, 0.0, 0.0)),
+        # polymerisation: controller binds a monomer, a transition schedules a new monomer
+        rule(1020, CTRL, MONO, group=1020, rel_pos=(0.0, 3.0, 0.0), ori_thr=-1.0, pos_thr=-4.0,
+             transition_to=1021),
+        rule(1021, CTRL, MONO, group=1020, first_state=1, only_via_transition=1, polymerize=1022,
+             transition_to=1023, wait_for_alignment=0, rel_pos=(0.0, 3.0, 0.0)),
+        rule(1022, CTRL, MONO, group=1020, only_via_transition=1, rel_pos=(0.0, 3.0, 0.0),
+             rel_ori=(0.0, 0.0, 0.0, 1.0)),
+        rule(1023, CTRL, MONO, group=1020, first_state=2, only_via_transition=1, wait_for_alignment=0,
+             rel_pos=(0.0, 3.0, 0.0)),
+    ]
+    out = np.zeros(len(rs), abi.RULE_DTYPE)   # (np.concatenate would drop the padded layout)
+    for i, r in enumerate(rs):
+        out[i] = r[0]
+    return out
+
+
+def _link_serially(p, start, end, itype=abi.INTERACTION_TYPE_CHAIN):
+    """linkParticlesSerially (setup/interaction_setup.cuh:13-42)."""
+    for i in range(start + 1, end):
+        a, b = p[i - 1], p[i]
+        k = a["n_active_interactions"]
+        a["interactions"][k] = (itype, abi.INTERACTION_GROUP_FORWARD, b["id"])
+        a["n_active_interactions"] = k + 1
+        k = b["n_active_interactions"]
+        b["interactions"][k] = (itype, abi.INTERACTION_GROUP_BACKWARD, a["id"])
+        b["n_active_interactions"] = k + 1
+
+
+def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
+    """A dense small box with uniform particles of all kinds, a few wrapped
+    chains, pre-bonded rule pairs, a test bond, and metabolites.  Returns
+    (config, types, rules, particles, metabolic, next_particle_id)."""
+    rng = np.random.default_rng(seed)
+    types = test_types()
+    rules = test_rules()
+    kinds = np.array([LIPID, DUMMY, TYPE_A, TYPE_B, HALF_A, HALF_B, CTRL, MONO, CHAIN_C])
+    weights = np.array([0.35, 0.2, 0.1, 0.1, 0.06, 0.06, 0.04, 0.05, 0.04])
+    p = blank_particles(n)
+    ty = rng.choice(kinds, size=n, p=weights / weights.sum()).astype(np.int32)
+    p["id"] = np.arange(n, dtype=np.int32)
+    p["type"] = ty
+    p["radius"] = types["radius"][ty]
+    p["hydrophobic"] = types["hydrophobic"][ty]
+    p["pos"] = (rng.random((n, 3)) * box).astype(np.float32)
+    p["rot"] = random_quaternions(rng, n)
+    p["velocity"] = (rng.normal(size=(n, 3)) * 0.2).astype(np.float32)
+    p["angular_velocity"] = random_quaternions(rng, n)
+    p["angular_velocity"][:, 3] += 8.0           # near-identity angular velocities
+    p["angular_velocity"] /= np.linalg.norm(p["angular_velocity"], axis=1, keepdims=True)
+    p["state"] = rng.choice([0, 0, 0, 1, 2, 3], size=n)
+    # chains: consecutive ids placed along a random walk
+    pos = 0
+    for c in range(6):
+        length = 8
+        start = 100 + c * 20
+        q = rng.random(3) * (box - 12) + 6
+        step = rng.normal(size=3)
+        step /= np.linalg.norm(step)
+        for i in range(start, start + length):
+            p[i]["type"] = CHAIN_A if (i - start) % 2 == 0 else CHAIN_B
+            p[i]["radius"] = types["radius"][p[i]["type"]]
+            p[i]["hydrophobic"] = 0
+            p[i]["pos"] = (q + step * 1.5 * (i - start)).astype(np.float32)
+        _link_serially(p, start, start + length)
+    # rule bonds already formed (both directions), including one that transitions
+    for k in range(10):
+        a, b = 300 + 2 * k, 301 + 2 * k
+        p[a]["type"], p[b]["type"] = (TYPE_A, TYPE_B) if k % 2 == 0 else (CTRL, MONO)
+        for i in (a, b):
+            p[i]["radius"] = types["radius"][p[i]["type"]]
+            p[i]["hydrophobic"] = 0
+        p[b]["pos"] = (p[a]["pos"] + rng.normal(size=3).astype(np.float32) * 1.5).clip(0, box)
+        rid = 1001 if k % 2 == 0 else 1020
+        for i, j in ((a, b), (b, a)):
+            kk = p[i]["n_active_interactions"]
+            p[i]["interactions"][kk] = (rid, 1001 if rid == 1001 else 1020, p[j]["id"])
+            p[i]["n_active_interactions"] = kk + 1
+        if k % 2 == 1:
+            p[a]["state"] = 1
+    # a test bond (interaction type 0) between two close particles
+    p[400]["pos"] = p[401]["pos"] + np.float32(2.0)
+    for i, j in ((400, 401), (401, 400)):
+        kk = p[i]["n_active_interactions"]
+        p[i]["interactions"][kk] = (0, -1, p[j]["id"])
+        p[i]["n_active_interactions"] = kk + 1
+    p["pos"] = p["pos"].clip(0, box)
+    m = uniform_metabolic(rng, nm, box, types, species)
+    m["velocity"] = (rng.normal(size=(nm, 3)) * 0.3).astype(np.float32)
+    cfg = abi.make_config(num_particles=n + capacity_slack, num_metabolic_particles=nm + 16, sim_size=box,
+                          grid_cell_size=6.0, max_interaction_distance=5.5, max_diffusion_distance=6.0,
+                          num_metabolites=species, seed=1000 + seed, noise_coordination_steps=4,
+                          relaxation_steps=6, metabolite_diffusion_steps=3, steps=10)
+    return cfg, types, rules, p, m, n
