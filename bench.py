@@ -1,0 +1,330 @@
+"""Throughput of the spatial_cell_sim step on one GB300 (particle-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plain_large|plain_small]
+
+A step is one iteration of the reference's step loop (main.cu:347-661) with
+16 noise-coordination, 32 relaxation and 8 diffusion sub-iterations; the
+metric counts particles plus metabolic particles per step.  The default
+workload is the single large instance: 2,097,152 particles (lipid / dummy /
+A / B = 40 / 40 / 10 / 10 %) and 8,388,608 metabolic particles of 8 species
+in a 635 nm box, 6 nm cells, seeded synthetic state (no dataset exists).
+
+``--impl ours`` prints one JSON line:
+  value     device-resident step throughput (CUDA events on the sim's stream,
+            state already in HBM; inputs of several GB, larger than L2);
+  e2e       the same through the C ABI with host buffers: sc_load_state from
+            pinned host memory, then per step sc_step + sc_reduce_frame into
+            pinned host memory (the frames.dat payload, persisted every step
+            as the reference does);
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+            measured launch time, against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (oracle/scport.cpp, OpenMP on all host cores)
+            timed on a same-density sub-box of the workload.
+``--impl reference`` times that CPU implementation alone (the reference has
+no CPU path of its own and its GPU build cannot be made on this machine).
+Under torchrun, every rank runs an independent replica (the path does not
+shard); value is the sum over ranks of items per step over the slowest rank.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from spatial_cell_gb300 import abi, scenes  # noqa: E402
+
+METRIC = "particle-steps/s on 1 GB300, batched vs plain at tol; serving p50/p99 latency"
+UNIT = "particle-steps/s"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# Algorithmic HBM bytes per launch of the step's kernels: each field a kernel
+# needs read once and each field it produces written once, neighbour data
+# served on chip (per-item figures of the measurement plan).
+def algorithmic_bytes(phase, N, Nm, S, bbar=0.0):
+    return {
+        "relax": N * (104 + 12 * bbar),
+        "relax_metab": Nm * 44 + N * 32,
+        "relax_partners": N * 44 + Nm * 32,
+        "diffuse": Nm * (16 + 8 * S),
+        "coordinate_noise": N * (84 + 12 * bbar),
+    }.get(phase)
+
+
+PHASES = {
+    "relax": abi.PHASE_RELAX,
+    "relax_metab": abi.PHASE_RELAX_METAB,
+    "relax_partners": abi.PHASE_RELAX_PARTNERS,
+    "diffuse": abi.PHASE_DIFFUSE,
+    "coordinate_noise": abi.PHASE_COORDINATE_NOISE,
+    "complexify": abi.PHASE_COMPLEXIFY,
+    "transition": abi.PHASE_TRANSITION,
+    "apply_velocities": abi.PHASE_APPLY_VELOCITIES,
+}
+
+
+def per_phase_times(sim, stream, torch, reps=3):
+    """Average device time of one launch of each neighbour phase (CUDA events
+    on the sim's stream).  Phases that double-buffer are run in pairs so the
+    state's buffer parity is unchanged afterwards."""
+    out = {}
+    for name, ph in PHASES.items():
+        if name in ("complexify", "transition", "apply_velocities"):
+            continue  # change the state; timed as part of the step only
+        sim.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2 * reps):
+            sim.run_phase(ph, 0)
+        e1.record(stream)
+        e1.synchronize()
+        out[name] = e0.elapsed_time(e1) / (2 * reps)
+    return out
+
+
+def cpu_sample(args, reps=1):
+    """Times the CPU oracle on a same-density sub-box of the workload."""
+    from oracle import engine as oengine
+    frac = args.cpu_fraction
+    cfg0 = scenes.workload_config(args.workload)
+    n = max(1024, int(cfg0.num_particles * frac))
+    nm = max(1024, int(cfg0.num_metabolic_particles * frac))
+    box = float(cfg0.sim_size * frac ** (1.0 / 3.0))
+    cfg = scenes.workload_config(args.workload, num_particles=n, num_metabolic_particles=nm, sim_size=box)
+    rng = np.random.default_rng(cfg.seed)
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    p = scenes.uniform_particles(rng, n, box, types)
+    m = scenes.uniform_metabolic(rng, nm, box, types, cfg.num_metabolites)
+    e = oengine.OracleEngine("port", cfg, types, rules)
+    e.load_state(p, m)
+    e.prepare()
+    threads = oengine.max_threads()
+    t0 = time.perf_counter()
+    e.step(reps)
+    dt = time.perf_counter() - t0
+    e.close()
+    rate = (n + nm) * reps / dt
+    sample = (f"{reps} step(s) of a {frac:.4g}-volume sub-box at the workload's density "
+              f"({n} + {nm} items, {box:.1f} nm), {dt:.1f} s")
+    return rate, threads, sample
+
+
+def run_reference(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    rate, threads, sample = cpu_sample(args, reps=max(1, args.steps if args.steps <= 2 else 1))
+    cfg = scenes.workload_config(args.workload)
+    line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; no dataset in the reference)",
+            "config": {"workload": args.workload, "particles": cfg.num_particles,
+                       "metabolic_particles": cfg.num_metabolic_particles, "box_nm": cfg.sim_size,
+                       "cell_nm": cfg.grid_cell_size, "species": cfg.num_metabolites},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from spatial_cell_gb300 import build, native
+
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build.build()
+    cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=scenes.WORKLOADS[args.workload]["seed"] + rank)
+    N, Nm, S = cfg.num_particles, cfg.num_metabolic_particles, cfg.num_metabolites
+    items = N + Nm
+    # pinned host buffers for the end-to-end leg
+    p_host = torch.empty(p.nbytes, dtype=torch.uint8, pin_memory=True)
+    m_host = torch.empty(m.nbytes, dtype=torch.uint8, pin_memory=True)
+    p_host.numpy()[:] = p.view(np.uint8)
+    m_host.numpy()[:] = m.view(np.uint8)
+    rp_host = torch.empty(N * abi.REDUCED_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    rm_host = torch.empty(Nm * abi.REDUCED_METABOLIC_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+
+    sim = native.Simulation(cfg, types, rules)
+    stream = torch.cuda.ExternalStream(sim.stream_handle())
+    sim.load_state(p, m)
+    sim.prepare()
+    for _ in range(args.warmup):
+        sim.step(1)
+    sim.sync()
+
+    # device-resident timing
+    launches0 = sim.counters().kernel_launches
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    sim.sync()
+    launches = sim.counters().kernel_launches - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = items * world * args.steps / (ms / 1e3)
+
+    # per-phase breakdown (for the roofline of the dominant kernel)
+    phase_ms = per_phase_times(sim, stream, torch)
+    counts = {"relax": cfg.relaxation_steps, "relax_metab": (cfg.relaxation_steps + 1) // 2,
+              "relax_partners": (cfg.relaxation_steps + 1) // 2, "diffuse": cfg.metabolite_diffusion_steps,
+              "coordinate_noise": cfg.noise_coordination_steps}
+    share = {k: phase_ms[k] * counts[k] / ms_per_step for k in phase_ms}
+    dom = max(share, key=share.get)
+    exp_p, _ = sim.export_state()
+    bbar = float(np.clip(exp_p["n_active_interactions"], 0, 8).mean())
+    peak, peak_kind = _measured_peaks()
+    alg = algorithmic_bytes(dom, N, Nm, S, bbar)
+    achieved = alg / (phase_ms[dom] / 1e3) / 1e9
+
+    # end to end through the C ABI with host buffers
+    sim2 = native.Simulation(cfg, types, rules)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim2.load_state_ptr(ctypes.c_void_p(p_host.data_ptr()), N, ctypes.c_void_p(m_host.data_ptr()), Nm, 0, N)
+    sim2.prepare()
+    for _ in range(args.steps):
+        sim2.step(1)
+        sim2.reduce_frame_ptr(ctypes.c_void_p(rp_host.data_ptr()), ctypes.c_void_p(rm_host.data_ptr()))
+    sim2.sync()
+    e2e_s = time.perf_counter() - t0
+    sim2.close()
+    e2e = {"value": items * world * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int((p.nbytes + m.nbytes) / args.steps),
+           "d2h_bytes_per_step": int(rp_host.numel() + rm_host.numel()),
+           "includes": "sc_load_state of the initial AoS state + sc_prepare, then per step sc_step + "
+                       "sc_reduce_frame to pinned host memory"}
+    sim.close()
+
+    line = None
+    if rank == 0:
+        cpu_rate, cpu_threads, cpu_desc = cpu_sample(args) if not args.no_cpu else (None, 0, "skipped")
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded; no dataset in the reference)",
+            "config": {"workload": args.workload, "particles": N, "metabolic_particles": Nm,
+                       "box_nm": cfg.sim_size, "cell_nm": cfg.grid_cell_size, "species": S,
+                       "sub_iterations": [cfg.noise_coordination_steps, cfg.relaxation_steps,
+                                          cfg.metabolite_diffusion_steps],
+                       "l2": "inputs larger than L2 (state of several GB)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_launch": alg, "launch_ms": phase_ms[dom]},
+            "phase_ms_per_launch": phase_ms, "phase_share_of_step": share,
+            "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                             "sample": cpu_desc},
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain_large", choices=sorted(scenes.WORKLOADS))
+    ap.add_argument("--cpu-fraction", type=float, default=1.0 / 16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

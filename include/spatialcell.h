@@ -271,6 +271,9 @@ int sc_export_state(sc_sim *sim, sc_particle *particles, sc_metabolic_particle *
  * of every sorted slot.  Either may be NULL. */
 int sc_export_grid(sc_sim *sim, int32_t which, uint32_t *ranges, uint32_t *perm);
 int sc_get_counters(sc_sim *sim, sc_counters *out);
+/* The sim's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events after the sim's. */
+void *sc_get_stream(sc_sim *sim);
 /* The frames.dat payload of the current state (reduceParticles on the
  * counters' ranges, zero beyond), into capacity-sized host buffers. */
 int sc_reduce_frame(sc_sim *sim, sc_reduced_particle *particles,

@@ -800,6 +800,48 @@ void reduce_one(const T &p, R &r) {
 
 extern "C" {
 
+// ---- scmath.h entry points for the CPU tests ---------------------------------
+// fn: 0 sin, 1 cos, 2 acos, 3 log, 4 exp, 5 pow(x, y)
+void scp_math_eval(int fn, const float *x, const float *y, float *out, int n) {
+    for (int i = 0; i < n; i++) {
+        switch (fn) {
+            case 0: out[i] = sc_sinf(x[i]); break;
+            case 1: out[i] = sc_cosf(x[i]); break;
+            case 2: out[i] = sc_acosf(x[i]); break;
+            case 3: out[i] = sc_logf(x[i]); break;
+            case 4: out[i] = sc_expf(x[i]); break;
+            default: out[i] = sc_powf(x[i], y[i]); break;
+        }
+    }
+}
+void scp_philox(const uint32_t *ctr, uint32_t k0, uint32_t k1, uint32_t *out) {
+    sc_u4 c = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    sc_u4 o = sc_philox4x32_10(c, k0, k1);
+    out[0] = o.x; out[1] = o.y; out[2] = o.z; out[3] = o.w;
+}
+void scp_f2h(const float *x, uint16_t *out, int n) {
+    for (int i = 0; i < n; i++) out[i] = sc_f2h(x[i]);
+}
+void scp_draws(uint64_t seed, uint32_t stream, uint32_t id0, int n, uint32_t step, uint32_t d, int normal,
+               float *out) {
+    for (int i = 0; i < n; i++)
+        out[i] = normal ? sc_normal(seed, stream, id0 + (uint32_t)i, step, d)
+                        : sc_uniform(seed, stream, id0 + (uint32_t)i, step, d);
+}
+// 1 where the single-precision form of a double comparison disagrees with it.
+// kind 0: lipid range (dist, s); kind 1: diffusion threshold (x)
+void scp_compare_forms(int kind, const float *a, const float *b, uint8_t *bad, int n) {
+    for (int i = 0; i < n; i++) {
+        if (kind == 0) {
+            bool exact = (double)a[i] <= (double)b[i] + 0.8 * (double)b[i] * 0.5;
+            bad[i] = sc_within_lipid_range(a[i], b[i]) != exact;
+        } else {
+            bool exact = (double)fabsf(a[i]) > 0.001;
+            bad[i] = sc_diffuse_exceeds(a[i]) != exact;
+        }
+    }
+}
+
 void scp_set_threads(int n) {
 #if defined(_OPENMP)
     if (n > 0) omp_set_num_threads(n);

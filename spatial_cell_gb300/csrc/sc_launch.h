@@ -1,0 +1,121 @@
+// sc_launch.h -- buffers of one sim on the device and the launchers of its
+// kernels (host side of the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sc_dev.cuh"
+
+struct PFields {
+    float4 *pos, *vel, *rot, *angvel, *posnoise, *angnoise, *dbg;
+    int4 *info;   // id, type, flags, hydrophobic
+    int *state, *lscs, *spoly, *nb, *bonds;
+};
+struct MFields {
+    float4 *pos, *vel, *rot, *angvel, *posnoise, *angnoise, *dbg;
+    int4 *info;
+    int *state;
+    float4 *met;  // SP floats per item
+    int *orig;
+};
+
+// Particle / metabolic field indices for the current-buffer table.
+enum { FP_POS, FP_VEL, FP_ROT, FP_ANGVEL, FP_POSNOISE, FP_ANGNOISE, FP_DBG, FP_INFO, FP_STATE, FP_LSCS, FP_SPOLY,
+       FP_NB, FP_BONDS, FP_COUNT };
+enum { FM_POS, FM_VEL, FM_ROT, FM_ANGVEL, FM_POSNOISE, FM_ANGNOISE, FM_DBG, FM_INFO, FM_STATE, FM_MET, FM_ORIG,
+       FM_COUNT };
+
+struct ScBuffers {
+    PFields p[2];
+    MFields m[2];
+    int cp[FP_COUNT];   // current buffer of each particle field
+    int cm[FM_COUNT];   // current buffer of each metabolic field
+    // metabolic fields no step kernel touches, in load order (indexed by orig)
+    int *mcLscs, *mcSpoly, *mcNb, *mcBonds;
+    // binning: keys / slot values ping-pong per item set, the buffer of the
+    // last pass holding the sorted keys and the permutation
+    uint32_t *keysP[2], *valsP[2], *keysM[2], *valsM[2], *hist, *lookback;
+    int sortCurP, sortCurM;
+    uint32_t *cellStartP, *cellStartM;
+    // polymerisation list
+    int *polyList;
+    int polyCap;
+    ScCounters *ctr;
+    // frames
+    sc_reduced_particle *redP;
+    sc_reduced_metabolic_particle *redM;
+
+    // current view of every particle / metabolic field
+    PFields P() const {
+        PFields f;
+        f.pos = p[cp[FP_POS]].pos; f.vel = p[cp[FP_VEL]].vel; f.rot = p[cp[FP_ROT]].rot;
+        f.angvel = p[cp[FP_ANGVEL]].angvel; f.posnoise = p[cp[FP_POSNOISE]].posnoise;
+        f.angnoise = p[cp[FP_ANGNOISE]].angnoise; f.dbg = p[cp[FP_DBG]].dbg; f.info = p[cp[FP_INFO]].info;
+        f.state = p[cp[FP_STATE]].state; f.lscs = p[cp[FP_LSCS]].lscs; f.spoly = p[cp[FP_SPOLY]].spoly;
+        f.nb = p[cp[FP_NB]].nb; f.bonds = p[cp[FP_BONDS]].bonds;
+        return f;
+    }
+    PFields Pnext() const {
+        PFields f;
+        f.pos = p[1 - cp[FP_POS]].pos; f.vel = p[1 - cp[FP_VEL]].vel; f.rot = p[1 - cp[FP_ROT]].rot;
+        f.angvel = p[1 - cp[FP_ANGVEL]].angvel; f.posnoise = p[1 - cp[FP_POSNOISE]].posnoise;
+        f.angnoise = p[1 - cp[FP_ANGNOISE]].angnoise; f.dbg = p[1 - cp[FP_DBG]].dbg;
+        f.info = p[1 - cp[FP_INFO]].info; f.state = p[1 - cp[FP_STATE]].state;
+        f.lscs = p[1 - cp[FP_LSCS]].lscs; f.spoly = p[1 - cp[FP_SPOLY]].spoly; f.nb = p[1 - cp[FP_NB]].nb;
+        f.bonds = p[1 - cp[FP_BONDS]].bonds;
+        return f;
+    }
+    MFields M() const {
+        MFields f;
+        f.pos = m[cm[FM_POS]].pos; f.vel = m[cm[FM_VEL]].vel; f.rot = m[cm[FM_ROT]].rot;
+        f.angvel = m[cm[FM_ANGVEL]].angvel; f.posnoise = m[cm[FM_POSNOISE]].posnoise;
+        f.angnoise = m[cm[FM_ANGNOISE]].angnoise; f.dbg = m[cm[FM_DBG]].dbg; f.info = m[cm[FM_INFO]].info;
+        f.state = m[cm[FM_STATE]].state; f.met = m[cm[FM_MET]].met; f.orig = m[cm[FM_ORIG]].orig;
+        return f;
+    }
+    MFields Mnext() const {
+        MFields f;
+        f.pos = m[1 - cm[FM_POS]].pos; f.vel = m[1 - cm[FM_VEL]].vel; f.rot = m[1 - cm[FM_ROT]].rot;
+        f.angvel = m[1 - cm[FM_ANGVEL]].angvel; f.posnoise = m[1 - cm[FM_POSNOISE]].posnoise;
+        f.angnoise = m[1 - cm[FM_ANGNOISE]].angnoise; f.dbg = m[1 - cm[FM_DBG]].dbg;
+        f.info = m[1 - cm[FM_INFO]].info; f.state = m[1 - cm[FM_STATE]].state; f.met = m[1 - cm[FM_MET]].met;
+        f.orig = m[1 - cm[FM_ORIG]].orig;
+        return f;
+    }
+    void flipAllP() { for (int k = 0; k < FP_COUNT; k++) cp[k] ^= 1; }
+    void flipAllM() { for (int k = 0; k < FM_COUNT; k++) cm[k] ^= 1; }
+};
+
+// sc_grid.cu
+int sc_sort_passes(int bits);
+size_t sc_sort_lookback_words(int cap);
+int sc_launch_sort(cudaStream_t st, const float4 *pos, const int4 *info, int n, const ScParams &P, uint32_t *keys[2],
+                   uint32_t *vals[2], uint32_t *hist, uint32_t *lookback, ScCounters *ctr, long long *launches);
+void sc_launch_cell_start(cudaStream_t st, const uint32_t *keys, int n, uint32_t cells, uint32_t *cellStart,
+                          long long *launches);
+void sc_launch_gather_particles(cudaStream_t st, const uint32_t *perm, int n, const PFields &src, const PFields &dst,
+                                long long *launches);
+void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, const MFields &src,
+                                const MFields &dst, long long *launches);
+
+// sc_step.cu: one launcher per reference phase (include/spatialcell.h, sc_phase)
+struct ScLaunchCtx {
+    cudaStream_t st;
+    ScParams P;
+    ScBuffers *B;
+    long long *launches;
+};
+void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic);
+void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac);
+void sc_phase_apply_noise(ScLaunchCtx &c);
+void sc_phase_relax(ScLaunchCtx &c);
+void sc_phase_relax_metab(ScLaunchCtx &c);
+void sc_phase_relax_partners(ScLaunchCtx &c);
+void sc_phase_apply_velocities(ScLaunchCtx &c);
+void sc_phase_complexify(ScLaunchCtx &c);
+void sc_phase_transition(ScLaunchCtx &c);
+void sc_phase_polymerize(ScLaunchCtx &c);
+void sc_phase_diffuse(ScLaunchCtx &c);
+void sc_phase_remove_interfering(ScLaunchCtx &c);
+void sc_phase_reduce(ScLaunchCtx &c);

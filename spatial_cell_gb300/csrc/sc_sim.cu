@@ -1,0 +1,612 @@
+// sc_sim.cu -- the C ABI of include/spatialcell.h: one sim = its device
+// buffers, one CUDA stream and the launch sequence of the step loop
+// (main.cu:347-661), with no host synchronisation inside a step.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sc_launch.h"
+
+extern "C" const char *sc_host_last_error(void);
+
+namespace {
+
+thread_local std::string g_err;
+
+// ---- AoS <-> SoA (device side; the host buffers move in one copy) -----------
+// Byte offsets of the reference's Particle (types.cuh:173-222).
+__device__ __forceinline__ float4 rd4(const uint8_t *r, int off) { return *(const float4 *)(r + off); }
+__device__ __forceinline__ float rdf(const uint8_t *r, int off) { return *(const float *)(r + off); }
+__device__ __forceinline__ int rdi(const uint8_t *r, int off) { return *(const int *)(r + off); }
+__device__ __forceinline__ int rdb(const uint8_t *r, int off) { return (int)*(const int8_t *)(r + off); }
+
+__global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int cap, PFields F) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    if (i >= n) {
+        F.pos[i] = F.vel[i] = F.rot[i] = F.angvel[i] = F.posnoise[i] = F.angnoise[i] = F.dbg[i] = make_float4(0, 0, 0, 0);
+        F.info[i] = make_int4(0, 0, 0, 0);
+        F.state[i] = F.lscs[i] = F.spoly[i] = F.nb[i] = 0;
+        return;
+    }
+    const uint8_t *r = aos + (size_t)i * 256;
+    F.info[i] = make_int4(rdi(r, 0), rdi(r, 4), rdi(r, 8), rdb(r, 24));
+    F.state[i] = rdb(r, 12);
+    F.lscs[i] = rdi(r, 16);
+    F.pos[i] = make_float4(rdf(r, 28), rdf(r, 32), rdf(r, 36), rdf(r, 20));
+    F.rot[i] = rd4(r, 48);
+    F.vel[i] = make_float4(rdf(r, 64), rdf(r, 68), rdf(r, 72), 0.0f);
+    F.posnoise[i] = make_float4(rdf(r, 76), rdf(r, 80), rdf(r, 84), 0.0f);
+    F.angvel[i] = rd4(r, 96);
+    F.angnoise[i] = rd4(r, 112);
+    int nb = rdi(r, 128);
+    F.nb[i] = nb;
+    for (int k = 0; k < 24; k++) F.bonds[(size_t)i * 24 + k] = k < 3 * min(max(nb, 0), 8) ? rdi(r, 132 + 4 * k) : 0;
+    F.spoly[i] = rdi(r, 228);
+    F.dbg[i] = rd4(r, 240);
+}
+
+__global__ void k_unpack_metabolic(const uint8_t *__restrict__ aos, int n, int cap, int SP, MFields F, int *cLscs,
+                                   int *cSpoly, int *cNb, int *cBonds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    F.orig[i] = i;
+    if (i >= n) {
+        F.pos[i] = F.vel[i] = F.rot[i] = F.angvel[i] = F.posnoise[i] = F.angnoise[i] = F.dbg[i] = make_float4(0, 0, 0, 0);
+        F.info[i] = make_int4(0, 0, 0, 0);
+        F.state[i] = 0;
+        cLscs[i] = cSpoly[i] = cNb[i] = 0;
+        for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = 0;
+        for (int q = 0; q < SP / 4; q++) F.met[(size_t)i * (SP / 4) + q] = make_float4(0, 0, 0, 0);
+        return;
+    }
+    const uint8_t *r = aos + (size_t)i * 304;
+    F.info[i] = make_int4(rdi(r, 0), rdi(r, 4), rdi(r, 8), rdb(r, 24));
+    F.state[i] = rdb(r, 12);
+    cLscs[i] = rdi(r, 16);
+    F.pos[i] = make_float4(rdf(r, 28), rdf(r, 32), rdf(r, 36), rdf(r, 20));
+    F.rot[i] = rd4(r, 48);
+    F.vel[i] = make_float4(rdf(r, 64), rdf(r, 68), rdf(r, 72), 0.0f);
+    F.posnoise[i] = make_float4(rdf(r, 76), rdf(r, 80), rdf(r, 84), 0.0f);
+    F.angvel[i] = rd4(r, 96);
+    F.angnoise[i] = rd4(r, 112);
+    int nb = rdi(r, 128);
+    cNb[i] = nb;
+    for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = k < 3 * min(max(nb, 0), 8) ? rdi(r, 132 + 4 * k) : 0;
+    cSpoly[i] = rdi(r, 228);
+    F.dbg[i] = rd4(r, 240);
+    float *met = (float *)(F.met) + (size_t)i * SP;
+    for (int k = 0; k < SP; k++) met[k] = k < SC_AOS_NUM_METABOLITES ? rdf(r, 256 + 4 * k) : 0.0f;
+}
+
+__device__ __forceinline__ void wr4(uint8_t *r, int off, float4 v) { *(float4 *)(r + off) = v; }
+__device__ __forceinline__ void wrf(uint8_t *r, int off, float v) { *(float *)(r + off) = v; }
+__device__ __forceinline__ void wri(uint8_t *r, int off, int v) { *(int *)(r + off) = v; }
+
+__device__ void pack_common(uint8_t *r, int4 in, int state, int lscs, float4 pos, float4 rot, float4 vel, float4 pn,
+                            float4 av, float4 an, int nb, const int *bonds, int spoly, float4 dbg) {
+    for (int k = 0; k < 256; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
+    wri(r, 0, in.x); wri(r, 4, in.y); wri(r, 8, in.z);
+    *(int8_t *)(r + 12) = (int8_t)state;
+    wri(r, 16, lscs);
+    wrf(r, 20, pos.w);
+    *(int8_t *)(r + 24) = (int8_t)in.w;
+    wrf(r, 28, pos.x); wrf(r, 32, pos.y); wrf(r, 36, pos.z);
+    wr4(r, 48, rot);
+    wrf(r, 64, vel.x); wrf(r, 68, vel.y); wrf(r, 72, vel.z);
+    wrf(r, 76, pn.x); wrf(r, 80, pn.y); wrf(r, 84, pn.z);
+    wr4(r, 96, av);
+    wr4(r, 112, an);
+    wri(r, 128, nb);
+    int nw = 3 * min(max(nb, 0), 8);
+    for (int k = 0; k < nw; k++) wri(r, 132 + 4 * k, bonds[k]);
+    wri(r, 228, spoly);
+    wr4(r, 240, dbg);
+}
+
+__global__ void k_pack_particles(uint8_t *__restrict__ aos, const int *nActivePtr, int cap, PFields F) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    uint8_t *r = aos + (size_t)i * 256;
+    if (i >= *nActivePtr) {
+        for (int k = 0; k < 256; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
+        return;
+    }
+    pack_common(r, F.info[i], F.state[i], F.lscs[i], F.pos[i], F.rot[i], F.vel[i], F.posnoise[i], F.angvel[i],
+                F.angnoise[i], F.nb[i], F.bonds + (size_t)i * 24, F.spoly[i], F.dbg[i]);
+}
+
+__global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePtr, int cap, int SP, MFields F,
+                                 const int *cLscs, const int *cSpoly, const int *cNb, const int *cBonds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    uint8_t *r = aos + (size_t)i * 304;
+    if (i >= *nActivePtr) {
+        for (int k = 0; k < 304; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
+        return;
+    }
+    int o = F.orig[i];
+    pack_common(r, F.info[i], F.state[i], cLscs[o], F.pos[i], F.rot[i], F.vel[i], F.posnoise[i], F.angvel[i],
+                F.angnoise[i], cNb[o], cBonds + (size_t)o * 24, cSpoly[o], F.dbg[i]);
+    for (int k = 256; k < 304; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
+    const float *met = (const float *)(F.met) + (size_t)i * SP;
+    for (int k = 0; k < SC_AOS_NUM_METABOLITES && k < SP; k++) wrf(r, 256 + 4 * k, met[k]);
+}
+
+__global__ void k_after_sort(ScCounters *c) { c->lastActive = c->nActive - 1; }
+__global__ void k_end_step(ScCounters *c) { c->step++; }
+
+}  // namespace
+
+struct sc_sim {
+    sc_config cfg;
+    ScParams P;
+    ScBuffers B;
+    cudaStream_t st = nullptr;
+    int device = 0;
+    long long launches = 0;
+    std::string err;
+    std::vector<void *> allocs;
+    uint8_t *staging = nullptr;
+    size_t stagingBytes = 0;
+    bool loaded = false;
+};
+
+namespace {
+
+int set_err(sc_sim *s, int code, const std::string &m) {
+    if (s) s->err = m;
+    g_err = m;
+    return code;
+}
+
+#define SC_CK(s, call)                                                                                    \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return set_err((s), e_ == cudaErrorMemoryAllocation ? SC_E_OOM : SC_E_CUDA,                   \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+    } while (0)
+
+template <class T>
+int dalloc(sc_sim *s, T **p, size_t count) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_err(s, e == cudaErrorMemoryAllocation ? SC_E_OOM : SC_E_CUDA,
+                       "cudaMalloc of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+    }
+    s->allocs.push_back((void *)*p);
+    return SC_OK;
+}
+
+#define SC_ALLOC(s, p, n)                   \
+    do {                                    \
+        int rc_ = dalloc((s), &(p), (n));   \
+        if (rc_) return rc_;                \
+    } while (0)
+
+inline int nb_of(long long n) { return (int)((n + SC_THREADS - 1) / SC_THREADS); }
+
+ScLaunchCtx ctx(sc_sim *s) {
+    ScLaunchCtx c;
+    c.st = s->st;
+    c.P = s->P;
+    c.B = &s->B;
+    c.launches = &s->launches;
+    return c;
+}
+
+int check_launch(sc_sim *s) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(s, SC_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return SC_OK;
+}
+
+void sort_particles(sc_sim *s) {
+    ScBuffers &B = s->B;
+    const int N = s->P.N;
+    PFields F = B.P();
+    int cur = sc_launch_sort(s->st, F.pos, F.info, N, s->P, B.keysP, B.valsP, B.hist, B.lookback, B.ctr, &s->launches);
+    B.sortCurP = cur;
+    sc_launch_cell_start(s->st, B.keysP[cur], N, s->P.cells, B.cellStartP, &s->launches);
+    sc_launch_gather_particles(s->st, B.valsP[cur], N, B.P(), B.Pnext(), &s->launches);
+    B.flipAllP();
+    k_after_sort<<<1, 1, 0, s->st>>>(B.ctr);
+    s->launches++;
+}
+
+void sort_metabolic(sc_sim *s) {
+    ScBuffers &B = s->B;
+    const int Nm = s->P.Nm;
+    MFields F = B.M();
+    int cur = sc_launch_sort(s->st, F.pos, F.info, Nm, s->P, B.keysM, B.valsM, B.hist, B.lookback, B.ctr, &s->launches);
+    B.sortCurM = cur;
+    sc_launch_cell_start(s->st, B.keysM[cur], Nm, s->P.cells, B.cellStartM, &s->launches);
+    sc_launch_gather_metabolic(s->st, B.valsM[cur], Nm, s->P.SP / 4, B.M(), B.Mnext(), &s->launches);
+    B.flipAllM();
+}
+
+int run_phase(sc_sim *s, int phase, int arg) {
+    ScLaunchCtx c = ctx(s);
+    switch (phase) {
+        case SC_PHASE_SORT_PARTICLES: sort_particles(s); break;
+        case SC_PHASE_SORT_METABOLIC: sort_metabolic(s); break;
+        case SC_PHASE_MOVE_BROWNIAN: sc_phase_move_brownian(c, false); break;
+        case SC_PHASE_MOVE_BROWNIAN_METAB: sc_phase_move_brownian(c, true); break;
+        case SC_PHASE_COORDINATE_NOISE:
+            sc_phase_coordinate_noise(c, (float)arg / s->cfg.noise_coordination_steps);
+            break;
+        case SC_PHASE_APPLY_NOISE: sc_phase_apply_noise(c); break;
+        case SC_PHASE_RELAX: sc_phase_relax(c); break;
+        case SC_PHASE_RELAX_METAB: sc_phase_relax_metab(c); break;
+        case SC_PHASE_RELAX_PARTNERS: sc_phase_relax_partners(c); break;
+        case SC_PHASE_APPLY_VELOCITIES: sc_phase_apply_velocities(c); break;
+        case SC_PHASE_COMPLEXIFY: sc_phase_complexify(c); break;
+        case SC_PHASE_TRANSITION: sc_phase_transition(c); break;
+        case SC_PHASE_POLYMERIZE: sc_phase_polymerize(c); break;
+        case SC_PHASE_DIFFUSE: sc_phase_diffuse(c); break;
+        case SC_PHASE_REMOVE_INTERFERING: sc_phase_remove_interfering(c); break;
+        case SC_PHASE_END_STEP:
+            k_end_step<<<1, 1, 0, s->st>>>(s->B.ctr);
+            s->launches++;
+            break;
+        default: return set_err(s, SC_E_INVALID, "unknown phase " + std::to_string(phase));
+    }
+    return check_launch(s);
+}
+
+int ensure_staging(sc_sim *s, size_t bytes) {
+    if (s->stagingBytes >= bytes) return SC_OK;
+    if (s->staging) {
+        cudaFree(s->staging);
+        s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->staging));
+        s->staging = nullptr;
+        s->stagingBytes = 0;
+    }
+    int rc = dalloc(s, &s->staging, bytes);
+    if (rc) return rc;
+    s->stagingBytes = bytes;
+    return SC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sc_last_error(const sc_sim *sim) {
+    if (sim) return sim->err.c_str();
+    if (!g_err.empty()) return g_err.c_str();
+    return sc_host_last_error();
+}
+
+int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, const sc_rule *rules, int32_t n_rules,
+              sc_sim **out) {
+    if (!cfg || !out) return set_err(nullptr, SC_E_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->num_particles < 0 || cfg->num_metabolic_particles < 0)
+        return set_err(nullptr, SC_E_INVALID, "negative capacity");
+    if (cfg->num_metabolites < 1 || cfg->num_metabolites > SC_AOS_NUM_METABOLITES)
+        return set_err(nullptr, SC_E_INVALID, "num_metabolites must be in 1..10");
+    if (n_types < 0 || n_rules < 0 || (n_types > 0 && !types) || (n_rules > 0 && !rules))
+        return set_err(nullptr, SC_E_INVALID, "bad table arguments");
+    int32_t ngrid = 0, bits = 0;
+    if (sc_config_grid(cfg, &ngrid, &bits) != SC_OK) return set_err(nullptr, SC_E_INVALID, sc_host_last_error());
+    if (!(cfg->max_interaction_distance >= 0.0f) || !(cfg->max_diffusion_distance >= 0.0f))
+        return set_err(nullptr, SC_E_INVALID, "negative interaction distance");
+    if (cfg->noise_coordination_steps < 0 || cfg->relaxation_steps < 0 || cfg->metabolite_diffusion_steps < 0)
+        return set_err(nullptr, SC_E_INVALID, "negative sub-iteration count");
+
+    sc_sim *s = new sc_sim();
+    s->cfg = *cfg;
+    cudaGetDevice(&s->device);
+    ScParams &P = s->P;
+    memset(&P, 0, sizeof P);
+    P.simSize = cfg->sim_size;
+    P.maxInt = cfg->max_interaction_distance;
+    P.maxDiff = cfg->max_diffusion_distance;
+    P.cell = cfg->grid_cell_size;
+    P.ngrid = ngrid;
+    P.bits = bits;
+    P.cells = (uint32_t)ngrid * (uint32_t)ngrid * (uint32_t)ngrid;
+    P.moveNoise = cfg->movement_noise_scale;
+    P.rotNoise = cfg->rotation_noise_scale;
+    P.metabNoise = cfg->metabolite_movement_noise_scale;
+    P.velDecay = cfg->velocity_decay;
+    P.angDecay = cfg->angular_velocity_decay;
+    P.S = cfg->num_metabolites;
+    P.SP = P.S <= 4 ? 4 : P.S <= 8 ? 8 : 12;
+    P.N = cfg->num_particles;
+    P.Nm = cfg->num_metabolic_particles;
+    P.coordSteps = cfg->noise_coordination_steps;
+    P.seed = cfg->seed;
+
+    auto bail = [&](int rc) {
+        sc_destroy(s);
+        return rc;
+    };
+    // tables: id-indexed rules + zero rule, partner index, partner-mapped rules
+    // (interactions.cuh:59-145; ascending rule id within a type)
+    int maxId = 0;
+    for (int i = 0; i < n_rules; i++) maxId = std::max(maxId, rules[i].id);
+    std::vector<sc_rule> flat((size_t)maxId + 2);
+    memset(flat.data(), 0, flat.size() * sizeof(sc_rule));
+    std::vector<char> seen((size_t)maxId + 1, 0);
+    for (int i = 0; i < n_rules; i++) {
+        int id = rules[i].id;
+        if (id < 0 || seen[(size_t)id]) continue;
+        seen[(size_t)id] = 1;
+        flat[(size_t)id] = rules[i];
+    }
+    std::map<int, std::vector<int>> byType;
+    for (int id = 0; id <= maxId; id++) {
+        if (!seen[(size_t)id]) continue;
+        if (flat[(size_t)id].first_partner_type >= 0) byType[flat[(size_t)id].first_partner_type].push_back(id);
+        if (flat[(size_t)id].second_partner_type >= 0) byType[flat[(size_t)id].second_partner_type].push_back(id);
+    }
+    std::vector<int> pidx(((size_t)maxId + 1) * 2, 0);
+    std::vector<sc_rule> prules;
+    for (auto &kv : byType) {
+        int start = (int)prules.size();
+        for (int id : kv.second) prules.push_back(flat[(size_t)id]);
+        if ((size_t)kv.first * 2 + 1 < pidx.size()) {
+            pidx[(size_t)kv.first * 2] = start;
+            pidx[(size_t)kv.first * 2 + 1] = (int)prules.size();
+        }
+    }
+    sc_rule *dFlat = nullptr, *dPrules = nullptr;
+    int *dPidx = nullptr;
+    sc_type_info *dTypes = nullptr;
+    int rc;
+    if ((rc = dalloc(s, &dFlat, flat.size())) || (rc = dalloc(s, &dPidx, pidx.size())) ||
+        (rc = dalloc(s, &dPrules, std::max<size_t>(prules.size(), 1))) ||
+        (rc = dalloc(s, &dTypes, std::max<int>(n_types, 1))))
+        return bail(rc);
+    cudaMemcpy(dFlat, flat.data(), flat.size() * sizeof(sc_rule), cudaMemcpyHostToDevice);
+    cudaMemcpy(dPidx, pidx.data(), pidx.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (!prules.empty()) cudaMemcpy(dPrules, prules.data(), prules.size() * sizeof(sc_rule), cudaMemcpyHostToDevice);
+    if (n_types > 0) cudaMemcpy(dTypes, types, (size_t)n_types * sizeof(sc_type_info), cudaMemcpyHostToDevice);
+    P.flat = dFlat;
+    P.nFlat = maxId + 1;
+    P.pidx = dPidx;
+    P.nPidx = (int)pidx.size();
+    P.prules = dPrules;
+    P.types = dTypes;
+    P.nTypes = n_types;
+
+    ScBuffers &B = s->B;
+    memset(&B, 0, sizeof B);
+    const size_t N = (size_t)P.N, Nm = (size_t)P.Nm, Q = (size_t)P.SP / 4;
+    for (int b = 0; b < 2; b++) {
+        PFields &f = B.p[b];
+        MFields &m = B.m[b];
+        if ((rc = dalloc(s, &f.pos, N)) || (rc = dalloc(s, &f.vel, N)) || (rc = dalloc(s, &f.rot, N)) ||
+            (rc = dalloc(s, &f.angvel, N)) || (rc = dalloc(s, &f.posnoise, N)) || (rc = dalloc(s, &f.angnoise, N)) ||
+            (rc = dalloc(s, &f.dbg, N)) || (rc = dalloc(s, &f.info, N)) || (rc = dalloc(s, &f.state, N)) ||
+            (rc = dalloc(s, &f.lscs, N)) || (rc = dalloc(s, &f.spoly, N)) || (rc = dalloc(s, &f.nb, N)) ||
+            (rc = dalloc(s, &f.bonds, N * 24)) || (rc = dalloc(s, &m.pos, Nm)) || (rc = dalloc(s, &m.vel, Nm)) ||
+            (rc = dalloc(s, &m.rot, Nm)) || (rc = dalloc(s, &m.angvel, Nm)) || (rc = dalloc(s, &m.posnoise, Nm)) ||
+            (rc = dalloc(s, &m.angnoise, Nm)) || (rc = dalloc(s, &m.dbg, Nm)) || (rc = dalloc(s, &m.info, Nm)) ||
+            (rc = dalloc(s, &m.state, Nm)) || (rc = dalloc(s, &m.met, Nm * Q)) || (rc = dalloc(s, &m.orig, Nm)) ||
+            (rc = dalloc(s, &B.keysP[b], N)) || (rc = dalloc(s, &B.valsP[b], N)) || (rc = dalloc(s, &B.keysM[b], Nm)) ||
+            (rc = dalloc(s, &B.valsM[b], Nm)))
+            return bail(rc);
+    }
+    const int passes = sc_sort_passes(bits);
+    if ((rc = dalloc(s, &B.mcLscs, Nm)) || (rc = dalloc(s, &B.mcSpoly, Nm)) || (rc = dalloc(s, &B.mcNb, Nm)) ||
+        (rc = dalloc(s, &B.mcBonds, Nm * 24)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
+        (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
+        (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
+        (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.redP, N)) ||
+        (rc = dalloc(s, &B.redM, Nm)))
+        return bail(rc);
+    B.polyCap = 4096;
+    cudaMemset(B.ctr, 0, sizeof(ScCounters));
+    cudaMemset(B.cellStartP, 0, ((size_t)P.cells + 1) * 4);
+    cudaMemset(B.cellStartM, 0, ((size_t)P.cells + 1) * 4);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
+    *out = s;
+    return SC_OK;
+}
+
+void sc_destroy(sc_sim *s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->st) {
+        cudaStreamSynchronize(s->st);
+        cudaStreamDestroy(s->st);
+    }
+    for (void *p : s->allocs) cudaFree(p);
+    delete s;
+}
+
+int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_metabolic_particle *metabolic,
+                  int32_t nm, int32_t step, int32_t next_particle_id) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    const int N = s->P.N, Nm = s->P.Nm;
+    if (n < 0 || nm < 0 || n > N || nm > Nm || (n > 0 && !particles) || (nm > 0 && !metabolic))
+        return set_err(s, SC_E_INVALID, "state larger than the capacity or missing");
+    for (int i = 0; i < n; i++)
+        if (particles[i].n_active_interactions < 0 || particles[i].n_active_interactions > SC_MAX_ACTIVE_INTERACTIONS)
+            return set_err(s, SC_E_INVALID, "particle " + std::to_string(i) + " has more than 8 interactions");
+    size_t bytes = std::max((size_t)n * sizeof(sc_particle), (size_t)nm * sizeof(sc_metabolic_particle));
+    int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
+    for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
+    if (N > 0) {
+        if (n) SC_CK(s, cudaMemcpyAsync(s->staging, particles, (size_t)n * sizeof(sc_particle), cudaMemcpyHostToDevice, s->st));
+        k_unpack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, n, N, B.p[0]);
+    }
+    if (Nm > 0) {
+        if (nm)
+            SC_CK(s, cudaMemcpyAsync(s->staging, metabolic, (size_t)nm * sizeof(sc_metabolic_particle),
+                                     cudaMemcpyHostToDevice, s->st));
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], B.mcLscs,
+                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+    }
+    ScCounters c;
+    memset(&c, 0, sizeof c);
+    c.nActive = n;
+    c.lastActive = n - 1;
+    c.nextId = next_particle_id;
+    c.nActiveM = nm;
+    c.step = step;
+    SC_CK(s, cudaMemcpyAsync(B.ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    rc = check_launch(s);
+    if (rc) return rc;
+    s->loaded = true;
+    return SC_OK;
+}
+
+int sc_prepare(sc_sim *s) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    cudaSetDevice(s->device);
+    int rc;
+    if ((rc = run_phase(s, SC_PHASE_SORT_PARTICLES, 0)) || (rc = run_phase(s, SC_PHASE_SORT_METABOLIC, 0)) ||
+        (rc = run_phase(s, SC_PHASE_REMOVE_INTERFERING, 0)) || (rc = run_phase(s, SC_PHASE_COMPLEXIFY, -1)))
+        return rc;
+    return SC_OK;
+}
+
+int sc_run_phase(sc_sim *s, int32_t phase, int32_t arg) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    cudaSetDevice(s->device);
+    return run_phase(s, phase, arg);
+}
+
+int sc_step(sc_sim *s, int32_t n_steps) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    if (n_steps < 0) return set_err(s, SC_E_INVALID, "negative step count");
+    cudaSetDevice(s->device);
+    const sc_config &c = s->cfg;
+    for (int k = 0; k < n_steps; k++) {
+        run_phase(s, SC_PHASE_SORT_PARTICLES, 0);
+        run_phase(s, SC_PHASE_SORT_METABOLIC, 0);
+        run_phase(s, SC_PHASE_MOVE_BROWNIAN, 0);
+        run_phase(s, SC_PHASE_MOVE_BROWNIAN_METAB, 0);
+        for (int j = 0; j < c.noise_coordination_steps; j++) run_phase(s, SC_PHASE_COORDINATE_NOISE, j);
+        run_phase(s, SC_PHASE_APPLY_NOISE, 0);
+        for (int j = 0; j < c.relaxation_steps; j++) {
+            run_phase(s, SC_PHASE_RELAX, j);
+            if (j % 2 == 0) {
+                run_phase(s, SC_PHASE_RELAX_METAB, j);
+                run_phase(s, SC_PHASE_RELAX_PARTNERS, j);
+            }
+        }
+        run_phase(s, SC_PHASE_APPLY_VELOCITIES, 0);
+        run_phase(s, SC_PHASE_COMPLEXIFY, 0);
+        run_phase(s, SC_PHASE_TRANSITION, 0);
+        run_phase(s, SC_PHASE_POLYMERIZE, 0);
+        for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
+        int rc = run_phase(s, SC_PHASE_END_STEP, 0);
+        if (rc) return rc;
+    }
+    return SC_OK;
+}
+
+int sc_sync(sc_sim *s) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    int derr = 0;
+    SC_CK(s, cudaMemcpy(&derr, &s->B.ctr->error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (derr) return set_err(s, SC_E_DEVICE, "device-side error code " + std::to_string(derr));
+    return SC_OK;
+}
+
+int sc_get_counters(sc_sim *s, sc_counters *out) {
+    if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
+    int rc = sc_sync(s);
+    ScCounters c;
+    SC_CK(s, cudaMemcpy(&c, s->B.ctr, sizeof c, cudaMemcpyDeviceToHost));
+    memset(out, 0, sizeof *out);
+    out->n_active_particles = c.nActive;
+    out->n_active_metabolic_particles = c.nActiveM;
+    out->next_particle_id = c.nextId;
+    out->step = c.step;
+    out->kernel_launches = s->launches;
+    out->device_error = c.error;
+    return rc == SC_E_DEVICE ? SC_OK : rc;
+}
+
+void *sc_get_stream(sc_sim *s) { return s ? (void *)s->st : nullptr; }
+
+int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *metabolic) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    const int N = s->P.N, Nm = s->P.Nm;
+    int rc = ensure_staging(s, std::max<size_t>(
+                                   std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
+                                   16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    if (particles && N > 0) {
+        k_pack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActive, N, B.P());
+        SC_CK(s, cudaMemcpyAsync(particles, s->staging, (size_t)N * sizeof(sc_particle), cudaMemcpyDeviceToHost, s->st));
+    }
+    if (metabolic && Nm > 0) {
+        SC_CK(s, cudaStreamSynchronize(s->st));
+        k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
+                                                              B.mcLscs, B.mcSpoly, B.mcNb, B.mcBonds);
+        SC_CK(s, cudaMemcpyAsync(metabolic, s->staging, (size_t)Nm * sizeof(sc_metabolic_particle),
+                                 cudaMemcpyDeviceToHost, s->st));
+    }
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    return check_launch(s);
+}
+
+int sc_export_grid(sc_sim *s, int32_t which, uint32_t *ranges, uint32_t *perm) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    const uint32_t cells = s->P.cells;
+    const int cap = which ? s->P.Nm : s->P.N;
+    if (ranges) {
+        std::vector<uint32_t> cs((size_t)cells + 1);
+        SC_CK(s, cudaMemcpy(cs.data(), which ? s->B.cellStartM : s->B.cellStartP, cs.size() * 4, cudaMemcpyDeviceToHost));
+        for (uint32_t c = 0; c < cells; c++) {
+            bool empty = cs[c] == cs[c + 1];
+            ranges[2 * (size_t)c] = empty ? 0 : cs[c];
+            ranges[2 * (size_t)c + 1] = empty ? 0 : cs[c + 1];
+        }
+    }
+    if (perm && cap > 0) {
+        const uint32_t *src = which ? s->B.valsM[s->B.sortCurM] : s->B.valsP[s->B.sortCurP];
+        SC_CK(s, cudaMemcpy(perm, src, (size_t)cap * 4, cudaMemcpyDeviceToHost));
+    }
+    return SC_OK;
+}
+
+int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabolic_particle *metabolic) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    ScLaunchCtx c = ctx(s);
+    sc_phase_reduce(c);
+    int rc = check_launch(s);
+    if (rc) return rc;
+    if (particles && s->P.N > 0)
+        SC_CK(s, cudaMemcpyAsync(particles, s->B.redP, (size_t)s->P.N * sizeof(sc_reduced_particle),
+                                 cudaMemcpyDeviceToHost, s->st));
+    if (metabolic && s->P.Nm > 0)
+        SC_CK(s, cudaMemcpyAsync(metabolic, s->B.redM, (size_t)s->P.Nm * sizeof(sc_reduced_metabolic_particle),
+                                 cudaMemcpyDeviceToHost, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    return SC_OK;
+}
+
+}  // extern "C"

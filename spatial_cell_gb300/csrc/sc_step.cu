@@ -1,0 +1,1073 @@
+// sc_step.cu -- the step's kernels on sm_103a, one per reference kernel.
+//
+// Each kernel computes, for every item it owns, exactly the floating-point
+// expression sequence of the reference kernel named in its comment (same
+// operand order, same implicit double-precision literals, no fused
+// multiply-add: the file is built with -fmad=false), so its results are
+// bit-identical to the reference's on the same input state.  What changes is
+// where the data lives: structure-of-arrays fields read 16 bytes at a time,
+// double buffering only for the fields a kernel's neighbours read, elementwise
+// kernels updating in place, and no memset of a whole 256-byte-per-item
+// buffer before each kernel (main.cu:326-638 does 92 of them per step).
+//
+// Launch shape: one thread per slot, 256 threads per CTA; the bound of every
+// kernel is the device-side active counter, so no host round trip is needed
+// between kernels (the reference reads nActiveParticles back three times per
+// step, main.cu:369,399,616).
+#include "sc_launch.h"
+
+__device__ __forceinline__ bool p_order(int ta, int ia, int tb, int ib) { return ta < tb || (ta == tb && ia < ib); }
+
+// ---- dynamics.cuh:19-215: move (its only live effect: debugVector.xyz = 0)
+// fused with brownianMovementAndRotation, in place --------------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_move_brownian(const int *__restrict__ nActivePtr,
+                                                              const int4 *__restrict__ info,
+                                                              const float4 *__restrict__ pos, float4 *dbg,
+                                                              float4 *posnoise, float4 *angnoise, ScParams P,
+                                                              float scale, uint32_t su, uint32_t sn,
+                                                              const int *__restrict__ stepPtr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    const int step = *stepPtr;
+    int4 in = info[i];
+    if (!(in.z & SC_ACTIVE)) return;
+    float4 d = dbg[i];
+    d.x = 0.0f; d.y = 0.0f; d.z = 0.0f;
+    dbg[i] = d;
+    float radius = pos[i].w;
+    uint32_t id = (uint32_t)in.x, st = (uint32_t)step;
+    uint64_t seed = P.seed;
+    sc_f4 r1 = sc_random_rotation(sc_uniform(seed, su, id, st, 0), sc_uniform(seed, su, id, st, 1),
+                                  sc_uniform(seed, su, id, st, 2));
+    float nrm = sc_normal(seed, sn, id, st, 0);
+    float mag = (float)((double)(fabsf(nrm) * scale) / fmax((double)radius / 2.5, 1.0));
+    st3(posnoise, i, sc_rotate(sc_up(), r1) * mag, 0.0f);
+    sc_f4 r2 = sc_random_rotation(sc_uniform(seed, su, id, st, 3), sc_uniform(seed, su, id, st, 4),
+                                  sc_uniform(seed, su, id, st, 5));
+    float t = (float)((double)P.rotNoise / ((double)radius / 2.5));
+    st4(angnoise, i, sc_slerp(ld4(angnoise, i), r2, t));
+}
+
+// ---- dynamics.cuh:217-242 applyNoise, in place -------------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_apply_noise(const int *__restrict__ nActivePtr,
+                                                            const int4 *__restrict__ info, float4 *vel,
+                                                            float4 *posnoise, float4 *angvel, float4 *angnoise) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    if (!(info[i].z & SC_ACTIVE)) return;
+    sc_f3 v = ld3(vel, i);
+    v += ld3(posnoise, i);
+    st3(vel, i, v, 0.0f);
+    st3(posnoise, i, sc_zero3(), 0.0f);
+    st4(angvel, i, sc_qmul(ld4(angnoise, i), ld4(angvel, i)));
+    st4(angnoise, i, sc_qid());
+}
+
+// ---- dynamics.cuh:244-282 applyVelocities, in place ---------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_apply_velocities(const int *__restrict__ nActivePtr,
+                                                                 const int4 *__restrict__ info, float4 *pos,
+                                                                 float4 *vel, float4 *rot, float4 *angvel,
+                                                                 ScParams P, float f) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    if (!(info[i].z & SC_ACTIVE)) return;
+    float4 p4 = pos[i];
+    sc_f3 p = sc_make_f3(p4.x, p4.y, p4.z);
+    sc_f3 v = ld3(vel, i);
+    p = clamp(p + v * f, 0.0f, P.simSize);
+    v *= P.velDecay;
+    sc_f4 av = ld4(angvel, i);
+    sc_f4 r = sc_qmul(sc_slerp(sc_qid(), av, f), ld4(rot, i));
+    r /= length(r);
+    av = sc_slerp(av, sc_qid(), 1.0f - P.angDecay);
+    pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+    st3(vel, i, v, 0.0f);
+    st4(rot, i, r);
+    st4(angvel, i, av);
+}
+
+// ---- dynamics.cuh:288-402 coordinateNoise -----------------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
+    const int *__restrict__ bonds, const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn,
+    float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = info[i];
+    int pnb = nb[i];
+    float4 pn4 = pnIn[i], an4 = anIn[i];
+    if (!(in.z & SC_ACTIVE) || pnb < 1) {
+        pnOut[i] = pn4;
+        anOut[i] = an4;
+        return;
+    }
+    pnb = min(pnb, SC_MAX_ACTIVE_INTERACTIONS);
+    int bt[SC_MAX_ACTIVE_INTERACTIONS], bp[SC_MAX_ACTIVE_INTERACTIONS];
+#pragma unroll
+    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+        bt[k] = k < pnb ? bonds[(size_t)i * 24 + 3 * k] : 0;
+        bp[k] = k < pnb ? bonds[(size_t)i * 24 + 3 * k + 2] : 0;
+    }
+    float4 p4 = pos[i];
+    sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    float prad = p4.w;
+    sc_f3 ppn = sc_make_f3(pn4.x, pn4.y, pn4.z);
+    sc_f4 pan = sc_make_f4(an4.x, an4.y, an4.z, an4.w);
+    sc_f3 dPN = sc_zero3();
+    sc_f4 dAN = sc_qid();
+    float w = 0.0f;
+    const float lim = P.maxInt;
+    scan27(P, cellStart, ppos, [&](int j) {
+        if (j == i) return;
+        int4 tin = info[j];
+        if (!(tin.z & SC_ACTIVE)) return;
+        float4 t4 = pos[j];
+        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
+        if (outside_cube(delta, lim)) return;
+#pragma unroll
+        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+            if (k >= pnb) break;
+            if (bt[k] < 10 && frac > 0.25f) continue;
+            if (bp[k] == tin.x) {
+                float trad = t4.w;
+                sc_f3 tpn = ld3(pnIn, j);
+                sc_f4 tan_ = ld4(anIn, j);
+                float pMag = length(ppn);
+                dPN += (tpn - ppn) * 0.9f * trad / (prad + trad) * 1.0f;
+                dPN *= fmaxf(length(dPN), pMag) / length(dPN);
+                dAN = sc_slerp(dAN, sc_qmul(sc_qinv(pan), tan_), 0.9f * trad / (prad + trad) * 1.0f);
+                w += 1.0f;
+            }
+        }
+    });
+    ppn += dPN / fmaxf(w, 1.0f);
+    pan = sc_qmul(sc_slerp(sc_qid(), dAN, 1.0f / fmaxf(w, 1.0f)), pan);
+    st3(pnOut, i, ppn, pn4.w);
+    st4(anOut, i, pan);
+}
+
+// ---- dynamics.cuh:405-822 relax ------------------------------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_relax(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
+    const int *__restrict__ bonds, const float4 *__restrict__ velIn, const float4 *__restrict__ rotIn,
+    const float4 *__restrict__ avIn, float4 *__restrict__ velOut, float4 *__restrict__ rotOut,
+    float4 *__restrict__ avOut, float4 *__restrict__ dbg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = info[i];
+    float4 v4 = velIn[i], r4 = rotIn[i], a4 = avIn[i];
+    if (!(in.z & SC_ACTIVE)) {
+        velOut[i] = v4;
+        rotOut[i] = r4;
+        avOut[i] = a4;
+        return;
+    }
+    float4 p4 = pos[i];
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
+    const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
+    sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
+    sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
+    const int pid = in.x, ptype = in.y, phydro = (int)(int8_t)(in.w & 0xff);
+    const int pnb = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    int bt[SC_MAX_ACTIVE_INTERACTIONS], bg[SC_MAX_ACTIVE_INTERACTIONS], bp[SC_MAX_ACTIVE_INTERACTIONS];
+#pragma unroll
+    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+        const int *b = bonds + (size_t)i * 24 + 3 * k;
+        bt[k] = k < pnb ? b[0] : 0;
+        bg[k] = k < pnb ? b[1] : 0;
+        bp[k] = k < pnb ? b[2] : 0;
+    }
+    sc_f4 pdbg = sc_make_f4(0, 0, 0, 0);
+    bool dbgTouched = false;
+    sc_f3 dV = sc_zero3();
+    sc_f4 dAV = sc_qid();
+    sc_f3 phobPos = sc_zero3();
+    float phobSum = 0.0f;
+    float w = 0.0f;
+    const sc_f3 up = sc_rotate(sc_up(), prot);
+    const sc_f3 nextUp = sc_rotate(up, pav);
+    const float lim = P.maxInt;
+    const float flex = SC_PI_REF / 8;
+    scan27(P, cellStart, ppos, [&](int j) {
+        if (j == i) return;
+        int4 tin = info[j];
+        if (!(tin.z & SC_ACTIVE)) return;
+        float4 t4 = pos[j];
+        const sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
+        sc_f3 delta = tpos - ppos;
+        if (outside_cube(delta, lim)) return;
+        const float trad = t4.w;
+        const int tid_ = tin.x, ttype = tin.y, thydro = (int)(int8_t)(tin.w & 0xff);
+        sc_f3 nd = normalize(delta);
+        float dist = sc_norm3(delta);
+        float idist = prad + trad;
+        if (phydro > 0 || thydro > 0) {
+            if (sc_within_lipid_range(dist, prad + trad) && phydro == SC_POLAR && thydro == SC_POLAR) {
+                sc_f3 tvel = ld3(velIn, j);
+                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+                sc_f3 pPV = -nextUp * prad + ppos + pvel;
+                sc_f3 tpPV = -nextTup * trad + tpos + tvel;
+                float L = length(tpPV - pPV) / (prad + trad);
+                float attr = (float)(fmin(fmax((double)L, 1e-6), (double)2.0f) / (double)2.0f);
+                w += 1.0f;
+                dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
+                float pap = sc_powf(fminf(1.0f / fmaxf(L, 1e-6f), 10.0f) / 10.0f, 0.2f);
+                phobSum += pap;
+                phobPos += tpPV * pap;
+            }
+        }
+        bool partners = false;
+#pragma unroll
+        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+            if (k >= pnb) break;
+            if (bp[k] != tid_) continue;
+            partners = true;
+            const int it = bt[k];
+            if (it >= 10) {
+                const sc_rule &pii = rule_at(P, it);
+                sc_f4 ro = rule_ori(pii);
+                sc_f3 rp = rule_pos(pii);
+                sc_f4 trot = ld4(rotIn, j), tav = ld4(avIn, j);
+                sc_f3 tvel = ld3(velIn, j);
+                bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
+                sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
+                sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
+                sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
+                sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
+                dAV = sc_slerp(dAV, sc_qmul(sc_slerp(rro, orro, 0.5f), rro), 0.9f * trad / (prad + trad));
+                sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot)))
+                               : sc_rotate(rp, sc_qmul(tav, trot));
+                rrp += tpos;
+                sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot)))
+                                : sc_rotate(rp, sc_qmul(pav, prot));
+                orrp += ppos;
+                w += 1.0f;
+                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+            }
+            if (it == 0) {
+                if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
+                sc_f4 trot = ld4(rotIn, j);
+                bool o1 = p_order(ptype, pid, ttype, tid_);
+                sc_f4 trod = sc_qmul(sc_quat(sc_up(), -SC_PI_REF / 6), sc_quat(sc_right(), SC_PI_REF / 6));
+                prot = sc_slerp(prot, o1 ? sc_qmul(trot, sc_qinv(trod)) : sc_qmul(trot, trod), 0.2f);
+                sc_f4 trpr = sc_quat(sc_forward(), -SC_PI_REF / 6);
+                sc_f3 rrp = o1 ? -sc_rotate(sc_up(), sc_qmul(trot, sc_qmul(sc_qinv(trod), trpr)))
+                               : sc_rotate(sc_up(), sc_qmul(trot, trpr));
+                rrp *= idist;
+                rrp += tpos;
+                pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.2f));
+                pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.2f));
+                pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.2f));
+            } else if (it == SC_INTERACTION_TYPE_CHAIN) {
+                if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
+                sc_f3 tvel = ld3(velIn, j);
+                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+                sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
+                bool fwd = bg[k] == SC_INTERACTION_GROUP_FORWARD;
+                dAV = sc_slerp(dAV, sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd), 0.9f * trad / (prad + trad));
+                sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
+                sc_f3 axis = sc_safe_cross(relUp, -nnd);
+                float ang = sc_angle3(relUp, -nnd);
+                sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
+                rrp *= idist;
+                rrp += tpos;
+                sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
+                sc_f3 oaxis = sc_safe_cross(oUp, nnd);
+                float oang = sc_angle3(oUp, nnd);
+                sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
+                orrp *= idist;
+                orrp += ppos;
+                w += 1.0f;
+                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+                pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.9f));
+                pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.9f));
+                pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.9f));
+            }
+        }
+        if (!partners) {
+            float cd = prad + trad;
+            if (dist < cd) {
+                sc_f3 tvel = ld3(velIn, j);
+                w += 1.0f;
+                dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+            }
+        }
+    });
+    sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
+    pav = sc_qmul(sc_slerp(sc_qid(), dAV, 1.0f / fmaxf(w, 1.0f)), pav);
+    if (phobSum > 0.0f) {
+        sc_f3 dir = normalize(phobPos / phobSum - (ppos + nv));
+        pav = sc_slerp(pav, sc_quat_from_to(-up, dir), 0.2f);
+    }
+    st3(velOut, i, nv, v4.w);
+    st4(rotOut, i, prot);
+    st4(avOut, i, pav);
+    if (dbgTouched) st4(dbg, i, pdbg);
+}
+
+// (float)((double)(rp + rt) + 0.8 * (double)rp) (metabolites.cuh:198,237,324),
+// recomputed only when the partner radius changes.
+struct CollisionDistCache {
+    float rt = 0.0f, cd = 0.0f;
+    bool valid = false;
+    __device__ __forceinline__ float get(float rp, float r) {
+        if (!valid || !(r == rt)) {
+            rt = r;
+            valid = true;
+            cd = (float)((double)(rp + r) + 0.8 * (double)rp);
+        }
+        return cd;
+    }
+};
+
+// ---- metabolites.cuh:140-264 relaxMetabolicParticles ----------------------
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab(
+    ScParams P, const uint32_t *__restrict__ cellStartM, const uint32_t *__restrict__ cellStartP,
+    const int *__restrict__ nActivePtr, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+    const float4 *__restrict__ mvelIn, float4 *__restrict__ mvelOut, const float4 *__restrict__ ppos_,
+    const int4 *__restrict__ pinfo, const float4 *__restrict__ pvel_) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    float4 v4 = mvelIn[i];
+    if (!(minfo[i].z & SC_ACTIVE)) {
+        mvelOut[i] = v4;
+        return;
+    }
+    float4 p4 = mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
+    const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+    sc_f3 dV = sc_zero3();
+    float w = 0.0f;
+    const float lim = P.maxInt;
+    CollisionDistCache cm, cp;
+    cells27(P, pp, [&](uint32_t key) {
+        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
+            if ((int)j == i) continue;
+            if (!(minfo[j].z & SC_ACTIVE)) continue;
+            float4 t4 = mpos[j];
+            sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
+            sc_f3 delta = tpos - pp;
+            if (outside_cube(delta, lim)) continue;
+            sc_f3 nd = normalize(delta);
+            float dist = sc_norm3(delta);
+            float cd = cm.get(prad, t4.w);
+            if (dist <= cd) {
+                w += 1.0f;
+                dV += (tpos - nd * cd + ld3(mvelIn, j) - (pp + pv)) * 0.9f * 1.0f;
+            }
+        }
+        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
+            int4 tin = pinfo[j];
+            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+            float4 t4 = ppos_[j];
+            sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
+            sc_f3 delta = tpos - pp;
+            if (outside_cube(delta, lim)) continue;
+            sc_f3 nd = normalize(delta);
+            float dist = sc_norm3(delta);
+            float cd = cp.get(prad, t4.w);
+            if (dist <= cd) {
+                w += 2.0f;
+                dV += (tpos - nd * cd + ld3(pvel_, j) - (pp + pv)) * 0.9f * 2.0f;
+            }
+        }
+    });
+    st3(mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+}
+
+// ---- metabolites.cuh:266-350 relaxMetabolicParticlePartners ----------------
+// Only lipids change, and only their own velocity, which no other thread of
+// this kernel reads: updated in place.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
+    ScParams P, const uint32_t *__restrict__ cellStartM, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
+    const float4 *__restrict__ mpos, const int4 *__restrict__ minfo, const float4 *__restrict__ mvel) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = pinfo[i];
+    if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) return;
+    float4 p4 = ppos_[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
+    float4 v4 = pvel_[i];
+    const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+    sc_f3 dV = sc_zero3();
+    float w = 0.0f;
+    const float lim = P.maxInt;
+    CollisionDistCache cc;
+    scan27(P, cellStartM, pp, [&](int j) {
+        if (!(minfo[j].z & SC_ACTIVE)) return;
+        float4 t4 = mpos[j];
+        sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
+        sc_f3 delta = tpos - pp;
+        if (outside_cube(delta, lim)) return;
+        sc_f3 nd = normalize(delta);
+        float dist = sc_norm3(delta);
+        float cd = cc.get(prad, t4.w);
+        if (dist <= cd) {
+            w += 2.0f;
+            dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
+        }
+    });
+    st3(pvel_, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+}
+
+// Alignment tests of complexify / transitionInteractions (interactions.cuh:319-324, 438-443).
+__device__ __forceinline__ void alignment(bool ord, sc_f4 prot, sc_f4 trot, sc_f3 up, sc_f3 tup, sc_f3 delta,
+                                          const sc_rule &r, float *oa, float *rpa) {
+    sc_f4 ro = rule_ori(r);
+    sc_f3 rp = rule_pos(r);
+    *oa = ord ? dot(sc_rotate(up, ro), tup) : dot(sc_rotate(tup, ro), up);
+    *rpa = ord ? dot(sc_rotate(rp, prot), delta) / sc_normsq3(delta)
+               : dot(sc_rotate(rp, trot), -delta) / sc_normsq3(delta);
+}
+__device__ __forceinline__ bool states_match(bool ord, int ps, int ts, const sc_rule &r) {
+    int fs = r.first_partner_state, ss = r.second_partner_state;
+    return ord ? ((fs < 0 || fs == ps) && (ss < 0 || ss == ts)) : ((ss < 0 || ss == ps) && (fs < 0 || fs == ts));
+}
+__device__ __forceinline__ bool group_active_in(const int *__restrict__ b, int nbv, int group) {
+    for (int k = 0; k < min(nbv, SC_MAX_ACTIVE_INTERACTIONS); k++)
+        if (b[3 * k + 1] == group) return true;
+    return false;
+}
+
+// ---- interactions.cuh:216-346 complexify --------------------------------------
+// New interactions are appended at slots [nb, nb') of the item's own list,
+// which no neighbour reads (they read [0, nb)); nb' goes to the next buffer.
+__global__ void __launch_bounds__(SC_THREADS) k_complexify(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
+    const int *__restrict__ state, const int *__restrict__ nbIn, int *__restrict__ nbOut, int *bonds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = info[i];
+    int pnb = nbIn[i];
+    int cs = 0, ce = 0;
+    if ((in.z & SC_ACTIVE) && in.y >= 0 && 2 * in.y + 1 < P.nPidx) {
+        cs = P.pidx[2 * in.y];
+        ce = P.pidx[2 * in.y + 1];
+    }
+    if (cs >= ce) {
+        nbOut[i] = pnb;
+        return;
+    }
+    float4 p4 = pos[i];
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const sc_f4 prot = ld4(rot, i);
+    const int pid = in.x, ptype = in.y, pstate = state[i];
+    const sc_f3 up = sc_rotate(sc_up(), prot);
+    int *pb = bonds + (size_t)i * 24;
+    const int nb0 = pnb;
+    const float lim = P.maxInt;
+    scan27(P, cellStart, ppos, [&](int j) {
+        if (j == i) return;
+        int4 tin = info[j];
+        if (!(tin.z & SC_ACTIVE)) return;
+        float4 t4 = pos[j];
+        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
+        if (outside_cube(delta, lim)) return;
+        sc_f4 trot = ld4(rot, j);
+        sc_f3 tup = sc_rotate(sc_up(), trot);
+        const int ttype = tin.y;
+        bool ord = p_order(ptype, pid, ttype, tin.x);
+        for (int k = cs; k < ce; k++) {
+            if (pnb >= SC_MAX_ACTIVE_INTERACTIONS) continue;
+            const sc_rule &pii = P.prules[k];
+            if (!((ptype == pii.first_partner_type && ttype == pii.second_partner_type) ||
+                  (ptype == pii.second_partner_type && ttype == pii.first_partner_type)) ||
+                pii.only_via_transition)
+                continue;
+            if (pii.group >= 0 && (group_active_in(pb, pnb, pii.group) ||
+                                   group_active_in(bonds + (size_t)j * 24, nbIn[j], pii.group)))
+                continue;
+            float oa, rpa;
+            alignment(ord, prot, trot, up, tup, delta, pii, &oa, &rpa);
+            if (oa > pii.orientation_alignment_threshold &&
+                fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold) &&
+                states_match(ord, pstate, state[j], pii)) {
+                pb[3 * pnb] = pii.id;
+                pb[3 * pnb + 1] = pii.group;
+                pb[3 * pnb + 2] = tin.x;
+                pnb++;
+            }
+        }
+    });
+    (void)nb0;
+    nbOut[i] = pnb;
+}
+
+// ---- interactions.cuh:349-555 transitionInteractions -------------------------
+__global__ void __launch_bounds__(SC_THREADS) k_transition(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const int *__restrict__ stepPtr, const float4 *__restrict__ pos, const float4 *__restrict__ rot,
+    const int4 *__restrict__ info, const int *__restrict__ stateIn, int *__restrict__ stateOut, const int *__restrict__ nbIn,
+    int *__restrict__ nbOut, const int *__restrict__ bondsIn, int *__restrict__ bondsOut, int *lscs, int *spoly) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    const int step = *stepPtr;
+    int4 in = info[i];
+    int pnb = min(max(nbIn[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    int pstate = stateIn[i];
+    int b[SC_MAX_ACTIVE_INTERACTIONS * 3];
+#pragma unroll
+    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS * 3; k++) b[k] = k < 3 * pnb ? bondsIn[(size_t)i * 24 + k] : 0;
+    if ((in.z & SC_ACTIVE) && pnb >= 1) {
+        float4 p4 = pos[i];
+        const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+        const sc_f4 prot = ld4(rot, i);
+        const int pid = in.x, ptype = in.y;
+        const sc_f3 up = sc_rotate(sc_up(), prot);
+        int src = -1;
+        int tId = 0, tGroup = 0, tSet = 0, tFirst = 0, tSecond = 0, tFs = 0, tSs = 0, tPoly = 0;
+        const float lim = P.maxInt;
+        scan27(P, cellStart, ppos, [&](int j) {
+            if (j == i) return;
+            int4 tin = info[j];
+            if (!(tin.z & SC_ACTIVE)) return;
+            float4 t4 = pos[j];
+            sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
+            if (outside_cube(delta, lim)) return;
+            bool loaded = false;
+            sc_f4 trot;
+            sc_f3 tup;
+            const int ttype = tin.y;
+            const bool ord = p_order(ptype, pid, ttype, tin.x);
+            for (int k = 0; k < pnb; k++) {
+                if (b[3 * k] < 10) continue;
+                if (b[3 * k + 2] != tin.x) continue;
+                const sc_rule &pii = rule_at(P, b[3 * k]);
+                if (!(pii.transition_to >= 0 || pii.break_after_transition)) continue;
+                if (!loaded) { trot = ld4(rot, j); tup = sc_rotate(sc_up(), trot); loaded = true; }
+                float oa, rpa;
+                alignment(ord, prot, trot, up, tup, delta, pii, &oa, &rpa);
+                bool aligned = pii.break_after_transition || !pii.wait_for_alignment ||
+                               (oa > pii.orientation_alignment_threshold &&
+                                fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold));
+                if (!(aligned && (!pii.wait_for_state || states_match(ord, pstate, stateIn[j], pii)))) continue;
+                if (pii.transition_to >= 0) {
+                    const sc_rule &tpii = rule_at(P, pii.transition_to);
+                    if (tpii.group >= 0 && tpii.group != pii.group) {
+                        bool ga = false;
+                        for (int l = 0; l < pnb; l++)
+                            if (b[3 * l + 1] == tpii.group) { ga = true; break; }
+                        if (!ga) ga = group_active_in(bondsIn + (size_t)j * 24, nbIn[j], tpii.group);
+                        if (ga) continue;
+                    }
+                    if (!tpii.set_state || !((ptype == tpii.first_partner_type && tpii.first_partner_state >= 0) ||
+                                             (ptype == tpii.second_partner_type && tpii.second_partner_state >= 0))) {
+                        b[3 * k] = tpii.id;
+                        b[3 * k + 1] = tpii.group;
+                    } else {
+                        src = k;
+                        tId = tpii.id; tGroup = tpii.group; tSet = tpii.set_state;
+                        tFirst = tpii.first_partner_type; tSecond = tpii.second_partner_type;
+                        tFs = tpii.first_partner_state; tSs = tpii.second_partner_state; tPoly = tpii.polymerize;
+                    }
+                } else if (pii.break_after_transition) {
+                    for (int l = k; l < pnb - 1; l++) {
+                        b[3 * l] = b[3 * l + 3];
+                        b[3 * l + 1] = b[3 * l + 4];
+                        b[3 * l + 2] = b[3 * l + 5];
+                    }
+                    pnb--;
+                    if (src > k) src--;
+                    k--;
+                }
+            }
+        });
+        if (src >= 0) {
+            b[3 * src] = tId;
+            b[3 * src + 1] = tGroup;
+            if (tSet) {
+                if (ptype == tFirst && tFs >= 0) { pstate = tFs; lscs[i] = step; }
+                if (ptype == tSecond && tSs >= 0) { pstate = tSs; lscs[i] = step; }
+            }
+            if (tPoly >= 0) {
+                const sc_rule &poly = rule_at(P, tPoly);
+                if (poly.first_partner_type == ptype || poly.second_partner_type == ptype) spoly[i] = tPoly;
+            }
+        }
+    }
+    stateOut[i] = pstate;
+    nbOut[i] = pnb;
+    for (int k = 0; k < 3 * pnb; k++) bondsOut[(size_t)i * 24 + k] = b[k];
+}
+
+// ---- interactions.cuh:558-740 polymerize --------------------------------------
+// The reference runs it in place with atomicAdd slot / id allocation and
+// cross-slot writes, so its outcome depends on thread scheduling.  Here the
+// scheduled items are collected and one thread performs them in slot order,
+// which is the order a one-thread-at-a-time execution of the reference gives.
+__global__ void __launch_bounds__(SC_THREADS) k_poly_collect(const int *__restrict__ nActivePtr,
+                                                             const int4 *__restrict__ info,
+                                                             const int *__restrict__ spoly, int *list, int cap,
+                                                             ScCounters *ctr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    if (!(info[i].z & SC_ACTIVE) || spoly[i] < 0) return;
+    int k = atomicAdd(&ctr->polyCount, 1);
+    if (k < cap) list[k] = i;
+}
+
+__device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFields &F, ScCounters *ctr, int i,
+                         int step) {
+    int4 in = F.info[i];
+    const sc_rule &poly = rule_at(P, F.spoly[i]);
+    const int pid = in.x, ptype = in.y;
+    int *pb = F.bonds + (size_t)i * 24;
+    int pnb = min(max(F.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    int api = -1, pmi = -1;
+    for (int k = 0; k < pnb; k++)
+        if (pb[3 * k + 1] == poly.group) { api = k; break; }
+    float4 p4 = F.pos[i];
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    if (api >= 0) {
+        int target = pb[3 * api + 2];
+        scan27(P, cellStart, ppos, [&](int j) {
+            if (j == i) return;
+            int4 tin = F.info[j];
+            if (!(tin.z & SC_ACTIVE)) return;
+            if (tin.x == target) pmi = j;
+        });
+    }
+    const bool first = poly.first_partner_type == ptype;
+    const int newType = first ? poly.second_partner_type : poly.first_partner_type;
+    const int newState = first ? poly.second_partner_state : poly.first_partner_state;
+    const int spolyId = F.spoly[i];
+    if (newType >= 0) {
+        float nr = 0.0f;
+        int nh = 0;
+        if (newType < P.nTypes) { nr = P.types[newType].radius; nh = P.types[newType].hydrophobic; }
+        int newIdx = ++ctr->lastActive;
+        if (newIdx < P.N) {
+            int newId = ctr->nextId++;
+            sc_f3 rp = rule_pos(poly);
+            sc_f4 ro = rule_ori(poly);
+            sc_f4 prot = ld4(F.rot, i);
+            sc_f3 npos = ppos + sc_rotate(ptype < newType ? rp : -rp, prot);
+            sc_f4 nrot = sc_qmul(prot, ptype < newType ? ro : sc_qinv(ro));
+            // Particle(newId, newType, 0, radius, hydrophobic, pos, rot): types.cuh:192-221
+            F.pos[newIdx] = make_float4(npos.x, npos.y, npos.z, nr);
+            F.vel[newIdx] = make_float4(0, 0, 0, 0);
+            st4(F.rot, newIdx, nrot);
+            F.angvel[newIdx] = make_float4(0, 0, 0, 1);
+            F.posnoise[newIdx] = make_float4(0, 0, 0, 0);
+            F.angnoise[newIdx] = make_float4(0, 0, 0, 1);
+            F.dbg[newIdx] = make_float4(0, 0, 0, 0);
+            F.info[newIdx] = make_int4(newId, newType, SC_ACTIVE, (int)(int8_t)nh);
+            F.state[newIdx] = newState >= 0 ? newState : 0;
+            F.lscs[newIdx] = newState >= 0 ? step : -1;
+            F.spoly[newIdx] = -1;
+            int *nbp = F.bonds + (size_t)newIdx * 24;
+            int nnb = 0;
+            nbp[0] = spolyId; nbp[1] = poly.group; nbp[2] = pid;
+            nnb = 1;
+            if (pmi >= 0) {
+                int *mb = F.bonds + (size_t)pmi * 24;
+                int mnb = min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS);
+                for (int k = 0; k < mnb; k++) {
+                    if (mb[3 * k + 1] == poly.group) {
+                        for (int l = k; l < mnb - 1; l++) {
+                            mb[3 * l] = mb[3 * l + 3]; mb[3 * l + 1] = mb[3 * l + 4]; mb[3 * l + 2] = mb[3 * l + 5];
+                        }
+                        mnb--;
+                        break;
+                    }
+                }
+                if (mnb < SC_MAX_ACTIVE_INTERACTIONS) {
+                    mb[3 * mnb] = SC_INTERACTION_TYPE_CHAIN; mb[3 * mnb + 1] = SC_INTERACTION_GROUP_FORWARD;
+                    mb[3 * mnb + 2] = newId;
+                }
+                mnb++;
+                F.nb[pmi] = mnb;
+                nbp[3] = SC_INTERACTION_TYPE_CHAIN; nbp[4] = SC_INTERACTION_GROUP_BACKWARD; nbp[5] = F.info[pmi].x;
+                nnb = 2;
+                pb[3 * api] = spolyId;
+                pb[3 * api + 2] = newId;
+            } else {
+                if (pnb < SC_MAX_ACTIVE_INTERACTIONS) {
+                    pb[3 * pnb] = spolyId; pb[3 * pnb + 1] = poly.group; pb[3 * pnb + 2] = newId;
+                }
+                pnb++;
+            }
+            for (int k = 3 * nnb; k < 24; k++) nbp[k] = 0;
+            F.nb[newIdx] = nnb;
+            ctr->nActive++;
+        }
+    } else {
+        // End of the chain; the reference's out-of-bounds stores without a
+        // previous monomer / active bond (interactions.cuh:728, 731-734) are skipped.
+        if (pmi >= 0) {
+            int *mb = F.bonds + (size_t)pmi * 24;
+            int mnb = min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS);
+            for (int k = 0; k < mnb; k++) {
+                if (mb[3 * k + 1] == poly.group) {
+                    for (int l = k; l < mnb - 1; l++) {
+                        mb[3 * l] = mb[3 * l + 3]; mb[3 * l + 1] = mb[3 * l + 4]; mb[3 * l + 2] = mb[3 * l + 5];
+                    }
+                    mnb--;
+                    break;
+                }
+            }
+            F.nb[pmi] = mnb;
+        }
+        if (api >= 0) {
+            for (int l = api; l < pnb - 1; l++) {
+                pb[3 * l] = pb[3 * l + 3]; pb[3 * l + 1] = pb[3 * l + 4]; pb[3 * l + 2] = pb[3 * l + 5];
+            }
+            pnb--;
+        }
+    }
+    F.nb[i] = pnb;
+    F.spoly[i] = -1;
+}
+
+// One CTA: sorts the collected slots (odd-even transposition in shared
+// memory), then thread 0 performs them in slot order.  If more were scheduled
+// than the list holds, the CTA walks all slots in order instead.
+#define SC_POLY_LIST_CAP 4096
+__global__ void __launch_bounds__(1024) k_polymerize(ScParams P, const uint32_t *__restrict__ cellStart, PFields F,
+                                                     ScCounters *ctr, const int *list) {
+    const int step = ctr->step;
+    __shared__ int s[SC_POLY_LIST_CAP];
+    __shared__ int s_n0;
+    const int count = ctr->polyCount;
+    if (count == 0) return;
+    if (threadIdx.x == 0) s_n0 = ctr->nActive;
+    __syncthreads();
+    const int n0 = s_n0;
+    if (count <= SC_POLY_LIST_CAP) {
+        for (int k = threadIdx.x; k < count; k += blockDim.x) s[k] = list[k];
+        __syncthreads();
+        for (int phase = 0; phase < count; phase++) {
+            for (int k = 2 * threadIdx.x + (phase & 1); k + 1 < count; k += 2 * blockDim.x) {
+                int a = s[k], b = s[k + 1];
+                if (a > b) { s[k] = b; s[k + 1] = a; }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < count; k++) {
+                int i = s[k];
+                if (i < n0 && (F.info[i].z & SC_ACTIVE) && F.spoly[i] >= 0) poly_one(P, cellStart, F, ctr, i, step);
+            }
+        }
+    } else {
+        if (threadIdx.x == 0) {
+            for (int i = 0; i < n0; i++)
+                if ((F.info[i].z & SC_ACTIVE) && F.spoly[i] >= 0) poly_one(P, cellStart, F, ctr, i, step);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) ctr->polyCount = 0;
+}
+
+// ---- metabolites.cuh:352-431 diffuseMetabolites ------------------------------
+template <int SP>
+__global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32_t *__restrict__ cellStart,
+                                                        const int *__restrict__ nActivePtr,
+                                                        const float4 *__restrict__ pos, const int4 *__restrict__ info,
+                                                        const float4 *__restrict__ metIn, float4 *__restrict__ metOut) {
+    constexpr int Q = SP / 4;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    float pm[SP];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        float4 v = metIn[(size_t)i * Q + q];
+        pm[4 * q] = v.x; pm[4 * q + 1] = v.y; pm[4 * q + 2] = v.z; pm[4 * q + 3] = v.w;
+    }
+    if (!(info[i].z & SC_ACTIVE)) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) metOut[(size_t)i * Q + q] = metIn[(size_t)i * Q + q];
+        return;
+    }
+    float4 p4 = pos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    float dm[SP];
+#pragma unroll
+    for (int k = 0; k < SP; k++) dm[k] = 0.0f;
+    const int S = P.S;
+    const float lim = P.maxDiff;
+    scan27(P, cellStart, pp, [&](int j) {
+        if (j == i) return;
+        if (!(info[j].z & SC_ACTIVE)) return;
+        float4 t4 = pos[j];
+        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - pp;
+        if (outside_cube(delta, lim)) return;
+        float dist = sc_norm3(delta);
+        if (dist <= lim) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                float4 v = metIn[(size_t)j * Q + q];
+                float tm[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    int k = 4 * q + c;
+                    if (k < S) {
+                        float diff = tm[c] - pm[k];
+                        if (sc_diffuse_exceeds(diff)) dm[k] += diff * 0.1f;
+                    }
+                }
+            }
+        }
+    });
+#pragma unroll
+    for (int k = 0; k < SP; k++)
+        if (k < S) pm[k] += dm[k];
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+        metOut[(size_t)i * Q + q] = make_float4(pm[4 * q], pm[4 * q + 1], pm[4 * q + 2], pm[4 * q + 3]);
+}
+
+// ---- metabolites.cuh:18-88 removeInterferingMetabolicParticles -------------
+// Only the item's own flags change and no other thread reads metabolic
+// flags here: updated in place.
+__global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
+    ScParams P, const uint32_t *__restrict__ cellStartP, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ mpos, int4 *__restrict__ minfo, const float4 *__restrict__ ppos_,
+    const int4 *__restrict__ pinfo) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = minfo[i];
+    if (!(in.z & SC_ACTIVE)) return;
+    float4 p4 = mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
+    int flags = in.z;
+    const float lim = P.maxInt;
+    scan27(P, cellStartP, pp, [&](int j) {
+        int4 tin = pinfo[j];
+        if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) return;
+        float4 t4 = ppos_[j];
+        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - pp;
+        if (outside_cube(delta, lim)) return;
+        float dist = sc_norm3(delta);
+        float interf = (float)((double)(prad + t4.w) + 0.001);
+        if (dist <= interf) flags = flags & ~SC_ACTIVE;
+    });
+    if (flags != in.z) minfo[i].z = flags;
+}
+
+// ---- dynamics.cuh:824-844 reduceParticles (frames.dat records) --------------
+__device__ __forceinline__ void reduce_common(sc_reduced_particle &r, int4 in, int state, float4 p4, float4 r4,
+                                              float4 d4) {
+    r.id = in.x;
+    r.type = in.y;
+    r.flags = in.z | (((int)(int8_t)state & 0x0000000F) << 16);
+    r.radius = sc_f2h(p4.w);
+    r.pos[0] = sc_f2h(p4.x); r.pos[1] = sc_f2h(p4.y); r.pos[2] = sc_f2h(p4.z);
+    r.rot[0] = sc_f2h(r4.x); r.rot[1] = sc_f2h(r4.y); r.rot[2] = sc_f2h(r4.z); r.rot[3] = sc_f2h(r4.w);
+    r.debug_vector[0] = sc_f2h(d4.x); r.debug_vector[1] = sc_f2h(d4.y);
+    r.debug_vector[2] = sc_f2h(d4.z); r.debug_vector[3] = sc_f2h(d4.w);
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_reduce_particles(const int *__restrict__ nActivePtr, int cap,
+                                                                 PFields F, sc_reduced_particle *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    sc_reduced_particle r;
+    memset(&r, 0, sizeof r);
+    if (i < *nActivePtr) reduce_common(r, F.info[i], F.state[i], F.pos[i], F.rot[i], F.dbg[i]);
+    out[i] = r;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_reduce_metabolic(const int *__restrict__ nActivePtr, int cap, int sp4,
+                                                                 MFields F, sc_reduced_metabolic_particle *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    sc_reduced_metabolic_particle r;
+    memset(&r, 0, sizeof r);
+    if (i < *nActivePtr) {
+        reduce_common(r.p, F.info[i], F.state[i], F.pos[i], F.rot[i], F.dbg[i]);
+        float4 m = F.met[(size_t)i * sp4];
+        r.metabolites[0] = sc_f2h(m.x); r.metabolites[1] = sc_f2h(m.y);
+        r.metabolites[2] = sc_f2h(m.z); r.metabolites[3] = sc_f2h(m.w);
+    }
+    out[i] = r;
+}
+
+// ---- launchers ------------------------------------------------------------------
+static inline int nblocks(int n) { return (n + SC_THREADS - 1) / SC_THREADS; }
+
+void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic) {
+    ScBuffers &B = *c.B;
+    if (!metabolic) {
+        PFields F = B.P();
+        if (c.P.N <= 0) return;
+        k_move_brownian<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.dbg, F.posnoise,
+                                                                  F.angnoise, c.P, c.P.moveNoise, SC_STREAM_P_UNIFORM,
+                                                                  SC_STREAM_P_NORMAL, &B.ctr->step);
+    } else {
+        MFields F = B.M();
+        if (c.P.Nm <= 0) return;
+        k_move_brownian<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, F.info, F.pos, F.dbg, F.posnoise,
+                                                                   F.angnoise, c.P, c.P.metabNoise,
+                                                                   SC_STREAM_M_UNIFORM, SC_STREAM_M_NORMAL,
+                                                                   &B.ctr->step);
+    }
+    (*c.launches)++;
+}
+
+void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P(), X = B.Pnext();
+    k_coordinate_noise<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info,
+                                                                 F.nb, F.bonds, F.posnoise, F.angnoise, X.posnoise,
+                                                                 X.angnoise, frac);
+    B.cp[FP_POSNOISE] ^= 1;
+    B.cp[FP_ANGNOISE] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_apply_noise(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N > 0) {
+        PFields F = B.P();
+        k_apply_noise<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.vel, F.posnoise, F.angvel,
+                                                                F.angnoise);
+        (*c.launches)++;
+    }
+    if (c.P.Nm > 0) {
+        MFields M = B.M();
+        k_apply_noise<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, M.info, M.vel, M.posnoise,
+                                                                 M.angvel, M.angnoise);
+        (*c.launches)++;
+    }
+}
+
+void sc_phase_relax(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P(), X = B.Pnext();
+    k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds,
+                                                      F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg);
+    B.cp[FP_VEL] ^= 1;
+    B.cp[FP_ROT] ^= 1;
+    B.cp[FP_ANGVEL] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_relax_metab(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.Nm <= 0) return;
+    MFields M = B.M(), X = B.Mnext();
+    PFields F = B.P();
+    k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
+                                                             M.info, M.vel, X.vel, F.pos, F.info, F.vel);
+    B.cm[FM_VEL] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_relax_partners(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    MFields M = B.M();
+    PFields F = B.P();
+    k_relax_partners<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
+                                                               F.vel, M.pos, M.info, M.vel);
+    (*c.launches)++;
+}
+
+void sc_phase_apply_velocities(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N > 0) {
+        PFields F = B.P();
+        k_apply_velocities<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.vel, F.rot,
+                                                                     F.angvel, c.P, 0.45f);
+        (*c.launches)++;
+    }
+    if (c.P.Nm > 0) {
+        MFields M = B.M();
+        k_apply_velocities<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, M.info, M.pos, M.vel, M.rot,
+                                                                      M.angvel, c.P, 0.45f);
+        (*c.launches)++;
+    }
+}
+
+void sc_phase_complexify(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P(), X = B.Pnext();
+    k_complexify<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.rot, F.info,
+                                                           F.state, F.nb, X.nb, F.bonds);
+    B.cp[FP_NB] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_transition(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P(), X = B.Pnext();
+    k_transition<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, &B.ctr->step, F.pos, F.rot,
+                                                           F.info, F.state, X.state, F.nb, X.nb, F.bonds, X.bonds,
+                                                           F.lscs, F.spoly);
+    B.cp[FP_STATE] ^= 1;
+    B.cp[FP_NB] ^= 1;
+    B.cp[FP_BONDS] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_polymerize(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P();
+    k_poly_collect<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.spoly, B.polyList, B.polyCap,
+                                                             B.ctr);
+    k_polymerize<<<1, 1024, 0, c.st>>>(c.P, B.cellStartP, F, B.ctr, B.polyList);
+    (*c.launches) += 2;
+}
+
+void sc_phase_diffuse(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.Nm <= 0) return;
+    MFields M = B.M(), X = B.Mnext();
+    switch (c.P.SP) {
+        case 4:
+            k_diffuse<4><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+                                                                   M.met, X.met);
+            break;
+        case 8:
+            k_diffuse<8><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+                                                                   M.met, X.met);
+            break;
+        default:
+            k_diffuse<12><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
+                                                                    M.info, M.met, X.met);
+            break;
+    }
+    B.cm[FM_MET] ^= 1;
+    (*c.launches)++;
+}
+
+void sc_phase_remove_interfering(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.Nm <= 0) return;
+    MFields M = B.M();
+    PFields F = B.P();
+    k_remove_interfering<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info,
+                                                                    F.pos, F.info);
+    (*c.launches)++;
+}
+
+void sc_phase_reduce(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N > 0) {
+        k_reduce_particles<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, c.P.N, B.P(), B.redP);
+        (*c.launches)++;
+    }
+    if (c.P.Nm > 0) {
+        k_reduce_metabolic<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, c.P.Nm, c.P.SP / 4, B.M(),
+                                                                      B.redM);
+        (*c.launches)++;
+    }
+}

@@ -123,6 +123,7 @@ SC_HD int sc_round_int(float x) { return (int)(x >= 0.0f ? x + 0.5f : x - 0.5f);
 
 // sin / cos of a reduced argument |r| <= ~pi/4 (Taylor through r^13 / r^14).
 SC_HD float sc_sin_poly(float r) {
+    if (r == 0.0f) return r;  // keeps the sign of zero
     float r2 = r * r;
     float p = 1.6059044372074283e-10f;
     p = p * r2 + (-2.5052107943679403e-08f);
@@ -162,6 +163,7 @@ SC_HD int sc_reduce_pio2(float x, float *r) {
 
 SC_HD float sc_sinf(float x) {
     if (!sc_isfinitef(x)) return x - x;  // NaN for +-inf and NaN
+    if (x == 0.0f) return x;             // sin(+-0) = +-0
     float r;
     int q = sc_reduce_pio2(x, &r);
     float s = sc_sin_poly(r), c = sc_cos_poly(r);
@@ -457,6 +459,26 @@ SC_HD sc_f3 sc_rotate(sc_f3 a, sc_f4 q) {
     return sc_make_f3(a.x * (1.0f - yy2 - zz2) + a.y * (xy2 - wz2) + a.z * (xz2 + wy2),
                       a.x * (xy2 + wz2) + a.y * (1.0f - xx2 - zz2) + a.z * (yz2 - wx2),
                       a.x * (xz2 - wy2) + a.y * (yz2 + wx2) + a.z * (1.0f - xx2 - yy2));
+}
+
+// ---------------------------------------------------------------------------
+// Single-precision forms of the reference's double-precision comparisons
+// (exactly equivalent; the tests check them against the double forms).
+// ---------------------------------------------------------------------------
+// (double)|x| > 0.001 for a float x: 0.001 is not a float, so the test is
+// |x| >= the smallest float above 0.001 (metabolites.cuh:416).
+#define SC_DIFFUSE_THRESHOLD 0.0010000000474974513f
+SC_HD bool sc_diffuse_exceeds(float diff) { return fabsf(diff) >= SC_DIFFUSE_THRESHOLD; }
+
+// (double)dist <= (double)s + 0.8 * (double)s * 0.5 (dynamics.cuh:478) for
+// float dist, s.  The bound lies within 1e-15 (relative) of 1.4 * s, so
+// single precision decides every dist outside [s*1.3999999, s*1.4000001]
+// (both products are rounded values of reals strictly below / above the
+// bound, and dist < RN(a) implies dist <= a); the rest falls back to double.
+SC_HD bool sc_within_lipid_range(float dist, float s) {
+    if (dist < s * 1.3999999f) return true;
+    if (dist > s * 1.4000001f) return false;
+    return (double)dist <= (double)s + 0.8 * (double)s * 0.5;
 }
 
 // The reference's cell index (grid.cuh:13-17): min((uint)(c / cell), n - 1).

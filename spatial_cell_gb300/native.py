@@ -1,0 +1,182 @@
+"""ctypes binding of libspatialcell.so (include/spatialcell.h).
+
+The library is built in-tree (spatial_cell_gb300/_lib) by
+``spatial_cell_gb300.build``.  Loading fails loudly when it is missing: there
+is no CPU fallback for any call.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libspatialcell.so")
+
+_lib = None
+
+_P = ctypes.c_void_p
+_SIGS = {
+    "sc_config_defaults": (None, [ctypes.POINTER(abi.Config)]),
+    "sc_config_load_json": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(abi.Config)]),
+    "sc_config_grid": (ctypes.c_int, [ctypes.POINTER(abi.Config), ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(ctypes.c_int32)]),
+    "sc_types_load_json": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "sc_rules_load_json": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "sc_create": (ctypes.c_int, [ctypes.POINTER(abi.Config), _P, ctypes.c_int32, _P, ctypes.c_int32,
+                                 ctypes.POINTER(_P)]),
+    "sc_destroy": (None, [_P]),
+    "sc_last_error": (ctypes.c_char_p, [_P]),
+    "sc_load_state": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "sc_prepare": (ctypes.c_int, [_P]),
+    "sc_step": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "sc_run_phase": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "sc_sync": (ctypes.c_int, [_P]),
+    "sc_export_state": (ctypes.c_int, [_P, _P, _P]),
+    "sc_export_grid": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "sc_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(abi.Counters)]),
+    "sc_reduce_frame": (ctypes.c_int, [_P, _P, _P]),
+    "sc_get_stream": (ctypes.c_void_p, [_P]),
+    "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
+    "sc_frames_write_frame": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config), _P, _P]),
+}
+
+# Every symbol include/spatialcell.h declares.
+EXPORTED = tuple(_SIGS)
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing; build it with `python -m spatial_cell_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class ScError(RuntimeError):
+    pass
+
+
+def _check(rc, sim=None, what=""):
+    if rc != 0:
+        msg = lib().sc_last_error(sim)
+        raise ScError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+
+def load_config_json(path, base=None):
+    c = abi.make_config() if base is None else base
+    _check(lib().sc_config_load_json(path.encode(), ctypes.byref(c)), None, "sc_config_load_json")
+    return c
+
+
+def load_types_json(path):
+    n = ctypes.c_int32(0)
+    _check(lib().sc_types_load_json(path.encode(), None, 0, ctypes.byref(n)), None, "sc_types_load_json")
+    out = np.zeros(n.value, abi.TYPE_INFO_DTYPE)
+    _check(lib().sc_types_load_json(path.encode(), abi.ptr(out), n.value, ctypes.byref(n)), None, "sc_types_load_json")
+    return out
+
+
+def load_rules_json(path):
+    n = ctypes.c_int32(0)
+    _check(lib().sc_rules_load_json(path.encode(), None, 0, ctypes.byref(n)), None, "sc_rules_load_json")
+    out = np.zeros(n.value, abi.RULE_DTYPE)
+    _check(lib().sc_rules_load_json(path.encode(), abi.ptr(out), n.value, ctypes.byref(n)), None, "sc_rules_load_json")
+    return out
+
+
+def grid(cfg):
+    n, b = ctypes.c_int32(0), ctypes.c_int32(0)
+    _check(lib().sc_config_grid(ctypes.byref(cfg), ctypes.byref(n), ctypes.byref(b)), None, "sc_config_grid")
+    return n.value, b.value
+
+
+class Simulation:
+    """One simulation on the current CUDA device (include/spatialcell.h)."""
+
+    def __init__(self, cfg, types, rules):
+        self.L = lib()
+        self.cfg = cfg
+        self.types = np.ascontiguousarray(types, dtype=abi.TYPE_INFO_DTYPE)
+        self.rules = np.ascontiguousarray(rules, dtype=abi.RULE_DTYPE)
+        h = ctypes.c_void_p()
+        _check(self.L.sc_create(ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules),
+                                len(self.rules), ctypes.byref(h)), None, "sc_create")
+        self.h = h
+        self.n_grid, self.bits, self.cells = abi.grid_dims(cfg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def load_state(self, particles, metabolic, step=0, next_particle_id=None):
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        m = np.ascontiguousarray(metabolic, abi.METABOLIC_DTYPE)
+        if next_particle_id is None:
+            next_particle_id = len(p)
+        _check(self.L.sc_load_state(self.h, abi.ptr(p), len(p), abi.ptr(m), len(m), step, next_particle_id), self.h,
+               "sc_load_state")
+
+    def load_state_ptr(self, p_ptr, n, m_ptr, nm, step=0, next_particle_id=0):
+        """Loads from raw host pointers (e.g. pinned buffers)."""
+        _check(self.L.sc_load_state(self.h, p_ptr, n, m_ptr, nm, step, next_particle_id), self.h, "sc_load_state")
+
+    def prepare(self):
+        _check(self.L.sc_prepare(self.h), self.h, "sc_prepare")
+
+    def step(self, n=1):
+        _check(self.L.sc_step(self.h, n), self.h, "sc_step")
+
+    def run_phase(self, phase, arg=0):
+        _check(self.L.sc_run_phase(self.h, phase, arg), self.h, f"sc_run_phase({phase})")
+
+    def sync(self):
+        _check(self.L.sc_sync(self.h), self.h, "sc_sync")
+
+    def export_state(self):
+        p = np.zeros(self.cfg.num_particles, abi.PARTICLE_DTYPE)
+        m = np.zeros(self.cfg.num_metabolic_particles, abi.METABOLIC_DTYPE)
+        _check(self.L.sc_export_state(self.h, abi.ptr(p), abi.ptr(m)), self.h, "sc_export_state")
+        return p, m
+
+    def export_grid(self, which):
+        r = np.zeros(self.cells * 2, np.uint32)
+        cap = self.cfg.num_metabolic_particles if which else self.cfg.num_particles
+        perm = np.zeros(max(cap, 1), np.uint32)
+        _check(self.L.sc_export_grid(self.h, which, abi.ptr(r), abi.ptr(perm)), self.h, "sc_export_grid")
+        return r, perm[:cap]
+
+    def stream_handle(self):
+        """The sim's cudaStream_t as an integer."""
+        return self.L.sc_get_stream(self.h)
+
+    def counters(self):
+        c = abi.Counters()
+        _check(self.L.sc_get_counters(self.h, ctypes.byref(c)), self.h, "sc_get_counters")
+        return c
+
+    def reduce_frame(self, out_p=None, out_m=None):
+        rp = np.zeros(self.cfg.num_particles, abi.REDUCED_DTYPE) if out_p is None else out_p
+        rm = np.zeros(self.cfg.num_metabolic_particles, abi.REDUCED_METABOLIC_DTYPE) if out_m is None else out_m
+        _check(self.L.sc_reduce_frame(self.h, abi.ptr(rp), abi.ptr(rm)), self.h, "sc_reduce_frame")
+        return rp, rm
+
+    def reduce_frame_ptr(self, p_ptr, m_ptr):
+        _check(self.L.sc_reduce_frame(self.h, p_ptr, m_ptr), self.h, "sc_reduce_frame")

@@ -1,0 +1,107 @@
+"""Parity of the sm_103a step with the CPU oracle (bit-exact).
+
+The oracle (oracle/scport.cpp) is itself pinned to the reference's own
+kernels (tests/test_oracle_ref.py) and to committed golden vectors
+(tests/test_golden.py).  Here the CUDA path is driven through the C ABI
+(libspatialcell.so) and compared with the oracle on the same input state:
+phase by phase in lock step, over whole steps, and on the sort results.
+Floating-point fields are compared as bit patterns.
+"""
+import numpy as np
+import pytest
+
+from spatial_cell_gb300 import abi, scenes
+from tests.helpers import assert_same_counters, assert_same_state, step_phases
+
+pytestmark = pytest.mark.gpu
+
+
+def _engines(product, scene):
+    from oracle.engine import OracleEngine
+    cfg, types, rules, p, m, nid = scene
+    gpu = product.Simulation(cfg, types, rules)
+    cpu = OracleEngine("port", cfg, types, rules)
+    for e in (gpu, cpu):
+        e.load_state(p, m, step=0, next_particle_id=nid)
+    return cfg, gpu, cpu
+
+
+def _same(cfg, gpu, cpu, what):
+    assert_same_state(gpu.export_state(), cpu.export_state(), species=cfg.num_metabolites, what=what)
+    assert_same_counters(gpu.counters(), cpu.counters(), what=what)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_lockstep_every_phase(product, seed):
+    """Prepare + two steps, comparing the whole state after every kernel."""
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(seed, n=900, nm=1800, box=42.0))
+    prep = [(abi.PHASE_SORT_PARTICLES, 0), (abi.PHASE_SORT_METABOLIC, 0), (abi.PHASE_REMOVE_INTERFERING, 0),
+            (abi.PHASE_COMPLEXIFY, -1)]
+    seq = prep + step_phases(cfg) * 2
+    for k, (ph, arg) in enumerate(seq):
+        gpu.run_phase(ph, arg)
+        cpu.run_phase(ph, arg)
+        _same(cfg, gpu, cpu, f"after phase #{k} ({ph}, {arg})")
+
+
+def test_sort_permutation_and_ranges(product):
+    """Stable sort permutation and the reference's gridRanges layout."""
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(5, n=1200, nm=2500, box=45.0))
+    gpu.prepare()
+    cpu.prepare()
+    for step in range(2):
+        for which, ph in ((0, abi.PHASE_SORT_PARTICLES), (1, abi.PHASE_SORT_METABOLIC)):
+            gpu.run_phase(ph)
+            cpu.run_phase(ph)
+            rg, pg = gpu.export_grid(which)
+            rc, pc = cpu.export_grid(which)
+            assert np.array_equal(pg, pc), f"permutation differs (set {which})"
+            assert np.array_equal(rg, rc), f"cell ranges differ (set {which})"
+        gpu.step(1)
+        cpu.step(1)
+
+
+@pytest.mark.parametrize("species", [10, 8])
+def test_whole_steps(product, species):
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(7, n=1500, nm=3000, box=48.0, species=species))
+    gpu.prepare()
+    cpu.prepare()
+    gpu.step(3)
+    cpu.step(3)
+    _same(cfg, gpu, cpu, "after 3 steps")
+    rg = gpu.reduce_frame()
+    rc = cpu.reduce_frame()
+    assert rg[0].tobytes() == rc[0].tobytes(), "reduced particle frame differs"
+    assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
+
+
+def test_measured_workload_small(product):
+    """The measured workload's physics at a reduced size (same density)."""
+    cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
+                                 seed=3)
+    rng = np.random.default_rng(3)
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    p = scenes.uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
+    m = scenes.uniform_metabolic(rng, cfg.num_metabolic_particles, cfg.sim_size, types, cfg.num_metabolites)
+    cfg_, gpu, cpu = _engines(product, (cfg, types, rules, p, m, len(p)))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, "measured workload, 2 steps")
+    gp, _ = gpu.export_state()
+    assert (gp["n_active_interactions"] > 0).sum() > 0, "the A+B rule formed no bond"
+
+
+def test_deterministic(product):
+    scene = scenes.test_scene(9, n=1000, nm=2000, box=40.0)
+    runs = []
+    for _ in range(2):
+        cfg, types, rules, p, m, nid = scene
+        s = product.Simulation(cfg, types, rules)
+        s.load_state(p, m, next_particle_id=nid)
+        s.prepare()
+        s.step(2)
+        runs.append(s.export_state())
+        s.close()
+    assert runs[0][0].tobytes() == runs[1][0].tobytes()
+    assert runs[0][1].tobytes() == runs[1][1].tobytes()
