@@ -223,11 +223,12 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
     p["angular_velocity"][:, 3] += 8.0           # near-identity angular velocities
     p["angular_velocity"] /= np.linalg.norm(p["angular_velocity"], axis=1, keepdims=True)
     p["state"] = rng.choice([0, 0, 0, 1, 2, 3], size=n)
-    # chains: consecutive ids placed along a random walk
-    pos = 0
+    # chains: consecutive ids placed along a straight segment
+    c0, r0, t0 = int(0.07 * n), int(0.6 * n), int(0.8 * n)   # where chains, bonded pairs, the test bond go
+    assert n >= 300, "the differential scene needs at least 300 particles"
     for c in range(6):
         length = 8
-        start = 100 + c * 20
+        start = c0 + c * 20
         q = rng.random(3) * (box - 12) + 6
         step = rng.normal(size=3)
         step /= np.linalg.norm(step)
@@ -239,7 +240,7 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
         _link_serially(p, start, start + length)
     # rule bonds already formed (both directions), including one that transitions
     for k in range(10):
-        a, b = 300 + 2 * k, 301 + 2 * k
+        a, b = r0 + 2 * k, r0 + 1 + 2 * k
         p[a]["type"], p[b]["type"] = (TYPE_A, TYPE_B) if k % 2 == 0 else (CTRL, MONO)
         for i in (a, b):
             p[i]["radius"] = types["radius"][p[i]["type"]]
@@ -253,8 +254,8 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
         if k % 2 == 1:
             p[a]["state"] = 1
     # a test bond (interaction type 0) between two close particles
-    p[400]["pos"] = p[401]["pos"] + np.float32(2.0)
-    for i, j in ((400, 401), (401, 400)):
+    p[t0]["pos"] = p[t0 + 1]["pos"] + np.float32(2.0)
+    for i, j in ((t0, t0 + 1), (t0 + 1, t0)):
         kk = p[i]["n_active_interactions"]
         p[i]["interactions"][kk] = (0, -1, p[j]["id"])
         p[i]["n_active_interactions"] = kk + 1
