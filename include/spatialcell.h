@@ -279,6 +279,31 @@ void *sc_get_stream(sc_sim *sim);
 int sc_reduce_frame(sc_sim *sim, sc_reduced_particle *particles,
                     sc_reduced_metabolic_particle *metabolic);
 
+/* ---- allocation-free cell sort (no counterpart in the reference) ----
+ * For callers that cannot let a library allocate device memory: a framework
+ * that owns the GPU's memory as its own pool, or a loop that cannot absorb
+ * the device-wide synchronisation of cudaMalloc / cudaFree.  Runs the binning
+ * of a sim's sort -- cell key of every item, stable onesweep radix sort, cell
+ * start table -- on buffers the caller owns; its working memory is one fixed
+ * static device array inside the library.
+ *   pos:  n float4 (x, y, z, radius), device memory
+ *   info: n int4 (id, type, flags, hydrophobic); only bit 0 of flags (active)
+ *         is read; device memory
+ *   perm: n uint32 out, the input index of every sorted slot
+ *   cell_start: cells + 1 uint32 out, cells = n_grid_cells^3 (sc_config_grid):
+ *         first sorted slot of every cell (a cell's items are
+ *         [cell_start[c], cell_start[c + 1]); inactive items come last)
+ *   stream: a cudaStream_t (NULL: the legacy default stream)
+ * Limit: n <= 262144; larger n returns SC_E_INVALID and launches nothing.
+ * The static array (about 4.3 MB) stays on every GPU that loads the library
+ * until the process exits.  All calls on a GPU share it, so calls whose work
+ * overlaps on that GPU race; order them on one stream.  The first call on a
+ * device looks up the array's address with that device current, and should
+ * come before any stream capture on the device.  Returns once the results
+ * are in perm / cell_start; SC_E_DEVICE if the sort reported an error. */
+int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info, int32_t n, uint32_t *perm,
+                         uint32_t *cell_start, void *stream);
+
 /* ---- frames.dat (storage.cuh:9-44) ---- */
 int sc_frames_write_header(void *file /* FILE* */, const sc_config *cfg);
 int sc_frames_write_frame(void *file /* FILE* */, const sc_config *cfg,

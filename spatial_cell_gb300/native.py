@@ -39,6 +39,7 @@ _SIGS = {
     "sc_get_stream": (ctypes.c_void_p, [_P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
     "sc_frames_write_frame": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config), _P, _P]),
+    "sc_sort_cells_static": (ctypes.c_int, [ctypes.POINTER(abi.Config), _P, _P, ctypes.c_int32, _P, _P, _P]),
 }
 
 # Every symbol include/spatialcell.h declares.
