@@ -177,7 +177,10 @@ typedef struct sc_config {
     int32_t report_every_nth_frame;
     /* extensions */
     int32_t num_metabolites;  /* simulated species S, 1..10 (reference: 10) */
-    int32_t _reserved;
+    int32_t periodic;         /* 0: the reference's walls (positions clamped to
+                                 [0, simSize]); 1: periodic box (minimum-image
+                                 pairs, wrapped cells and positions; needs at
+                                 least 3 cells per axis) */
     uint64_t seed;            /* Philox key of the Brownian noise */
 } sc_config;
 

@@ -114,6 +114,8 @@ struct scp_sim {
     std::vector<int32_t> pidx;      // partner index, 2 * (max rule id + 1)
     std::vector<sc_rule> prules;    // partner-mapped rules
     int nActive = 0, lastActive = -1, nextId = 0, nActiveM = 0, step = 0;
+    bool periodic = false;   // periodic box extension (cfg.periodic)
+    int nUsed = 2;           // cells per axis that hold positions, ceil(simSize / cell)
 
     const sc_rule &rule(int id) const {
         static const sc_rule z = zero_rule();
@@ -122,17 +124,32 @@ struct scp_sim {
     uint32_t cell_key(uint32_t gx, uint32_t gy, uint32_t gz) const {
         return (gx << (2 * nbits)) | (gy << nbits) | gz;
     }
+    // cells per axis the cell index clamps to: the power-of-two grid of
+    // config.cuh:65-74, or in a periodic box the cells the box spans
+    int idx_limit() const { return periodic ? nUsed : ngrid; }
     uint32_t key_of(sc_f3 pos) const {
         float c = cfg.grid_cell_size;
-        return cell_key(sc_grid_idx(pos.x, c, ngrid), sc_grid_idx(pos.y, c, ngrid), sc_grid_idx(pos.z, c, ngrid));
+        int n = idx_limit();
+        return cell_key(sc_grid_idx(pos.x, c, n), sc_grid_idx(pos.y, c, n), sc_grid_idx(pos.z, c, n));
     }
+    // position of a neighbour as seen from pos (its nearest periodic image)
+    sc_f3 img(sc_f3 t, sc_f3 pos) const { return periodic ? sc_image3(t, pos, cfg.sim_size) : t; }
     // Visits the 27 (clamped) cells around pos in the reference's gx, gy, gz
     // order; per cell calls f(key).
     template <class F>
     void cells27(sc_f3 pos, F &&f) const {
         float c = cfg.grid_cell_size;
-        int cx = (int)sc_grid_idx(pos.x, c, ngrid), cy = (int)sc_grid_idx(pos.y, c, ngrid),
-            cz = (int)sc_grid_idx(pos.z, c, ngrid);
+        int n = idx_limit();
+        int cx = (int)sc_grid_idx(pos.x, c, n), cy = (int)sc_grid_idx(pos.y, c, n), cz = (int)sc_grid_idx(pos.z, c, n);
+        if (periodic) {
+            // offsets -1, 0, +1 per axis, wrapped (the order of a periodic scan)
+            for (int ox = -1; ox <= 1; ox++)
+                for (int oy = -1; oy <= 1; oy++)
+                    for (int oz = -1; oz <= 1; oz++)
+                        f(cell_key((uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n),
+                                   (uint32_t)((cz + oz + n) % n)));
+            return;
+        }
         for (int gx = std::max(cx - 1, 0); gx <= std::min(cx + 1, ngrid - 1); gx++)
             for (int gy = std::max(cy - 1, 0); gy <= std::min(cy + 1, ngrid - 1); gy++)
                 for (int gz = std::max(cz - 1, 0); gz <= std::min(cz + 1, ngrid - 1); gz++)
@@ -243,7 +260,7 @@ void apply_velocities(const scp_sim &s, std::vector<T> &items, int n, float f) {
     for (int i = 0; i < n; i++) {
         T &p = items[i];
         if (!(p.flags & kActive)) continue;
-        p.pos = clamp(p.pos + p.vel * f, 0.0f, s.cfg.sim_size);
+        p.pos = s.periodic ? sc_wrap3(p.pos + p.vel * f, s.cfg.sim_size) : clamp(p.pos + p.vel * f, 0.0f, s.cfg.sim_size);
         p.vel *= s.cfg.velocity_decay;
         p.rot = sc_qmul(sc_slerp(sc_qid(), p.angVel, f), p.rot);
         p.rot /= length(p.rot);
@@ -267,7 +284,7 @@ void coordinate_noise(scp_sim &s, float frac) {
             if (j == i) return;
             const PP &tp = cur[j];
             if (!(tp.flags & kActive)) return;
-            sc_f3 delta = tp.pos - p.pos;
+            sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
             if (outside_cube(delta, lim)) return;
             for (int k = 0; k < p.nb; k++) {
                 const sc_interaction &it = p.bonds[k];
@@ -309,8 +326,12 @@ void relax(scp_sim &s) {
         const sc_f3 nextUp = sc_rotate(up, p.angVel);
         s.scan(s.rangesP, p.pos, [&](int j) {
             if (j == i) return;
-            const PP &tp = cur[j];
-            if (!(tp.flags & kActive)) return;
+            const PP &tp0 = cur[j];
+            if (!(tp0.flags & kActive)) return;
+            PP timg;
+            const PP *tq = &tp0;
+            if (s.periodic) { timg = tp0; timg.pos = s.img(tp0.pos, p.pos); tq = &timg; }
+            const PP &tp = *tq;
             sc_f3 delta = tp.pos - p.pos;
             if (outside_cube(delta, lim)) return;
             sc_f3 nd = normalize(delta);
@@ -431,27 +452,29 @@ void relax_metab(scp_sim &s) {
                 if ((int)j == i) continue;
                 const PM &tp = cur[j];
                 if (!(tp.flags & kActive)) continue;
-                sc_f3 delta = tp.pos - p.pos;
+                sc_f3 tpos = s.img(tp.pos, p.pos);
+                sc_f3 delta = tpos - p.pos;
                 if (outside_cube(delta, lim)) continue;
                 sc_f3 nd = normalize(delta);
                 float dist = sc_norm3(delta);
                 float cd = metab_collision_dist(p.radius, tp.radius);
                 if (dist <= cd) {
                     w += 1.0f;
-                    dV += (tp.pos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 1.0f;
+                    dV += (tpos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 1.0f;
                 }
             }
             for (uint32_t j = s.rangesP[2 * (size_t)key]; j < s.rangesP[2 * (size_t)key + 1]; j++) {
                 const PP &tp = parts[j];
                 if (!(tp.flags & kActive) || tp.type != SC_PARTICLE_TYPE_LIPID) continue;
-                sc_f3 delta = tp.pos - p.pos;
+                sc_f3 tpos = s.img(tp.pos, p.pos);
+                sc_f3 delta = tpos - p.pos;
                 if (outside_cube(delta, lim)) continue;
                 sc_f3 nd = normalize(delta);
                 float dist = sc_norm3(delta);
                 float cd = metab_collision_dist(p.radius, tp.radius);
                 if (dist <= cd) {
                     w += 2.0f;
-                    dV += (tp.pos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 2.0f;
+                    dV += (tpos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 2.0f;
                 }
             }
         });
@@ -477,14 +500,15 @@ void relax_partners(scp_sim &s) {
         s.scan(s.rangesM, p.pos, [&](int j) {
             const PM &tp = met[j];
             if (!(tp.flags & kActive)) return;
-            sc_f3 delta = tp.pos - p.pos;
+            sc_f3 tpos = s.img(tp.pos, p.pos);
+            sc_f3 delta = tpos - p.pos;
             if (outside_cube(delta, lim)) return;
             sc_f3 nd = normalize(delta);
             float dist = sc_norm3(delta);
             float cd = metab_collision_dist(p.radius, tp.radius);
             if (dist <= cd) {
                 w += 2.0f;
-                dV += (tp.pos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 2.0f;
+                dV += (tpos - nd * cd + tp.vel - (p.pos + p.vel)) * 0.9f * 2.0f;
             }
         });
         p.vel += dV / fmaxf(w, 1.0f);
@@ -533,7 +557,7 @@ void complexify(scp_sim &s) {
                 if (j == i) return;
                 const PP &tp = cur[j];
                 if (!(tp.flags & kActive)) return;
-                sc_f3 delta = tp.pos - p.pos;
+                sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
                 if (outside_cube(delta, lim)) return;
                 sc_f3 tup = sc_rotate(sc_up(), tp.rot);
                 for (int k = cs; k < ce; k++) {
@@ -580,7 +604,7 @@ void transition(scp_sim &s) {
             if (j == i) return;
             const PP &tp = cur[j];
             if (!(tp.flags & kActive)) return;
-            sc_f3 delta = tp.pos - p.pos;
+            sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
             if (outside_cube(delta, lim)) return;
             sc_f3 tup = sc_rotate(sc_up(), tp.rot);
             for (int k = 0; k < p.nb; k++) {
@@ -672,8 +696,9 @@ void polymerize(scp_sim &s) {
                 int newId = s.nextId++;
                 sc_f3 rp = rule_pos(poly);
                 sc_f4 ro = rule_ori(poly);
-                PP np = make_particle(newId, newType, ti.radius, ti.hydrophobic,
-                                      p.pos + sc_rotate(p.type < newType ? rp : -rp, p.rot),
+                sc_f3 npos = p.pos + sc_rotate(p.type < newType ? rp : -rp, p.rot);
+                if (s.periodic) npos = sc_wrap3(npos, s.cfg.sim_size);
+                PP np = make_particle(newId, newType, ti.radius, ti.hydrophobic, npos,
                                       sc_qmul(p.rot, p.type < newType ? ro : sc_qinv(ro)));
                 if (newState >= 0) { np.state = (int8_t)newState; np.lscs = s.step; }
                 np.bonds[np.nb] = {p.spoly, poly.group, p.id};
@@ -742,7 +767,7 @@ void diffuse(scp_sim &s) {
             if (j == i) return;
             const PM &tp = cur[j];
             if (!(tp.flags & kActive)) return;
-            sc_f3 delta = tp.pos - p.pos;
+            sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
             if (outside_cube(delta, lim)) return;
             float dist = sc_norm3(delta);
             if (dist <= lim) {
@@ -772,7 +797,7 @@ void remove_interfering(scp_sim &s) {
         s.scan(s.rangesP, p.pos, [&](int j) {
             const PP &tp = parts[j];
             if (!(tp.flags & kActive) || tp.type != SC_PARTICLE_TYPE_LIPID) return;
-            sc_f3 delta = tp.pos - p.pos;
+            sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
             if (outside_cube(delta, lim)) return;
             float dist = sc_norm3(delta);
             float interf = (float)((double)(p.radius + tp.radius) + 0.001);
@@ -869,6 +894,9 @@ scp_sim *scp_create(const sc_config *cfg, const sc_type_info *types, int n_types
     while (p2 < ng) { p2 *= 2; bits++; }
     s->ngrid = p2;
     s->nbits = bits;
+    s->periodic = cfg->periodic != 0;
+    s->nUsed = ng;
+    if (s->periodic && ng < 3) { delete s; return nullptr; }
     s->cells = (size_t)p2 * p2 * p2;
     s->N = cfg->num_particles;
     s->Nm = cfg->num_metabolic_particles;

@@ -35,6 +35,36 @@
 #define SC_THREADS 256
 #define SC_ACTIVE SC_PARTICLE_FLAG_ACTIVE
 
+// Pair lists.  Between a sort and applyVelocities no position, flag, type,
+// radius or interaction changes, so the pairs that contribute to
+// coordinateNoise / relax / relaxMetabolicParticles /
+// relaxMetabolicParticlePartners are fixed for all of their sub-iterations
+// (16 / 32 / 16 / 16 launches); likewise the diffusion pairs between
+// applyVelocities and the next sort (8 launches).  Each list holds, per item
+// and in the reference's visiting order, the candidate slots that pass every
+// position-only test of the kernel, with the branch the pair takes.  Entries
+// are tiled by warps of 32 items: entry k of item i is at
+// ((i / 32) * K + k) * 32 + i % 32, so the 32 threads of a warp read one
+// 128-byte line per k and all K entries of a warp sit in one K*128-byte block
+// (one page, where a k-major layout would put each k of an item in a different
+// page).  An item with more pairs than the list holds is marked by a count
+// above the capacity and its kernels scan its neighbourhood instead.
+#define SC_LIST_PP 32   // particle-particle: rule/chain/test bonds, polar pairs, collisions
+#define SC_LIST_M 96    // metabolic: colliding metabolic particles and lipids
+#define SC_LIST_LM 48   // lipid <- metabolic collisions
+#define SC_LIST_D 96    // metabolic diffusion partners
+#define SC_PP_POLAR 0x80000000u
+#define SC_PP_PARTNER 0x40000000u
+#define SC_PP_COLLIDE 0x20000000u
+#define SC_PP_INDEX 0x1FFFFFFFu
+#define SC_M_FROM_P 0x80000000u
+#define SC_M_INDEX 0x7FFFFFFFu
+
+__host__ __device__ __forceinline__ size_t sc_list_at(int K, int i, int k) {
+    return ((size_t)(i >> 5) * (size_t)K + (size_t)k) * 32 + (size_t)(i & 31);
+}
+__host__ __device__ __forceinline__ size_t sc_list_words(int K, int cap) { return (size_t)((cap + 31) / 32) * 32 * K; }
+
 // Device-side error codes (sticky, first one wins).
 #define SC_DERR_LOOKBACK_TIMEOUT 1
 #define SC_DERR_POLY_OVERFLOW 2
@@ -66,7 +96,20 @@ struct ScParams {
     const sc_rule *prules;    // partner-mapped rules
     const sc_type_info *types;
     int nTypes;
+    int listLimit;            // effective pair-list capacity (<= each list's size; smaller only in tests)
+    int periodic;             // periodic box extension (sc_config.periodic)
+    int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
 };
+
+// Cells per axis the cell index clamps to: the power-of-two grid of
+// config.cuh:65-74, or in a periodic box the cells the box spans.
+__host__ __device__ __forceinline__ int cell_limit(const ScParams &P) { return P.periodic ? P.nUsed : P.ngrid; }
+
+// A neighbour's position as seen from p: itself, or in a periodic box its
+// nearest image.
+__device__ __forceinline__ sc_f3 img(const ScParams &P, sc_f3 t, sc_f3 p) {
+    return P.periodic ? sc_image3(t, p, P.simSize) : t;
+}
 
 __device__ __forceinline__ sc_f4 ld4(const float4 *p, int i) {
     float4 v = p[i];
@@ -112,9 +155,29 @@ __device__ __forceinline__ uint32_t cell_key(const ScParams &P, uint32_t gx, uin
 // the visiting order is exactly the reference's.
 template <class F>
 __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__restrict__ cellStart, sc_f3 pos, F &&f) {
-    int n = P.ngrid;
+    int n = cell_limit(P);
     int cx = (int)sc_grid_idx(pos.x, P.cell, n), cy = (int)sc_grid_idx(pos.y, P.cell, n),
         cz = (int)sc_grid_idx(pos.z, P.cell, n);
+    if (P.periodic) {
+        // offsets -1, 0, +1 per axis, wrapped; the z run of a column is one
+        // slot range unless it wraps
+        for (int ox = -1; ox <= 1; ox++) {
+            for (int oy = -1; oy <= 1; oy++) {
+                uint32_t base = cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n), 0);
+                if (cz >= 1 && cz <= n - 2) {
+                    for (uint32_t j = cellStart[base | (uint32_t)(cz - 1)], e = cellStart[(base | (uint32_t)(cz + 1)) + 1];
+                         j < e; j++)
+                        f((int)j);
+                } else {
+                    for (int oz = -1; oz <= 1; oz++) {
+                        uint32_t key = base | (uint32_t)((cz + oz + n) % n);
+                        for (uint32_t j = cellStart[key], e = cellStart[key + 1]; j < e; j++) f((int)j);
+                    }
+                }
+            }
+        }
+        return;
+    }
     int x0 = max(cx - 1, 0), x1 = min(cx + 1, n - 1);
     int y0 = max(cy - 1, 0), y1 = min(cy + 1, n - 1);
     uint32_t z0 = (uint32_t)max(cz - 1, 0), z1 = (uint32_t)min(cz + 1, n - 1);
@@ -131,9 +194,17 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
 // arrays cell by cell, metabolites.cuh:174-248).
 template <class F>
 __device__ __forceinline__ void cells27(const ScParams &P, sc_f3 pos, F &&f) {
-    int n = P.ngrid;
+    int n = cell_limit(P);
     int cx = (int)sc_grid_idx(pos.x, P.cell, n), cy = (int)sc_grid_idx(pos.y, P.cell, n),
         cz = (int)sc_grid_idx(pos.z, P.cell, n);
+    if (P.periodic) {
+        for (int ox = -1; ox <= 1; ox++)
+            for (int oy = -1; oy <= 1; oy++)
+                for (int oz = -1; oz <= 1; oz++)
+                    f(cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n),
+                               (uint32_t)((cz + oz + n) % n)));
+        return;
+    }
     for (int gx = max(cx - 1, 0); gx <= min(cx + 1, n - 1); gx++)
         for (int gy = max(cy - 1, 0); gy <= min(cy + 1, n - 1); gy++)
             for (int gz = max(cz - 1, 0); gz <= min(cz + 1, n - 1); gz++)

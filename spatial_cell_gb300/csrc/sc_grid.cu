@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_sort_keys(const float4 *__restri
         uint32_t k = inactiveKey;
         if (info[i].z & SC_ACTIVE) {
             sc_f3 p = ld3(pos, i);
-            k = cell_key(P, sc_grid_idx(p.x, P.cell, P.ngrid), sc_grid_idx(p.y, P.cell, P.ngrid),
-                         sc_grid_idx(p.z, P.cell, P.ngrid));
+            int lim = cell_limit(P);
+            k = cell_key(P, sc_grid_idx(p.x, P.cell, lim), sc_grid_idx(p.y, P.cell, lim), sc_grid_idx(p.z, P.cell, lim));
         }
         keys[i] = k;
         for (int d = 0; d < passes; d++) atomicAdd(&sh[d * 256 + ((k >> (8 * d)) & 0xffu)], 1u);

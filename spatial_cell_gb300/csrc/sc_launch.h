@@ -38,6 +38,11 @@ struct ScBuffers {
     uint32_t *keysP[2], *valsP[2], *keysM[2], *valsM[2], *hist, *lookback;
     int sortCurP, sortCurM;
     uint32_t *cellStartP, *cellStartM;
+    // pair lists (sc_dev.cuh) and whether each matches the current state
+    uint32_t *listPP, *listM, *listLM, *listD;
+    int *cntPP, *cntM, *cntLM, *cntD;
+    bool validPP, validM, validLM, validD;
+    void invalidateLists() { validPP = validM = validLM = validD = false; }
     // polymerisation list
     int *polyList;
     int polyCap;

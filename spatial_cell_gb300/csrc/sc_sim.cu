@@ -2,6 +2,7 @@
 // buffers, one CUDA stream and the launch sequence of the step loop
 // (main.cu:347-661), with no host synchronisation inside a step.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -232,8 +233,24 @@ void sort_metabolic(sc_sim *s) {
     B.flipAllM();
 }
 
+// Which pair lists a phase invalidates (it changes positions, flags, types,
+// radii or interactions their tests read, or re-sorts slots they index).
+void invalidate_after(ScBuffers &B, int phase) {
+    switch (phase) {
+        case SC_PHASE_SORT_PARTICLES: B.validPP = B.validM = B.validLM = false; break;
+        case SC_PHASE_SORT_METABOLIC: B.validM = B.validLM = B.validD = false; break;
+        case SC_PHASE_APPLY_VELOCITIES: B.invalidateLists(); break;
+        case SC_PHASE_COMPLEXIFY:
+        case SC_PHASE_TRANSITION:
+        case SC_PHASE_POLYMERIZE: B.validPP = B.validLM = false; break;
+        case SC_PHASE_REMOVE_INTERFERING: B.validM = B.validLM = B.validD = false; break;
+        default: break;
+    }
+}
+
 int run_phase(sc_sim *s, int phase, int arg) {
     ScLaunchCtx c = ctx(s);
+    invalidate_after(s->B, phase);
     switch (phase) {
         case SC_PHASE_SORT_PARTICLES: sort_particles(s); break;
         case SC_PHASE_SORT_METABOLIC: sort_metabolic(s); break;
@@ -301,6 +318,10 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         return set_err(nullptr, SC_E_INVALID, "negative interaction distance");
     if (cfg->noise_coordination_steps < 0 || cfg->relaxation_steps < 0 || cfg->metabolite_diffusion_steps < 0)
         return set_err(nullptr, SC_E_INVALID, "negative sub-iteration count");
+    // The periodic extension wraps neighbourhoods over the cells the box
+    // spans; with fewer than three a cell would be visited twice.
+    if (cfg->periodic && ceilf(cfg->sim_size / cfg->grid_cell_size) < 3.0f)
+        return set_err(nullptr, SC_E_INVALID, "a periodic box needs at least 3 grid cells per axis");
 
     sc_sim *s = new sc_sim();
     s->cfg = *cfg;
@@ -325,6 +346,12 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.Nm = cfg->num_metabolic_particles;
     P.coordSteps = cfg->noise_coordination_steps;
     P.seed = cfg->seed;
+    // SC_PAIR_LIST_LIMIT caps the pair lists (tests use it to run the
+    // neighbourhood-scan path of every kernel); unset means full capacity.
+    P.listLimit = 1 << 30;
+    P.periodic = cfg->periodic != 0;
+    P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
+    if (const char *lim = getenv("SC_PAIR_LIST_LIMIT")) P.listLimit = std::max(0, atoi(lim));
 
     auto bail = [&](int rc) {
         sc_destroy(s);
@@ -403,8 +430,13 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
         (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.redP, N)) ||
-        (rc = dalloc(s, &B.redM, Nm)))
+        (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
+        (rc = dalloc(s, &B.cntPP, N)) || (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
+        (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
+        (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||
+        (rc = dalloc(s, &B.cntD, Nm)))
         return bail(rc);
+    B.invalidateLists();
     B.polyCap = 4096;
     cudaMemset(B.ctr, 0, sizeof(ScCounters));
     cudaMemset(B.cellStartP, 0, ((size_t)P.cells + 1) * 4);
@@ -442,6 +474,7 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
     if (rc) return rc;
     ScBuffers &B = s->B;
+    B.invalidateLists();
     for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
     if (N > 0) {

@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_apply_velocities(const int *__re
     float4 p4 = pos[i];
     sc_f3 p = sc_make_f3(p4.x, p4.y, p4.z);
     sc_f3 v = ld3(vel, i);
-    p = clamp(p + v * f, 0.0f, P.simSize);
+    p = P.periodic ? sc_wrap3(p + v * f, P.simSize) : clamp(p + v * f, 0.0f, P.simSize);
     v *= P.velDecay;
     sc_f4 av = ld4(angvel, i);
     sc_f4 r = sc_qmul(sc_slerp(sc_qid(), av, f), ld4(rot, i));
@@ -86,51 +86,147 @@ __global__ void __launch_bounds__(SC_THREADS) k_apply_velocities(const int *__re
     st4(angvel, i, av);
 }
 
-// ---- dynamics.cuh:288-402 coordinateNoise -----------------------------------
-__global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
-    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
-    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
-    const int *__restrict__ bonds, const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn,
-    float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
+// ---- pair lists ------------------------------------------------------------------
+// The list of item i is read as entries list[k * cap + i], k < cnt[i]; cnt[i]
+// above the list's capacity means "scan instead".
+template <int K>
+struct PairList {
+    const uint32_t *__restrict__ list;
+    const int *__restrict__ cnt;
+    int cap;
+};
+
+// Bonds of one particle held in registers.
+struct BondRegs {
+    int n;
+    int t[SC_MAX_ACTIVE_INTERACTIONS], g[SC_MAX_ACTIVE_INTERACTIONS], p[SC_MAX_ACTIVE_INTERACTIONS];
+    __device__ __forceinline__ void load(const int *__restrict__ nb, const int *__restrict__ bonds, int i) {
+        n = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+#pragma unroll
+        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+            const int *b = bonds + (size_t)i * 24 + 3 * k;
+            t[k] = k < n ? b[0] : 0;
+            g[k] = k < n ? b[1] : 0;
+            p[k] = k < n ? b[2] : 0;
+        }
+    }
+    __device__ __forceinline__ bool has_partner(int id) const {
+        bool r = false;
+#pragma unroll
+        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
+            if (k < n && p[k] == id) r = true;
+        return r;
+    }
+};
+
+// The position-only tests of relax for candidate j of particle i
+// (dynamics.cuh:452-478, 584-589, 775-777): returns the entry flags, 0 if
+// the pair contributes nothing.
+__device__ __forceinline__ uint32_t pp_flags(const ScParams &P, int i, int j, sc_f3 ppos, float prad, int phydro,
+                                             const BondRegs &B, const float4 *__restrict__ pos,
+                                             const int4 *__restrict__ info) {
+    if (j == i) return 0;
+    int4 tin = info[j];
+    if (!(tin.z & SC_ACTIVE)) return 0;
+    float4 t4 = pos[j];
+    sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
+    if (outside_cube(delta, P.maxInt)) return 0;
+    float dist = sc_norm3(delta);
+    float s = prad + t4.w;
+    int thydro = (int)(int8_t)(tin.w & 0xff);
+    uint32_t f = 0;
+    if ((phydro > 0 || thydro > 0) && sc_within_lipid_range(dist, s) && phydro == SC_POLAR && thydro == SC_POLAR)
+        f |= SC_PP_POLAR;
+    bool partner = B.has_partner(tin.x);
+    if (partner) f |= SC_PP_PARTNER;
+    if (!partner && dist < s) f |= SC_PP_COLLIDE;
+    return f;
+}
+
+// Particle-particle list, built once after the sort; read by coordinateNoise
+// and relax.
+__global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint32_t *__restrict__ cellStart,
+                                                         const int *__restrict__ nActivePtr,
+                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
+                                                         const int *__restrict__ nb, const int *__restrict__ bonds,
+                                                         uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = info[i];
-    int pnb = nb[i];
+    if (!(in.z & SC_ACTIVE)) { cnt[i] = 0; return; }
+    BondRegs B;
+    B.load(nb, bonds, i);
+    float4 p4 = pos[i];
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const int phydro = (int)(int8_t)(in.w & 0xff);
+    int c = 0;
+    scan27(P, cellStart, ppos, [&](int j) {
+        uint32_t f = pp_flags(P, i, j, ppos, p4.w, phydro, B, pos, info);
+        if (f) {
+            if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
+            c++;
+        }
+    });
+    cnt[i] = c;
+}
+
+// Visits the contributing pairs of particle i in the reference's order: from
+// the list, or (list overflow) by scanning.
+template <class F>
+__device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__restrict__ cellStart,
+                                       const PairList<SC_LIST_PP> &L, int i, sc_f3 ppos, float prad, int phydro,
+                                       const BondRegs &B, const float4 *__restrict__ pos,
+                                       const int4 *__restrict__ info, F &&f) {
+    int c = L.cnt[i];
+    if (c <= min(SC_LIST_PP, P.listLimit)) {
+        for (int k = 0; k < c; k++) {
+            uint32_t e = L.list[sc_list_at(SC_LIST_PP, i, k)];
+            f((int)(e & SC_PP_INDEX), e);
+        }
+    } else {
+        scan27(P, cellStart, ppos, [&](int j) {
+            uint32_t fl = pp_flags(P, i, j, ppos, prad, phydro, B, pos, info);
+            if (fl) f(j, fl);
+        });
+    }
+}
+
+// ---- dynamics.cuh:288-402 coordinateNoise -----------------------------------
+// Only interaction partners change anything; they are the PARTNER entries of
+// the particle-particle list, in the reference's visiting order.
+__global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
+    const int *__restrict__ bonds, PairList<SC_LIST_PP> L, const float4 *__restrict__ pnIn,
+    const float4 *__restrict__ anIn, float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = info[i];
     float4 pn4 = pnIn[i], an4 = anIn[i];
-    if (!(in.z & SC_ACTIVE) || pnb < 1) {
+    if (!(in.z & SC_ACTIVE) || nb[i] < 1) {
         pnOut[i] = pn4;
         anOut[i] = an4;
         return;
     }
-    pnb = min(pnb, SC_MAX_ACTIVE_INTERACTIONS);
-    int bt[SC_MAX_ACTIVE_INTERACTIONS], bp[SC_MAX_ACTIVE_INTERACTIONS];
-#pragma unroll
-    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-        bt[k] = k < pnb ? bonds[(size_t)i * 24 + 3 * k] : 0;
-        bp[k] = k < pnb ? bonds[(size_t)i * 24 + 3 * k + 2] : 0;
-    }
+    BondRegs B;
+    B.load(nb, bonds, i);
     float4 p4 = pos[i];
-    sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
-    float prad = p4.w;
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
     sc_f3 ppn = sc_make_f3(pn4.x, pn4.y, pn4.z);
     sc_f4 pan = sc_make_f4(an4.x, an4.y, an4.z, an4.w);
     sc_f3 dPN = sc_zero3();
     sc_f4 dAN = sc_qid();
     float w = 0.0f;
-    const float lim = P.maxInt;
-    scan27(P, cellStart, ppos, [&](int j) {
-        if (j == i) return;
-        int4 tin = info[j];
-        if (!(tin.z & SC_ACTIVE)) return;
-        float4 t4 = pos[j];
-        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
-        if (outside_cube(delta, lim)) return;
+    for_pp(P, cellStart, L, i, ppos, prad, (int)(int8_t)(in.w & 0xff), B, pos, info, [&](int j, uint32_t fl) {
+        if (!(fl & SC_PP_PARTNER)) return;
+        const int tid_ = info[j].x;
+        const float trad = pos[j].w;
 #pragma unroll
         for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-            if (k >= pnb) break;
-            if (bt[k] < 10 && frac > 0.25f) continue;
-            if (bp[k] == tin.x) {
-                float trad = t4.w;
+            if (k >= B.n) break;
+            if (B.t[k] < 10 && frac > 0.25f) continue;
+            if (B.p[k] == tid_) {
                 sc_f3 tpn = ld3(pnIn, j);
                 sc_f4 tan_ = ld4(anIn, j);
                 float pMag = length(ppn);
@@ -151,9 +247,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
 __global__ void __launch_bounds__(SC_THREADS) k_relax(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
-    const int *__restrict__ bonds, const float4 *__restrict__ velIn, const float4 *__restrict__ rotIn,
-    const float4 *__restrict__ avIn, float4 *__restrict__ velOut, float4 *__restrict__ rotOut,
-    float4 *__restrict__ avOut, float4 *__restrict__ dbg) {
+    const int *__restrict__ bonds, PairList<SC_LIST_PP> L, const float4 *__restrict__ velIn,
+    const float4 *__restrict__ rotIn, const float4 *__restrict__ avIn, float4 *__restrict__ velOut,
+    float4 *__restrict__ rotOut, float4 *__restrict__ avOut, float4 *__restrict__ dbg) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = info[i];
@@ -171,15 +267,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
     sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
     sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
     const int pid = in.x, ptype = in.y, phydro = (int)(int8_t)(in.w & 0xff);
-    const int pnb = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
-    int bt[SC_MAX_ACTIVE_INTERACTIONS], bg[SC_MAX_ACTIVE_INTERACTIONS], bp[SC_MAX_ACTIVE_INTERACTIONS];
-#pragma unroll
-    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-        const int *b = bonds + (size_t)i * 24 + 3 * k;
-        bt[k] = k < pnb ? b[0] : 0;
-        bg[k] = k < pnb ? b[1] : 0;
-        bp[k] = k < pnb ? b[2] : 0;
-    }
+    BondRegs B;
+    B.load(nb, bonds, i);
     sc_f4 pdbg = sc_make_f4(0, 0, 0, 0);
     bool dbgTouched = false;
     sc_f3 dV = sc_zero3();
@@ -189,115 +278,109 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
     float w = 0.0f;
     const sc_f3 up = sc_rotate(sc_up(), prot);
     const sc_f3 nextUp = sc_rotate(up, pav);
-    const float lim = P.maxInt;
     const float flex = SC_PI_REF / 8;
-    scan27(P, cellStart, ppos, [&](int j) {
-        if (j == i) return;
-        int4 tin = info[j];
-        if (!(tin.z & SC_ACTIVE)) return;
+    for_pp(P, cellStart, L, i, ppos, prad, phydro, B, pos, info, [&](int j, uint32_t fl) {
         float4 t4 = pos[j];
-        const sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
-        sc_f3 delta = tpos - ppos;
-        if (outside_cube(delta, lim)) return;
+        const sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos);
         const float trad = t4.w;
-        const int tid_ = tin.x, ttype = tin.y, thydro = (int)(int8_t)(tin.w & 0xff);
-        sc_f3 nd = normalize(delta);
-        float dist = sc_norm3(delta);
-        float idist = prad + trad;
-        if (phydro > 0 || thydro > 0) {
-            if (sc_within_lipid_range(dist, prad + trad) && phydro == SC_POLAR && thydro == SC_POLAR) {
-                sc_f3 tvel = ld3(velIn, j);
-                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
-                sc_f3 pPV = -nextUp * prad + ppos + pvel;
-                sc_f3 tpPV = -nextTup * trad + tpos + tvel;
-                float L = length(tpPV - pPV) / (prad + trad);
-                float attr = (float)(fmin(fmax((double)L, 1e-6), (double)2.0f) / (double)2.0f);
-                w += 1.0f;
-                dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
-                float pap = sc_powf(fminf(1.0f / fmaxf(L, 1e-6f), 10.0f) / 10.0f, 0.2f);
-                phobSum += pap;
-                phobPos += tpPV * pap;
-            }
+        const float idist = prad + trad;
+        if (fl & SC_PP_POLAR) {
+            // dynamics.cuh:478-582: polar (lipid) head / tail attraction
+            sc_f3 tvel = ld3(velIn, j);
+            sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+            sc_f3 pPV = -nextUp * prad + ppos + pvel;
+            sc_f3 tpPV = -nextTup * trad + tpos + tvel;
+            float Lr = length(tpPV - pPV) / (prad + trad);
+            float attr = (float)(fmin(fmax((double)Lr, 1e-6), (double)2.0f) / (double)2.0f);
+            w += 1.0f;
+            dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
+            float pap = sc_powf(fminf(1.0f / fmaxf(Lr, 1e-6f), 10.0f) / 10.0f, 0.2f);
+            phobSum += pap;
+            phobPos += tpPV * pap;
         }
-        bool partners = false;
+        if (fl & SC_PP_PARTNER) {
+            // dynamics.cuh:584-771: interaction partners
+            int4 tin = info[j];
+            const int tid_ = tin.x, ttype = tin.y;
 #pragma unroll
-        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-            if (k >= pnb) break;
-            if (bp[k] != tid_) continue;
-            partners = true;
-            const int it = bt[k];
-            if (it >= 10) {
-                const sc_rule &pii = rule_at(P, it);
-                sc_f4 ro = rule_ori(pii);
-                sc_f3 rp = rule_pos(pii);
-                sc_f4 trot = ld4(rotIn, j), tav = ld4(avIn, j);
-                sc_f3 tvel = ld3(velIn, j);
-                bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
-                sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
-                sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
-                sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
-                sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
-                dAV = sc_slerp(dAV, sc_qmul(sc_slerp(rro, orro, 0.5f), rro), 0.9f * trad / (prad + trad));
-                sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot)))
-                               : sc_rotate(rp, sc_qmul(tav, trot));
-                rrp += tpos;
-                sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot)))
-                                : sc_rotate(rp, sc_qmul(pav, prot));
-                orrp += ppos;
-                w += 1.0f;
-                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
-                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
-                dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
-            }
-            if (it == 0) {
-                if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
-                sc_f4 trot = ld4(rotIn, j);
-                bool o1 = p_order(ptype, pid, ttype, tid_);
-                sc_f4 trod = sc_qmul(sc_quat(sc_up(), -SC_PI_REF / 6), sc_quat(sc_right(), SC_PI_REF / 6));
-                prot = sc_slerp(prot, o1 ? sc_qmul(trot, sc_qinv(trod)) : sc_qmul(trot, trod), 0.2f);
-                sc_f4 trpr = sc_quat(sc_forward(), -SC_PI_REF / 6);
-                sc_f3 rrp = o1 ? -sc_rotate(sc_up(), sc_qmul(trot, sc_qmul(sc_qinv(trod), trpr)))
-                               : sc_rotate(sc_up(), sc_qmul(trot, trpr));
-                rrp *= idist;
-                rrp += tpos;
-                pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.2f));
-                pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.2f));
-                pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.2f));
-            } else if (it == SC_INTERACTION_TYPE_CHAIN) {
-                if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
-                sc_f3 tvel = ld3(velIn, j);
-                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
-                sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
-                bool fwd = bg[k] == SC_INTERACTION_GROUP_FORWARD;
-                dAV = sc_slerp(dAV, sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd), 0.9f * trad / (prad + trad));
-                sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
-                sc_f3 axis = sc_safe_cross(relUp, -nnd);
-                float ang = sc_angle3(relUp, -nnd);
-                sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
-                rrp *= idist;
-                rrp += tpos;
-                sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
-                sc_f3 oaxis = sc_safe_cross(oUp, nnd);
-                float oang = sc_angle3(oUp, nnd);
-                sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
-                orrp *= idist;
-                orrp += ppos;
-                w += 1.0f;
-                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
-                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
-                dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
-                pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.9f));
-                pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.9f));
-                pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.9f));
+            for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+                if (k >= B.n) break;
+                if (B.p[k] != tid_) continue;
+                const int it = B.t[k];
+                if (it >= 10) {
+                    const sc_rule &pii = rule_at(P, it);
+                    sc_f4 ro = rule_ori(pii);
+                    sc_f3 rp = rule_pos(pii);
+                    sc_f4 trot = ld4(rotIn, j), tav = ld4(avIn, j);
+                    sc_f3 tvel = ld3(velIn, j);
+                    bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
+                    sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
+                    sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
+                    sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
+                    sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
+                    dAV = sc_slerp(dAV, sc_qmul(sc_slerp(rro, orro, 0.5f), rro), 0.9f * trad / (prad + trad));
+                    sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot)))
+                                   : sc_rotate(rp, sc_qmul(tav, trot));
+                    rrp += tpos;
+                    sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot)))
+                                    : sc_rotate(rp, sc_qmul(pav, prot));
+                    orrp += ppos;
+                    w += 1.0f;
+                    sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                    sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                    dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+                }
+                if (it == 0) {
+                    if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
+                    sc_f4 trot = ld4(rotIn, j);
+                    bool o1 = p_order(ptype, pid, ttype, tid_);
+                    sc_f4 trod = sc_qmul(sc_quat(sc_up(), -SC_PI_REF / 6), sc_quat(sc_right(), SC_PI_REF / 6));
+                    prot = sc_slerp(prot, o1 ? sc_qmul(trot, sc_qinv(trod)) : sc_qmul(trot, trod), 0.2f);
+                    sc_f4 trpr = sc_quat(sc_forward(), -SC_PI_REF / 6);
+                    sc_f3 rrp = o1 ? -sc_rotate(sc_up(), sc_qmul(trot, sc_qmul(sc_qinv(trod), trpr)))
+                                   : sc_rotate(sc_up(), sc_qmul(trot, trpr));
+                    rrp *= idist;
+                    rrp += tpos;
+                    pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.2f));
+                    pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.2f));
+                    pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.2f));
+                } else if (it == SC_INTERACTION_TYPE_CHAIN) {
+                    if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
+                    sc_f3 tvel = ld3(velIn, j);
+                    sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+                    sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
+                    bool fwd = B.g[k] == SC_INTERACTION_GROUP_FORWARD;
+                    dAV = sc_slerp(dAV, sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd),
+                                   0.9f * trad / (prad + trad));
+                    sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
+                    sc_f3 axis = sc_safe_cross(relUp, -nnd);
+                    float ang = sc_angle3(relUp, -nnd);
+                    sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
+                    rrp *= idist;
+                    rrp += tpos;
+                    sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
+                    sc_f3 oaxis = sc_safe_cross(oUp, nnd);
+                    float oang = sc_angle3(oUp, nnd);
+                    sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
+                    orrp *= idist;
+                    orrp += ppos;
+                    w += 1.0f;
+                    sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                    sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                    dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+                    pdbg.x = (float)((double)pdbg.x + (double)(rrp.x - ppos.x) * (1.0 - (double)0.9f));
+                    pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.9f));
+                    pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.9f));
+                }
             }
         }
-        if (!partners) {
+        if (fl & SC_PP_COLLIDE) {
+            // dynamics.cuh:775-786: soft collision with a non-partner
+            sc_f3 nd = normalize(tpos - ppos);
             float cd = prad + trad;
-            if (dist < cd) {
-                sc_f3 tvel = ld3(velIn, j);
-                w += 1.0f;
-                dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
-            }
+            sc_f3 tvel = ld3(velIn, j);
+            w += 1.0f;
+            dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
         }
     });
     sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
@@ -328,11 +411,53 @@ struct CollisionDistCache {
 };
 
 // ---- metabolites.cuh:140-264 relaxMetabolicParticles ----------------------
+// List: per metabolic item, cell by cell, the colliding metabolic items then
+// the colliding lipids (SC_M_FROM_P), as the reference's loops visit them.
+__global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
+                                                        const uint32_t *__restrict__ cellStartP,
+                                                        const int *__restrict__ nActivePtr,
+                                                        const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                                        const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                        uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    if (!(minfo[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
+    float4 p4 = mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w, lim = P.maxInt;
+    CollisionDistCache cm, cp;
+    int c = 0;
+    cells27(P, pp, [&](uint32_t key) {
+        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
+            if ((int)j == i || !(minfo[j].z & SC_ACTIVE)) continue;
+            float4 t4 = mpos[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (sc_norm3(delta) <= cm.get(prad, t4.w)) {
+                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j;
+                c++;
+            }
+        }
+        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
+            int4 tin = pinfo[j];
+            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+            float4 t4 = ppos_[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (sc_norm3(delta) <= cp.get(prad, t4.w)) {
+                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j | SC_M_FROM_P;
+                c++;
+            }
+        }
+    });
+    cnt[i] = c;
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab(
     ScParams P, const uint32_t *__restrict__ cellStartM, const uint32_t *__restrict__ cellStartP,
     const int *__restrict__ nActivePtr, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-    const float4 *__restrict__ mvelIn, float4 *__restrict__ mvelOut, const float4 *__restrict__ ppos_,
-    const int4 *__restrict__ pinfo, const float4 *__restrict__ pvel_) {
+    PairList<SC_LIST_M> L, const float4 *__restrict__ mvelIn, float4 *__restrict__ mvelOut,
+    const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, const float4 *__restrict__ pvel_) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     float4 v4 = mvelIn[i];
@@ -346,50 +471,101 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab(
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    const float lim = P.maxInt;
     CollisionDistCache cm, cp;
-    cells27(P, pp, [&](uint32_t key) {
-        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
-            if ((int)j == i) continue;
-            if (!(minfo[j].z & SC_ACTIVE)) continue;
-            float4 t4 = mpos[j];
-            sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
-            sc_f3 delta = tpos - pp;
-            if (outside_cube(delta, lim)) continue;
-            sc_f3 nd = normalize(delta);
-            float dist = sc_norm3(delta);
-            float cd = cm.get(prad, t4.w);
-            if (dist <= cd) {
+    const int c = L.cnt[i];
+    if (c <= min(SC_LIST_M, P.listLimit)) {
+        for (int k = 0; k < c; k++) {
+            uint32_t e = L.list[sc_list_at(SC_LIST_M, i, k)];
+            int j = (int)(e & SC_M_INDEX);
+            if (!(e & SC_M_FROM_P)) {
+                float4 t4 = mpos[j];
+                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+                sc_f3 nd = normalize(tpos - pp);
+                float cd = cm.get(prad, t4.w);
                 w += 1.0f;
                 dV += (tpos - nd * cd + ld3(mvelIn, j) - (pp + pv)) * 0.9f * 1.0f;
-            }
-        }
-        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
-            int4 tin = pinfo[j];
-            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
-            float4 t4 = ppos_[j];
-            sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
-            sc_f3 delta = tpos - pp;
-            if (outside_cube(delta, lim)) continue;
-            sc_f3 nd = normalize(delta);
-            float dist = sc_norm3(delta);
-            float cd = cp.get(prad, t4.w);
-            if (dist <= cd) {
+            } else {
+                float4 t4 = ppos_[j];
+                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+                sc_f3 nd = normalize(tpos - pp);
+                float cd = cp.get(prad, t4.w);
                 w += 2.0f;
                 dV += (tpos - nd * cd + ld3(pvel_, j) - (pp + pv)) * 0.9f * 2.0f;
             }
         }
-    });
+    } else {
+        const float lim = P.maxInt;
+        cells27(P, pp, [&](uint32_t key) {
+            for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
+                if ((int)j == i) continue;
+                if (!(minfo[j].z & SC_ACTIVE)) continue;
+                float4 t4 = mpos[j];
+                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+                sc_f3 delta = tpos - pp;
+                if (outside_cube(delta, lim)) continue;
+                sc_f3 nd = normalize(delta);
+                float dist = sc_norm3(delta);
+                float cd = cm.get(prad, t4.w);
+                if (dist <= cd) {
+                    w += 1.0f;
+                    dV += (tpos - nd * cd + ld3(mvelIn, j) - (pp + pv)) * 0.9f * 1.0f;
+                }
+            }
+            for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
+                int4 tin = pinfo[j];
+                if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+                float4 t4 = ppos_[j];
+                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+                sc_f3 delta = tpos - pp;
+                if (outside_cube(delta, lim)) continue;
+                sc_f3 nd = normalize(delta);
+                float dist = sc_norm3(delta);
+                float cd = cp.get(prad, t4.w);
+                if (dist <= cd) {
+                    w += 2.0f;
+                    dV += (tpos - nd * cd + ld3(pvel_, j) - (pp + pv)) * 0.9f * 2.0f;
+                }
+            }
+        });
+    }
     st3(mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
 // ---- metabolites.cuh:266-350 relaxMetabolicParticlePartners ----------------
 // Only lipids change, and only their own velocity, which no other thread of
-// this kernel reads: updated in place.
+// this kernel reads: updated in place.  List: the colliding metabolic items.
+__global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
+                                                         const int *__restrict__ nActivePtr,
+                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                                         uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    int4 in = pinfo[i];
+    if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) { cnt[i] = 0; return; }
+    float4 p4 = ppos_[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w, lim = P.maxInt;
+    CollisionDistCache cc;
+    int c = 0;
+    scan27(P, cellStartM, pp, [&](int j) {
+        if (!(minfo[j].z & SC_ACTIVE)) return;
+        float4 t4 = mpos[j];
+        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+        if (outside_cube(delta, lim)) return;
+        if (sc_norm3(delta) <= cc.get(prad, t4.w)) {
+            if (c < min(SC_LIST_LM, P.listLimit)) list[sc_list_at(SC_LIST_LM, i, c)] = (uint32_t)j;
+            c++;
+        }
+    });
+    cnt[i] = c;
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     ScParams P, const uint32_t *__restrict__ cellStartM, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
-    const float4 *__restrict__ mpos, const int4 *__restrict__ minfo, const float4 *__restrict__ mvel) {
+    PairList<SC_LIST_LM> L, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+    const float4 *__restrict__ mvel) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = pinfo[i];
@@ -401,22 +577,30 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    const float lim = P.maxInt;
     CollisionDistCache cc;
-    scan27(P, cellStartM, pp, [&](int j) {
-        if (!(minfo[j].z & SC_ACTIVE)) return;
-        float4 t4 = mpos[j];
-        sc_f3 tpos = sc_make_f3(t4.x, t4.y, t4.z);
-        sc_f3 delta = tpos - pp;
-        if (outside_cube(delta, lim)) return;
-        sc_f3 nd = normalize(delta);
-        float dist = sc_norm3(delta);
+    auto body = [&](int j, float4 t4) {
+        sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+        sc_f3 nd = normalize(tpos - pp);
         float cd = cc.get(prad, t4.w);
-        if (dist <= cd) {
-            w += 2.0f;
-            dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
+        w += 2.0f;
+        dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
+    };
+    const int c = L.cnt[i];
+    if (c <= min(SC_LIST_LM, P.listLimit)) {
+        for (int k = 0; k < c; k++) {
+            int j = (int)L.list[sc_list_at(SC_LIST_LM, i, k)];
+            body(j, mpos[j]);
         }
-    });
+    } else {
+        const float lim = P.maxInt;
+        scan27(P, cellStartM, pp, [&](int j) {
+            if (!(minfo[j].z & SC_ACTIVE)) return;
+            float4 t4 = mpos[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) return;
+            if (sc_norm3(delta) <= cc.get(prad, t4.w)) body(j, t4);
+        });
+    }
     st3(pvel_, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
@@ -472,7 +656,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
         int4 tin = info[j];
         if (!(tin.z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
-        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
+        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
         if (outside_cube(delta, lim)) return;
         sc_f4 trot = ld4(rot, j);
         sc_f3 tup = sc_rotate(sc_up(), trot);
@@ -533,7 +717,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
             int4 tin = info[j];
             if (!(tin.z & SC_ACTIVE)) return;
             float4 t4 = pos[j];
-            sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - ppos;
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
             if (outside_cube(delta, lim)) return;
             bool loaded = false;
             sc_f4 trot;
@@ -653,6 +837,7 @@ __device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFi
             sc_f4 ro = rule_ori(poly);
             sc_f4 prot = ld4(F.rot, i);
             sc_f3 npos = ppos + sc_rotate(ptype < newType ? rp : -rp, prot);
+            if (P.periodic) npos = sc_wrap3(npos, P.simSize);
             sc_f4 nrot = sc_qmul(prot, ptype < newType ? ro : sc_qinv(ro));
             // Particle(newId, newType, 0, radius, hydrophobic, pos, rot): types.cuh:192-221
             F.pos[newIdx] = make_float4(npos.x, npos.y, npos.z, nr);
@@ -771,11 +956,38 @@ __global__ void __launch_bounds__(1024) k_polymerize(ScParams P, const uint32_t 
 }
 
 // ---- metabolites.cuh:352-431 diffuseMetabolites ------------------------------
+// List: the metabolic items within maxDiffusionDistance (cube, then sphere),
+// built after applyVelocities and read by all diffusion sub-iterations.
+__global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32_t *__restrict__ cellStart,
+                                                        const int *__restrict__ nActivePtr,
+                                                        const float4 *__restrict__ pos, const int4 *__restrict__ info,
+                                                        uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    if (!(info[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
+    float4 p4 = pos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float lim = P.maxDiff;
+    int c = 0;
+    scan27(P, cellStart, pp, [&](int j) {
+        if (j == i || !(info[j].z & SC_ACTIVE)) return;
+        float4 t4 = pos[j];
+        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+        if (outside_cube(delta, lim)) return;
+        if (sc_norm3(delta) <= lim) {
+            if (c < min(SC_LIST_D, P.listLimit)) list[sc_list_at(SC_LIST_D, i, c)] = (uint32_t)j;
+            c++;
+        }
+    });
+    cnt[i] = c;
+}
+
 template <int SP>
 __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32_t *__restrict__ cellStart,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
-                                                        const float4 *__restrict__ metIn, float4 *__restrict__ metOut) {
+                                                        PairList<SC_LIST_D> L, const float4 *__restrict__ metIn,
+                                                        float4 *__restrict__ metOut) {
     constexpr int Q = SP / 4;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
@@ -790,36 +1002,41 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
         for (int q = 0; q < Q; q++) metOut[(size_t)i * Q + q] = metIn[(size_t)i * Q + q];
         return;
     }
-    float4 p4 = pos[i];
-    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     float dm[SP];
 #pragma unroll
     for (int k = 0; k < SP; k++) dm[k] = 0.0f;
     const int S = P.S;
-    const float lim = P.maxDiff;
-    scan27(P, cellStart, pp, [&](int j) {
-        if (j == i) return;
-        if (!(info[j].z & SC_ACTIVE)) return;
-        float4 t4 = pos[j];
-        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - pp;
-        if (outside_cube(delta, lim)) return;
-        float dist = sc_norm3(delta);
-        if (dist <= lim) {
+    auto body = [&](int j) {
 #pragma unroll
-            for (int q = 0; q < Q; q++) {
-                float4 v = metIn[(size_t)j * Q + q];
-                float tm[4] = {v.x, v.y, v.z, v.w};
+        for (int q = 0; q < Q; q++) {
+            float4 v = metIn[(size_t)j * Q + q];
+            float tm[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    int k = 4 * q + c;
-                    if (k < S) {
-                        float diff = tm[c] - pm[k];
-                        if (sc_diffuse_exceeds(diff)) dm[k] += diff * 0.1f;
-                    }
+            for (int c = 0; c < 4; c++) {
+                int k = 4 * q + c;
+                if (k < S) {
+                    float diff = tm[c] - pm[k];
+                    if (sc_diffuse_exceeds(diff)) dm[k] += diff * 0.1f;
                 }
             }
         }
-    });
+    };
+    const int c = L.cnt[i];
+    if (c <= min(SC_LIST_D, P.listLimit)) {
+        for (int k = 0; k < c; k++) body((int)L.list[sc_list_at(SC_LIST_D, i, k)]);
+    } else {
+        float4 p4 = pos[i];
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const float lim = P.maxDiff;
+        scan27(P, cellStart, pp, [&](int j) {
+            if (j == i) return;
+            if (!(info[j].z & SC_ACTIVE)) return;
+            float4 t4 = pos[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) return;
+            if (sc_norm3(delta) <= lim) body(j);
+        });
+    }
 #pragma unroll
     for (int k = 0; k < SP; k++)
         if (k < S) pm[k] += dm[k];
@@ -848,7 +1065,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
         int4 tin = pinfo[j];
         if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) return;
         float4 t4 = ppos_[j];
-        sc_f3 delta = sc_make_f3(t4.x, t4.y, t4.z) - pp;
+        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
         if (outside_cube(delta, lim)) return;
         float dist = sc_norm3(delta);
         float interf = (float)((double)(prad + t4.w) + 0.001);
@@ -917,13 +1134,32 @@ void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic) {
     (*c.launches)++;
 }
 
+static void ensure_pp(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (B.validPP) return;
+    PFields F = B.P();
+    k_build_pp<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
+                                                         F.bonds, B.listPP, B.cntPP, c.P.N);
+    (*c.launches)++;
+    B.validPP = true;
+}
+
+static PairList<SC_LIST_PP> pp_list(const ScLaunchCtx &c) {
+    PairList<SC_LIST_PP> L;
+    L.list = c.B->listPP;
+    L.cnt = c.B->cntPP;
+    L.cap = c.P.N;
+    return L;
+}
+
 void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
+    ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
     k_coordinate_noise<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info,
-                                                                 F.nb, F.bonds, F.posnoise, F.angnoise, X.posnoise,
-                                                                 X.angnoise, frac);
+                                                                 F.nb, F.bonds, pp_list(c), F.posnoise, F.angnoise,
+                                                                 X.posnoise, X.angnoise, frac);
     B.cp[FP_POSNOISE] ^= 1;
     B.cp[FP_ANGNOISE] ^= 1;
     (*c.launches)++;
@@ -948,9 +1184,10 @@ void sc_phase_apply_noise(ScLaunchCtx &c) {
 void sc_phase_relax(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
+    ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
     k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds,
-                                                      F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg);
+                                                      pp_list(c), F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg);
     B.cp[FP_VEL] ^= 1;
     B.cp[FP_ROT] ^= 1;
     B.cp[FP_ANGVEL] ^= 1;
@@ -962,8 +1199,18 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     if (c.P.Nm <= 0) return;
     MFields M = B.M(), X = B.Mnext();
     PFields F = B.P();
+    if (!B.validM) {
+        k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
+                                                             M.info, F.pos, F.info, B.listM, B.cntM, c.P.Nm);
+        (*c.launches)++;
+        B.validM = true;
+    }
+    PairList<SC_LIST_M> L;
+    L.list = B.listM;
+    L.cnt = B.cntM;
+    L.cap = c.P.Nm;
     k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
-                                                             M.info, M.vel, X.vel, F.pos, F.info, F.vel);
+                                                             M.info, L, M.vel, X.vel, F.pos, F.info, F.vel);
     B.cm[FM_VEL] ^= 1;
     (*c.launches)++;
 }
@@ -973,8 +1220,18 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     if (c.P.N <= 0) return;
     MFields M = B.M();
     PFields F = B.P();
+    if (!B.validLM) {
+        k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos,
+                                                             M.info, B.listLM, B.cntLM, c.P.N);
+        (*c.launches)++;
+        B.validLM = true;
+    }
+    PairList<SC_LIST_LM> L;
+    L.list = B.listLM;
+    L.cnt = B.cntLM;
+    L.cap = c.P.N;
     k_relax_partners<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
-                                                               F.vel, M.pos, M.info, M.vel);
+                                                               F.vel, L, M.pos, M.info, M.vel);
     (*c.launches)++;
 }
 
@@ -1031,18 +1288,28 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.Nm <= 0) return;
     MFields M = B.M(), X = B.Mnext();
+    if (!B.validD) {
+        k_build_d<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+                                                             B.listD, B.cntD, c.P.Nm);
+        (*c.launches)++;
+        B.validD = true;
+    }
+    PairList<SC_LIST_D> L;
+    L.list = B.listD;
+    L.cnt = B.cntD;
+    L.cap = c.P.Nm;
     switch (c.P.SP) {
         case 4:
             k_diffuse<4><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                                   M.met, X.met);
+                                                                   L, M.met, X.met);
             break;
         case 8:
             k_diffuse<8><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                                   M.met, X.met);
+                                                                   L, M.met, X.met);
             break;
         default:
             k_diffuse<12><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
-                                                                    M.info, M.met, X.met);
+                                                                    M.info, L, M.met, X.met);
             break;
     }
     B.cm[FM_MET] ^= 1;

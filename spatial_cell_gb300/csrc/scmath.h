@@ -481,6 +481,22 @@ SC_HD bool sc_within_lipid_range(float dist, float s) {
     return (double)dist <= (double)s + 0.8 * (double)s * 0.5;
 }
 
+// ---------------------------------------------------------------------------
+// Periodic box (an extension; the reference clamps positions to its walls).
+// A neighbour's position is replaced by its nearest periodic image relative
+// to the item, so every pair expression keeps its reference form.
+// ---------------------------------------------------------------------------
+SC_HD float sc_image1(float t, float p, float L) {
+    float d = t - p, h = L * 0.5f;
+    return d > h ? t - L : (d < -h ? t + L : t);
+}
+SC_HD sc_f3 sc_image3(sc_f3 t, sc_f3 p, float L) {
+    return sc_make_f3(sc_image1(t.x, p.x, L), sc_image1(t.y, p.y, L), sc_image1(t.z, p.z, L));
+}
+// Brings a coordinate displaced by less than one box length back into [0, L].
+SC_HD float sc_wrap1(float x, float L) { return x >= L ? x - L : (x < 0.0f ? x + L : x); }
+SC_HD sc_f3 sc_wrap3(sc_f3 v, float L) { return sc_make_f3(sc_wrap1(v.x, L), sc_wrap1(v.y, L), sc_wrap1(v.z, L)); }
+
 // The reference's cell index (grid.cuh:13-17): min((uint)(c / cell), n - 1).
 // The float -> unsigned conversion saturates as the GPU's cvt.rzi.u32.f32
 // does (negative and NaN -> 0), which keeps the host build defined too.

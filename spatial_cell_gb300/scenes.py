@@ -122,7 +122,7 @@ def workload_config(name, **overrides):
     w = WORKLOADS[name]
     kw = dict(num_particles=w["n"], num_metabolic_particles=w["nm"], sim_size=w["box"], grid_cell_size=6.0,
               max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=w["seed"],
-              steps=200 if name == "plain_small" else 1000)
+              steps=200 if name == "plain_small" else 1000, periodic=1)
     kw.update(overrides)
     return abi.make_config(**kw)
 
@@ -201,7 +201,7 @@ def _link_serially(p, start, end, itype=abi.INTERACTION_TYPE_CHAIN):
         b["n_active_interactions"] = k + 1
 
 
-def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
+def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, periodic=0):
     """A dense small box with uniform particles of all kinds, a few wrapped
     chains, pre-bonded rule pairs, a test bond, and metabolites.  Returns
     (config, types, rules, particles, metabolic, next_particle_id)."""
@@ -265,5 +265,5 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64):
     cfg = abi.make_config(num_particles=n + capacity_slack, num_metabolic_particles=nm + 16, sim_size=box,
                           grid_cell_size=6.0, max_interaction_distance=5.5, max_diffusion_distance=6.0,
                           num_metabolites=species, seed=1000 + seed, noise_coordination_steps=4,
-                          relaxation_steps=6, metabolite_diffusion_steps=3, steps=10)
+                          relaxation_steps=6, metabolite_diffusion_steps=3, steps=10, periodic=periodic)
     return cfg, types, rules, p, m, n

@@ -31,7 +31,7 @@ def scene_workload():
     n, nm = 1000, 2000
     box = float(635.0 * (n / 2097152) ** (1.0 / 3.0))
     cfg = scenes.workload_config("plain_large", num_particles=n, num_metabolic_particles=nm, sim_size=box,
-                                 num_metabolites=10, seed=77)
+                                 num_metabolites=10, seed=77, periodic=0)
     rng = np.random.default_rng(77)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, n, box, types)

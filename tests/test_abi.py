@@ -133,7 +133,8 @@ def test_invalid_arguments_rejected_before_cuda(product):
     h = ctypes.c_void_p()
     types = np.zeros(4, abi.TYPE_INFO_DTYPE)
     for kw in (dict(num_metabolites=0), dict(num_metabolites=11), dict(num_particles=-1),
-               dict(grid_cell_size=0.0), dict(sim_size=1e6, grid_cell_size=0.5), dict(relaxation_steps=-1)):
+               dict(grid_cell_size=0.0), dict(sim_size=1e6, grid_cell_size=0.5), dict(relaxation_steps=-1),
+               dict(periodic=1, sim_size=12.0, grid_cell_size=6.0)):
         cfg = abi.make_config(**kw)
         rc = L.sc_create(ctypes.byref(cfg), abi.ptr(types), 4, None, 0, ctypes.byref(h))
         assert rc == -1, kw

@@ -31,10 +31,11 @@ def _same(cfg, gpu, cpu, what):
     assert_same_counters(gpu.counters(), cpu.counters(), what=what)
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_lockstep_every_phase(product, seed):
-    """Prepare + two steps, comparing the whole state after every kernel."""
-    cfg, gpu, cpu = _engines(product, scenes.test_scene(seed, n=900, nm=1800, box=42.0))
+@pytest.mark.parametrize("seed,periodic", [(0, 0), (1, 0), (2, 1), (3, 1)])
+def test_lockstep_every_phase(product, seed, periodic):
+    """Prepare + two steps, comparing the whole state after every kernel
+    (reference walls, and the periodic box extension)."""
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(seed, n=900, nm=1800, box=42.0, periodic=periodic))
     prep = [(abi.PHASE_SORT_PARTICLES, 0), (abi.PHASE_SORT_METABOLIC, 0), (abi.PHASE_REMOVE_INTERFERING, 0),
             (abi.PHASE_COMPLEXIFY, -1)]
     seq = prep + step_phases(cfg) * 2
@@ -61,9 +62,10 @@ def test_sort_permutation_and_ranges(product):
         cpu.step(1)
 
 
-@pytest.mark.parametrize("species", [10, 8])
-def test_whole_steps(product, species):
-    cfg, gpu, cpu = _engines(product, scenes.test_scene(7, n=1500, nm=3000, box=48.0, species=species))
+@pytest.mark.parametrize("species,periodic", [(10, 0), (8, 0), (8, 1)])
+def test_whole_steps(product, species, periodic):
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(7, n=1500, nm=3000, box=48.0, species=species,
+                                                        periodic=periodic))
     gpu.prepare()
     cpu.prepare()
     gpu.step(3)
@@ -75,10 +77,11 @@ def test_whole_steps(product, species):
     assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
 
 
-def test_measured_workload_small(product):
+@pytest.mark.parametrize("periodic", [1, 0])
+def test_measured_workload_small(product, periodic):
     """The measured workload's physics at a reduced size (same density)."""
     cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
-                                 seed=3)
+                                 seed=3, periodic=periodic)
     rng = np.random.default_rng(3)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
@@ -105,3 +108,16 @@ def test_deterministic(product):
         s.close()
     assert runs[0][0].tobytes() == runs[1][0].tobytes()
     assert runs[0][1].tobytes() == runs[1][1].tobytes()
+
+
+@pytest.mark.parametrize("limit,periodic", [("0", 0), ("2", 0), ("2", 1)])
+def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic):
+    """Items whose pair list overflows are handled by scanning their
+    neighbourhood; with the list capacity capped, both paths run side by side
+    and must still match the oracle bit for bit."""
+    monkeypatch.setenv("SC_PAIR_LIST_LIMIT", limit)
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, f"2 steps with pair lists capped at {limit}")
