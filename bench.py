@@ -159,15 +159,22 @@ def per_phase_times(sim, stream, torch, reps=3):
     return out
 
 
+def sub_box(workload, frac):
+    """Overrides giving a frac-volume box of the workload at its densities."""
+    if frac == 1.0:
+        return {}
+    cfg0 = scenes.workload_config(workload)
+    return dict(num_particles=max(1024, int(cfg0.num_particles * frac)),
+                num_metabolic_particles=max(1024, int(cfg0.num_metabolic_particles * frac)),
+                sim_size=float(cfg0.sim_size * frac ** (1.0 / 3.0)))
+
+
 def cpu_sample(args, reps=1):
     """Times the CPU oracle on a same-density sub-box of the workload."""
     from oracle import engine as oengine
     frac = args.cpu_fraction
-    cfg0 = scenes.workload_config(args.workload)
-    n = max(1024, int(cfg0.num_particles * frac))
-    nm = max(1024, int(cfg0.num_metabolic_particles * frac))
-    box = float(cfg0.sim_size * frac ** (1.0 / 3.0))
-    cfg = scenes.workload_config(args.workload, num_particles=n, num_metabolic_particles=nm, sim_size=box)
+    cfg = scenes.workload_config(args.workload, **sub_box(args.workload, frac))
+    n, nm, box = cfg.num_particles, cfg.num_metabolic_particles, cfg.sim_size
     rng = np.random.default_rng(cfg.seed)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, n, box, types)
@@ -213,7 +220,8 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
-    cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=scenes.WORKLOADS[args.workload]["seed"] + rank)
+    cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=scenes.WORKLOADS[args.workload]["seed"] + rank,
+                                                    **sub_box(args.workload, args.fraction))
     N, Nm, S = cfg.num_particles, cfg.num_metabolic_particles, cfg.num_metabolites
     items = N + Nm
     # pinned host buffers for the end-to-end leg
@@ -295,7 +303,9 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded; no dataset in the reference)",
-            "config": {"workload": args.workload, "particles": N, "metabolic_particles": Nm,
+            "config": {"workload": args.workload if args.fraction == 1.0
+                       else f"{args.workload} (sub-box, {args.fraction:g} of its volume)",
+                       "particles": N, "metabolic_particles": Nm,
                        "box_nm": cfg.sim_size, "cell_nm": cfg.grid_cell_size, "species": S,
                        "sub_iterations": [cfg.noise_coordination_steps, cfg.relaxation_steps,
                                           cfg.metabolite_diffusion_steps],
@@ -326,6 +336,8 @@ def main():
     ap.add_argument("--workload", default="plain_large", choices=sorted(scenes.WORKLOADS))
     ap.add_argument("--cpu-fraction", type=float, default=1.0 / 16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fraction", type=float, default=1.0,
+                    help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

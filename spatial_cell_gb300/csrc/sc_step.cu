@@ -244,31 +244,34 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
 }
 
 // ---- dynamics.cuh:405-822 relax ------------------------------------------------
-__global__ void __launch_bounds__(SC_THREADS) k_relax(
-    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
-    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
-    const int *__restrict__ bonds, PairList<SC_LIST_PP> L, const float4 *__restrict__ velIn,
-    const float4 *__restrict__ rotIn, const float4 *__restrict__ avIn, float4 *__restrict__ velOut,
-    float4 *__restrict__ rotOut, float4 *__restrict__ avOut, float4 *__restrict__ dbg) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    int4 in = info[i];
-    float4 v4 = velIn[i], r4 = rotIn[i], a4 = avIn[i];
-    if (!(in.z & SC_ACTIVE)) {
-        velOut[i] = v4;
-        rotOut[i] = r4;
-        avOut[i] = a4;
-        return;
-    }
-    float4 p4 = pos[i];
+struct RelaxArgs {
+    const uint32_t *__restrict__ cellStart;
+    const int *__restrict__ nActivePtr;
+    const float4 *__restrict__ pos;
+    const int4 *__restrict__ info;
+    const int *__restrict__ nb;
+    const int *__restrict__ bonds;
+    PairList<SC_LIST_PP> L;
+    const float4 *__restrict__ velIn, *__restrict__ rotIn, *__restrict__ avIn;
+    float4 *__restrict__ velOut, *__restrict__ rotOut, *__restrict__ avOut, *__restrict__ dbg;
+};
+
+// One particle's relaxation.  SCAN = false reads the particle's pair list;
+// SCAN = true (list overflow) visits its 27 cells and applies the list's
+// tests to each candidate.  The bond loop reads the particle's bonds from
+// memory one at a time, so its body is emitted once.
+template <bool SCAN>
+__device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4, float4 r4,
+                                           float4 a4) {
+    float4 p4 = A.pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
     const float prad = p4.w;
     const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
     sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
     sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
     const int pid = in.x, ptype = in.y, phydro = (int)(int8_t)(in.w & 0xff);
-    BondRegs B;
-    B.load(nb, bonds, i);
+    const int nbi = min(max(A.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    const int *__restrict__ myBonds = A.bonds + (size_t)i * 24;
     sc_f4 pdbg = sc_make_f4(0, 0, 0, 0);
     bool dbgTouched = false;
     sc_f3 dV = sc_zero3();
@@ -279,15 +282,15 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
     const sc_f3 up = sc_rotate(sc_up(), prot);
     const sc_f3 nextUp = sc_rotate(up, pav);
     const float flex = SC_PI_REF / 8;
-    for_pp(P, cellStart, L, i, ppos, prad, phydro, B, pos, info, [&](int j, uint32_t fl) {
-        float4 t4 = pos[j];
+    auto body = [&](int j, uint32_t fl) {
+        float4 t4 = A.pos[j];
         const sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos);
         const float trad = t4.w;
         const float idist = prad + trad;
         if (fl & SC_PP_POLAR) {
             // dynamics.cuh:478-582: polar (lipid) head / tail attraction
-            sc_f3 tvel = ld3(velIn, j);
-            sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+            sc_f3 tvel = ld3(A.velIn, j);
+            sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(A.rotIn, j)), pav);
             sc_f3 pPV = -nextUp * prad + ppos + pvel;
             sc_f3 tpPV = -nextTup * trad + tpos + tvel;
             float Lr = length(tpPV - pPV) / (prad + trad);
@@ -299,20 +302,19 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
             phobPos += tpPV * pap;
         }
         if (fl & SC_PP_PARTNER) {
-            // dynamics.cuh:584-771: interaction partners
-            int4 tin = info[j];
+            // dynamics.cuh:584-771: interaction partners, in bond-slot order
+            int4 tin = A.info[j];
             const int tid_ = tin.x, ttype = tin.y;
-#pragma unroll
-            for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-                if (k >= B.n) break;
-                if (B.p[k] != tid_) continue;
-                const int it = B.t[k];
+#pragma unroll 1
+            for (int k = 0; k < nbi; k++) {
+                if (myBonds[3 * k + 2] != tid_) continue;
+                const int it = myBonds[3 * k];
                 if (it >= 10) {
                     const sc_rule &pii = rule_at(P, it);
                     sc_f4 ro = rule_ori(pii);
                     sc_f3 rp = rule_pos(pii);
-                    sc_f4 trot = ld4(rotIn, j), tav = ld4(avIn, j);
-                    sc_f3 tvel = ld3(velIn, j);
+                    sc_f4 trot = ld4(A.rotIn, j), tav = ld4(A.avIn, j);
+                    sc_f3 tvel = ld3(A.velIn, j);
                     bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
                     sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
                     sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
@@ -331,8 +333,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
                     dV += (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
                 }
                 if (it == 0) {
-                    if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
-                    sc_f4 trot = ld4(rotIn, j);
+                    if (!dbgTouched) { pdbg = ld4(A.dbg, i); dbgTouched = true; }
+                    sc_f4 trot = ld4(A.rotIn, j);
                     bool o1 = p_order(ptype, pid, ttype, tid_);
                     sc_f4 trod = sc_qmul(sc_quat(sc_up(), -SC_PI_REF / 6), sc_quat(sc_right(), SC_PI_REF / 6));
                     prot = sc_slerp(prot, o1 ? sc_qmul(trot, sc_qinv(trod)) : sc_qmul(trot, trod), 0.2f);
@@ -345,11 +347,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
                     pdbg.y = (float)((double)pdbg.y + (double)(rrp.y - ppos.y) * (1.0 - (double)0.2f));
                     pdbg.z = (float)((double)pdbg.z + (double)(rrp.z - ppos.z) * (1.0 - (double)0.2f));
                 } else if (it == SC_INTERACTION_TYPE_CHAIN) {
-                    if (!dbgTouched) { pdbg = ld4(dbg, i); dbgTouched = true; }
-                    sc_f3 tvel = ld3(velIn, j);
-                    sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(rotIn, j)), pav);
+                    if (!dbgTouched) { pdbg = ld4(A.dbg, i); dbgTouched = true; }
+                    sc_f3 tvel = ld3(A.velIn, j);
+                    sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(A.rotIn, j)), pav);
                     sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
-                    bool fwd = B.g[k] == SC_INTERACTION_GROUP_FORWARD;
+                    bool fwd = myBonds[3 * k + 1] == SC_INTERACTION_GROUP_FORWARD;
                     dAV = sc_slerp(dAV, sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd),
                                    0.9f * trad / (prad + trad));
                     sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
@@ -378,21 +380,62 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(
             // dynamics.cuh:775-786: soft collision with a non-partner
             sc_f3 nd = normalize(tpos - ppos);
             float cd = prad + trad;
-            sc_f3 tvel = ld3(velIn, j);
+            sc_f3 tvel = ld3(A.velIn, j);
             w += 1.0f;
             dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
         }
-    });
+    };
+    if (SCAN) {
+        BondRegs B;
+        B.load(A.nb, A.bonds, i);
+        scan27(P, A.cellStart, ppos, [&](int j) {
+            uint32_t fl = pp_flags(P, i, j, ppos, prad, phydro, B, A.pos, A.info);
+            if (fl) body(j, fl);
+        });
+    } else {
+        const int c = A.L.cnt[i];
+        for (int k = 0; k < c; k++) {
+            uint32_t e = A.L.list[sc_list_at(SC_LIST_PP, i, k)];
+            body((int)(e & SC_PP_INDEX), e);
+        }
+    }
     sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
     pav = sc_qmul(sc_slerp(sc_qid(), dAV, 1.0f / fmaxf(w, 1.0f)), pav);
     if (phobSum > 0.0f) {
         sc_f3 dir = normalize(phobPos / phobSum - (ppos + nv));
         pav = sc_slerp(pav, sc_quat_from_to(-up, dir), 0.2f);
     }
-    st3(velOut, i, nv, v4.w);
-    st4(rotOut, i, prot);
-    st4(avOut, i, pav);
-    if (dbgTouched) st4(dbg, i, pdbg);
+    st3(A.velOut, i, nv, v4.w);
+    st4(A.rotOut, i, prot);
+    st4(A.avOut, i, pav);
+    if (dbgTouched) st4(A.dbg, i, pdbg);
+}
+
+// Items whose list fits; the others are left to k_relax_overflow.
+__global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *A.nActivePtr) return;
+    int4 in = A.info[i];
+    float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
+    if (!(in.z & SC_ACTIVE)) {
+        A.velOut[i] = v4;
+        A.rotOut[i] = r4;
+        A.avOut[i] = a4;
+        return;
+    }
+    if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) return;
+    relax_item<false>(P, A, i, in, v4, r4, a4);
+}
+
+// Active items whose list overflowed: their neighbourhood is scanned.  A
+// separate kernel keeps the scan code out of k_relax's instruction stream.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, RelaxArgs A) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *A.nActivePtr) return;
+    if (A.L.cnt[i] <= min(SC_LIST_PP, P.listLimit)) return;
+    int4 in = A.info[i];
+    if (!(in.z & SC_ACTIVE)) return;
+    relax_item<true>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
 }
 
 // (float)((double)(rp + rt) + 0.8 * (double)rp) (metabolites.cuh:198,237,324),
@@ -1186,8 +1229,11 @@ void sc_phase_relax(ScLaunchCtx &c) {
     if (c.P.N <= 0) return;
     ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
-    k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds,
-                                                      pp_list(c), F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg);
+    RelaxArgs A{B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds, pp_list(c),
+                F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg};
+    k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax_overflow<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
+    (*c.launches)++;
     B.cp[FP_VEL] ^= 1;
     B.cp[FP_ROT] ^= 1;
     B.cp[FP_ANGVEL] ^= 1;

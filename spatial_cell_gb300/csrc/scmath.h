@@ -33,15 +33,20 @@
 
 #if defined(__CUDACC__)
 #define SC_HD __host__ __device__ __forceinline__
+// Long functions called from many sites are compiled once per kernel and
+// called, which keeps the kernels' instruction footprint small.
+#define SC_HD_COLD static __host__ __device__ __noinline__
 #define SC_ALIGN16 __align__(16)
 #else
 #define SC_HD static inline
+#define SC_HD_COLD static inline
 #define SC_ALIGN16 __attribute__((aligned(16)))
 #endif
 
 // ---------------------------------------------------------------------------
 // Vector types (layout-compatible with CUDA's float3 / float4)
 // ---------------------------------------------------------------------------
+struct sc_f2 { float x, y; };
 struct sc_f3 { float x, y, z; };
 struct SC_ALIGN16 sc_f4 { float x, y, z, w; };
 
@@ -161,7 +166,7 @@ SC_HD int sc_reduce_pio2(float x, float *r) {
     return (int)(((int64_t)kd) & 3);
 }
 
-SC_HD float sc_sinf(float x) {
+SC_HD_COLD float sc_sinf(float x) {
     if (!sc_isfinitef(x)) return x - x;  // NaN for +-inf and NaN
     if (x == 0.0f) return x;             // sin(+-0) = +-0
     float r;
@@ -169,7 +174,7 @@ SC_HD float sc_sinf(float x) {
     float s = sc_sin_poly(r), c = sc_cos_poly(r);
     return q == 0 ? s : q == 1 ? c : q == 2 ? -s : -c;
 }
-SC_HD float sc_cosf(float x) {
+SC_HD_COLD float sc_cosf(float x) {
     if (!sc_isfinitef(x)) return x - x;
     float r;
     int q = sc_reduce_pio2(x, &r);
@@ -203,7 +208,7 @@ SC_HD float sc_asin_poly(float z) {
 #define SC_PIO2_HI 1.5707963705062866f
 #define SC_PIO2_LO (-4.371138828673793e-08f)
 
-SC_HD float sc_acosf(float x) {
+SC_HD_COLD float sc_acosf(float x) {
     if (!(x == x)) return x;                       // NaN
     float ax = fabsf(x);
     if (ax > 1.0f) return (x - x) / (x - x);       // NaN outside the domain
@@ -273,7 +278,7 @@ SC_HD float sc_expf(float z) {
 
 // pow for x >= 0 (the step only raises non-negative bases to 0.2):
 // exp(y * log(x)) with the IEEE special cases of pow for those inputs.
-SC_HD float sc_powf(float x, float y) {
+SC_HD_COLD float sc_powf(float x, float y) {
     if (y == 0.0f) return 1.0f;
     if (!(x == x) || !(y == y)) return x + y;
     if (x == 1.0f) return 1.0f;
@@ -424,6 +429,18 @@ SC_HD sc_f4 sc_qinv(sc_f4 a) {
 }
 
 // math.cuh:220-262
+// The weights of slerp for an angle whose cosine is cosO (not near 1).
+SC_HD_COLD sc_f2 sc_slerp_weights(float cosO, float t, bool flip) {
+    float omega = sc_acosf(cosO);
+    float invSin = 1.0f / sc_sinf(omega);
+    float s1 = sc_sinf((1.0f - t) * omega) * invSin;
+    float s2 = flip ? -sc_sinf(t * omega) * invSin : sc_sinf(t * omega) * invSin;
+    sc_f2 r;
+    r.x = s1;
+    r.y = s2;
+    return r;
+}
+
 SC_HD sc_f4 sc_slerp(sc_f4 a, sc_f4 b, float t) {
     const float eps = 1e-6f;
     float cosO = a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
@@ -434,10 +451,9 @@ SC_HD sc_f4 sc_slerp(sc_f4 a, sc_f4 b, float t) {
         s1 = 1.0f - t;
         s2 = flip ? -t : t;
     } else {
-        float omega = sc_acosf(cosO);
-        float invSin = 1.0f / sc_sinf(omega);
-        s1 = sc_sinf((1.0f - t) * omega) * invSin;
-        s2 = flip ? -sc_sinf(t * omega) * invSin : sc_sinf(t * omega) * invSin;
+        sc_f2 sw = sc_slerp_weights(cosO, t, flip);
+        s1 = sw.x;
+        s2 = sw.y;
     }
     return sc_make_f4(s1 * a.x + s2 * b.x, s1 * a.y + s2 * b.y, s1 * a.z + s2 * b.z, s1 * a.w + s2 * b.w);
 }
