@@ -854,12 +854,26 @@ void scp_draws(uint64_t seed, uint32_t stream, uint32_t id0, int n, uint32_t ste
                         : sc_uniform(seed, stream, id0 + (uint32_t)i, step, d);
 }
 // 1 where the single-precision form of a double comparison disagrees with it.
-// kind 0: lipid range (dist, s); kind 1: diffusion threshold (x)
+// kind 0: lipid range (dist, s); kind 1: diffusion threshold (x);
+// kind 2: metabolic collision distance (rp, rt); kind 3: polar attraction (L);
+// kind 4: Brownian step length (x, radius); kind 5: rotation weight (rn, radius).
+// Values are compared as bit patterns.
+static bool same_bits(float x, float y) { return sc_f2u(x) == sc_f2u(y) || (x != x && y != y); }
 void scp_compare_forms(int kind, const float *a, const float *b, uint8_t *bad, int n) {
     for (int i = 0; i < n; i++) {
         if (kind == 0) {
             bool exact = (double)a[i] <= (double)b[i] + 0.8 * (double)b[i] * 0.5;
             bad[i] = sc_within_lipid_range(a[i], b[i]) != exact;
+        } else if (kind == 2) {
+            bad[i] = !same_bits(sc_coll_dist(a[i], b[i]), metab_collision_dist(a[i], b[i]));
+        } else if (kind == 4) {
+            bad[i] = !same_bits(sc_noise_mag(a[i], b[i]),
+                                (float)((double)a[i] / fmax((double)b[i] / 2.5, 1.0)));
+        } else if (kind == 5) {
+            bad[i] = !same_bits(sc_rot_noise(a[i], b[i]), (float)((double)a[i] / ((double)b[i] / 2.5)));
+        } else if (kind == 3) {
+            float L = a[i];
+            bad[i] = !same_bits(sc_polar_attr(L), (float)(fmin(fmax((double)L, 1e-6), (double)2.0f) / (double)2.0f));
         } else {
             bool exact = (double)fabsf(a[i]) > 0.001;
             bad[i] = sc_diffuse_exceeds(a[i]) != exact;

@@ -78,7 +78,13 @@ struct ScCounters {
     int polyCount;    // scheduled polymerisations collected this step
     int step;         // the step loop counter (main.cu:347)
     int tileCounter[4];
+    int ppClassCount[4];  // items per relax work class (k_build_pp)
 };
+
+// Relax work classes: items with bond partners in their list, items with
+// polar (lipid) pairs and no partners, and the rest.  k_relax runs the
+// classes one after another so a warp's items take the same branches.
+#define SC_RELAX_CLASSES 3
 
 struct ScParams {
     float simSize, maxInt, maxDiff, cell;

@@ -41,6 +41,7 @@ struct ScBuffers {
     // pair lists (sc_dev.cuh) and whether each matches the current state
     uint32_t *listPP, *listM, *listLM, *listD;
     int *cntPP, *cntM, *cntLM, *cntD;
+    int *classPP;  // SC_RELAX_CLASSES segments of N item indices
     bool validPP, validM, validLM, validD;
     void invalidateLists() { validPP = validM = validLM = validD = false; }
     // polymerisation list

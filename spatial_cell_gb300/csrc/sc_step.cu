@@ -40,11 +40,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_move_brownian(const int *__restr
     sc_f4 r1 = sc_random_rotation(sc_uniform(seed, su, id, st, 0), sc_uniform(seed, su, id, st, 1),
                                   sc_uniform(seed, su, id, st, 2));
     float nrm = sc_normal(seed, sn, id, st, 0);
-    float mag = (float)((double)(fabsf(nrm) * scale) / fmax((double)radius / 2.5, 1.0));
+    float mag = sc_noise_mag(fabsf(nrm) * scale, radius);
     st3(posnoise, i, sc_rotate(sc_up(), r1) * mag, 0.0f);
     sc_f4 r2 = sc_random_rotation(sc_uniform(seed, su, id, st, 3), sc_uniform(seed, su, id, st, 4),
                                   sc_uniform(seed, su, id, st, 5));
-    float t = (float)((double)P.rotNoise / ((double)radius / 2.5));
+    float t = sc_rot_noise(P.rotNoise, radius);
     st4(angnoise, i, sc_slerp(ld4(angnoise, i), r2, t));
 }
 
@@ -149,25 +149,40 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
                                                          const int *__restrict__ nActivePtr,
                                                          const float4 *__restrict__ pos, const int4 *__restrict__ info,
                                                          const int *__restrict__ nb, const int *__restrict__ bonds,
-                                                         uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
+                                                         uint32_t *__restrict__ list, int *__restrict__ cnt, int cap,
+                                                         int *__restrict__ classIdx, int *__restrict__ classCount) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = info[i];
-    if (!(in.z & SC_ACTIVE)) { cnt[i] = 0; return; }
-    BondRegs B;
-    B.load(nb, bonds, i);
-    float4 p4 = pos[i];
-    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
-    const int phydro = (int)(int8_t)(in.w & 0xff);
-    int c = 0;
-    scan27(P, cellStart, ppos, [&](int j) {
-        uint32_t f = pp_flags(P, i, j, ppos, p4.w, phydro, B, pos, info);
-        if (f) {
-            if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
-            c++;
-        }
-    });
-    cnt[i] = c;
+    int cls = 2;
+    if (!(in.z & SC_ACTIVE)) {
+        cnt[i] = 0;
+    } else {
+        BondRegs B;
+        B.load(nb, bonds, i);
+        float4 p4 = pos[i];
+        const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+        const int phydro = (int)(int8_t)(in.w & 0xff);
+        int c = 0;
+        uint32_t any = 0;
+        scan27(P, cellStart, ppos, [&](int j) {
+            uint32_t f = pp_flags(P, i, j, ppos, p4.w, phydro, B, pos, info);
+            if (f) {
+                if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
+                c++;
+                any |= f;
+            }
+        });
+        cnt[i] = c;
+        if (c <= min(SC_LIST_PP, P.listLimit)) cls = (any & SC_PP_PARTNER) ? 0 : (any & SC_PP_POLAR) ? 1 : 2;
+    }
+    // append i to its class (warp-aggregated; order within a class is free)
+    unsigned same = __match_any_sync(__activemask(), cls);
+    int leader = __ffs(same) - 1, lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&classCount[cls], __popc(same));
+    base = __shfl_sync(same, base, leader);
+    classIdx[(size_t)cls * cap + base + __popc(same & ((1u << lane) - 1u))] = i;
 }
 
 // Visits the contributing pairs of particle i in the reference's order: from
@@ -254,6 +269,8 @@ struct RelaxArgs {
     PairList<SC_LIST_PP> L;
     const float4 *__restrict__ velIn, *__restrict__ rotIn, *__restrict__ avIn;
     float4 *__restrict__ velOut, *__restrict__ rotOut, *__restrict__ avOut, *__restrict__ dbg;
+    const int *__restrict__ classIdx;    // items by work class (k_build_pp)
+    const int *__restrict__ classCount;
 };
 
 // One particle's relaxation.  SCAN = false reads the particle's pair list;
@@ -294,7 +311,7 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
             sc_f3 pPV = -nextUp * prad + ppos + pvel;
             sc_f3 tpPV = -nextTup * trad + tpos + tvel;
             float Lr = length(tpPV - pPV) / (prad + trad);
-            float attr = (float)(fmin(fmax((double)Lr, 1e-6), (double)2.0f) / (double)2.0f);
+            float attr = sc_polar_attr(Lr);
             w += 1.0f;
             dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
             float pap = sc_powf(fminf(1.0f / fmaxf(Lr, 1e-6f), 10.0f) / 10.0f, 0.2f);
@@ -413,8 +430,12 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
 
 // Items whose list fits; the others are left to k_relax_overflow.
 __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *A.nActivePtr) return;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n0 = A.classCount[0], n1 = A.classCount[1], n2 = A.classCount[2];
+    if (t >= n0 + n1 + n2) return;
+    const int i = t < n0 ? A.classIdx[t]
+                         : t < n0 + n1 ? A.classIdx[(size_t)A.L.cap + (t - n0)]
+                                       : A.classIdx[2 * (size_t)A.L.cap + (t - n0 - n1)];
     int4 in = A.info[i];
     float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
     if (!(in.z & SC_ACTIVE)) {
@@ -447,7 +468,7 @@ struct CollisionDistCache {
         if (!valid || !(r == rt)) {
             rt = r;
             valid = true;
-            cd = (float)((double)(rp + r) + 0.8 * (double)rp);
+            cd = sc_coll_dist(rp, r);
         }
         return cd;
     }
@@ -496,82 +517,111 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
     cnt[i] = c;
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_relax_metab(
-    ScParams P, const uint32_t *__restrict__ cellStartM, const uint32_t *__restrict__ cellStartP,
-    const int *__restrict__ nActivePtr, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-    PairList<SC_LIST_M> L, const float4 *__restrict__ mvelIn, float4 *__restrict__ mvelOut,
-    const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, const float4 *__restrict__ pvel_) {
+struct RelaxMArgs {
+    const uint32_t *__restrict__ cellStartM, *__restrict__ cellStartP;
+    const int *__restrict__ nActivePtr;
+    const float4 *__restrict__ mpos;
+    const int4 *__restrict__ minfo;
+    PairList<SC_LIST_M> L;
+    const float4 *__restrict__ mvelIn;
+    float4 *__restrict__ mvelOut;
+    const float4 *__restrict__ ppos;
+    const int4 *__restrict__ pinfo;
+    const float4 *__restrict__ pvel;
+};
+
+// The contribution of one colliding neighbour (a metabolic item, or a lipid
+// with twice the weight) to dV and w, metabolites.cuh:196-203 / 235-242.
+__device__ __forceinline__ void metab_pair(const ScParams &P, sc_f3 pp, sc_f3 ppv, float prad, float4 t4, float4 tv,
+                                           bool fromP, CollisionDistCache &cc, sc_f3 &dV, float &w) {
+    sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+    sc_f3 nd = normalize(tpos - pp);
+    float cd = cc.get(prad, t4.w);
+    float k = fromP ? 2.0f : 1.0f;
+    w += k;
+    dV += (tpos - nd * cd + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * k;
+}
+
+// Items whose list fits.  The next entry's neighbour data is loaded while the
+// current one is evaluated (the loop is bound by the latency of those loads).
+__global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, RelaxMArgs A) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    float4 v4 = mvelIn[i];
-    if (!(minfo[i].z & SC_ACTIVE)) {
-        mvelOut[i] = v4;
+    if (i >= *A.nActivePtr) return;
+    float4 v4 = A.mvelIn[i];
+    if (!(A.minfo[i].z & SC_ACTIVE)) {
+        A.mvelOut[i] = v4;
         return;
     }
-    float4 p4 = mpos[i];
+    const int c = A.L.cnt[i];
+    if (c > min(SC_LIST_M, P.listLimit)) return;
+    float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const float prad = p4.w;
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+    const sc_f3 ppv = pp + pv;
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    CollisionDistCache cm, cp;
-    const int c = L.cnt[i];
-    if (c <= min(SC_LIST_M, P.listLimit)) {
-        for (int k = 0; k < c; k++) {
-            uint32_t e = L.list[sc_list_at(SC_LIST_M, i, k)];
-            int j = (int)(e & SC_M_INDEX);
-            if (!(e & SC_M_FROM_P)) {
-                float4 t4 = mpos[j];
-                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
-                sc_f3 nd = normalize(tpos - pp);
-                float cd = cm.get(prad, t4.w);
-                w += 1.0f;
-                dV += (tpos - nd * cd + ld3(mvelIn, j) - (pp + pv)) * 0.9f * 1.0f;
-            } else {
-                float4 t4 = ppos_[j];
-                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
-                sc_f3 nd = normalize(tpos - pp);
-                float cd = cp.get(prad, t4.w);
-                w += 2.0f;
-                dV += (tpos - nd * cd + ld3(pvel_, j) - (pp + pv)) * 0.9f * 2.0f;
+    CollisionDistCache cc;
+    if (c > 0) {
+        uint32_t e = A.L.list[sc_list_at(SC_LIST_M, i, 0)];
+        bool fromP = (e & SC_M_FROM_P) != 0;
+        int j = (int)(e & SC_M_INDEX);
+        float4 t4 = fromP ? A.ppos[j] : A.mpos[j];
+        float4 tv = fromP ? A.pvel[j] : A.mvelIn[j];
+        for (int k = 1; k <= c; k++) {
+            uint32_t en = 0;
+            float4 t4n = t4, tvn = tv;
+            if (k < c) {
+                en = A.L.list[sc_list_at(SC_LIST_M, i, k)];
+                int jn = (int)(en & SC_M_INDEX);
+                bool fn = (en & SC_M_FROM_P) != 0;
+                t4n = fn ? A.ppos[jn] : A.mpos[jn];
+                tvn = fn ? A.pvel[jn] : A.mvelIn[jn];
             }
+            metab_pair(P, pp, ppv, prad, t4, tv, fromP, cc, dV, w);
+            fromP = (en & SC_M_FROM_P) != 0;
+            t4 = t4n;
+            tv = tvn;
         }
-    } else {
-        const float lim = P.maxInt;
-        cells27(P, pp, [&](uint32_t key) {
-            for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
-                if ((int)j == i) continue;
-                if (!(minfo[j].z & SC_ACTIVE)) continue;
-                float4 t4 = mpos[j];
-                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
-                sc_f3 delta = tpos - pp;
-                if (outside_cube(delta, lim)) continue;
-                sc_f3 nd = normalize(delta);
-                float dist = sc_norm3(delta);
-                float cd = cm.get(prad, t4.w);
-                if (dist <= cd) {
-                    w += 1.0f;
-                    dV += (tpos - nd * cd + ld3(mvelIn, j) - (pp + pv)) * 0.9f * 1.0f;
-                }
-            }
-            for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
-                int4 tin = pinfo[j];
-                if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
-                float4 t4 = ppos_[j];
-                sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
-                sc_f3 delta = tpos - pp;
-                if (outside_cube(delta, lim)) continue;
-                sc_f3 nd = normalize(delta);
-                float dist = sc_norm3(delta);
-                float cd = cp.get(prad, t4.w);
-                if (dist <= cd) {
-                    w += 2.0f;
-                    dV += (tpos - nd * cd + ld3(pvel_, j) - (pp + pv)) * 0.9f * 2.0f;
-                }
-            }
-        });
     }
-    st3(mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+    st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+}
+
+// Active items whose list overflowed: the reference's loops over the 27 cells.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *A.nActivePtr) return;
+    if (A.L.cnt[i] <= min(SC_LIST_M, P.listLimit)) return;
+    if (!(A.minfo[i].z & SC_ACTIVE)) return;
+    float4 v4 = A.mvelIn[i];
+    float4 p4 = A.mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const float prad = p4.w;
+    const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+    const sc_f3 ppv = pp + pv;
+    sc_f3 dV = sc_zero3();
+    float w = 0.0f;
+    CollisionDistCache cc;
+    const float lim = P.maxInt;
+    cells27(P, pp, [&](uint32_t key) {
+        for (uint32_t j = A.cellStartM[key], e = A.cellStartM[key + 1]; j < e; j++) {
+            if ((int)j == i) continue;
+            if (!(A.minfo[j].z & SC_ACTIVE)) continue;
+            float4 t4 = A.mpos[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (sc_norm3(delta) <= cc.get(prad, t4.w)) metab_pair(P, pp, ppv, prad, t4, A.mvelIn[j], false, cc, dV, w);
+        }
+        for (uint32_t j = A.cellStartP[key], e = A.cellStartP[key + 1]; j < e; j++) {
+            int4 tin = A.pinfo[j];
+            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+            float4 t4 = A.ppos[j];
+            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (sc_norm3(delta) <= cc.get(prad, t4.w)) metab_pair(P, pp, ppv, prad, t4, A.pvel[j], true, cc, dV, w);
+        }
+    });
+    st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
 // ---- metabolites.cuh:266-350 relaxMetabolicParticlePartners ----------------
@@ -1181,8 +1231,10 @@ static void ensure_pp(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (B.validPP) return;
     PFields F = B.P();
+    cudaMemsetAsync(B.ctr->ppClassCount, 0, sizeof(B.ctr->ppClassCount), c.st);
     k_build_pp<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
-                                                         F.bonds, B.listPP, B.cntPP, c.P.N);
+                                                         F.bonds, B.listPP, B.cntPP, c.P.N, B.classPP,
+                                                         B.ctr->ppClassCount);
     (*c.launches)++;
     B.validPP = true;
 }
@@ -1230,7 +1282,7 @@ void sc_phase_relax(ScLaunchCtx &c) {
     ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
     RelaxArgs A{B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds, pp_list(c),
-                F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg};
+                F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg, B.classPP, B.ctr->ppClassCount};
     k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
     k_relax_overflow<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
     (*c.launches)++;
@@ -1255,10 +1307,11 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     L.list = B.listM;
     L.cnt = B.cntM;
     L.cap = c.P.Nm;
-    k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
-                                                             M.info, L, M.vel, X.vel, F.pos, F.info, F.vel);
+    RelaxMArgs A{B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, L, M.vel, X.vel, F.pos, F.info, F.vel};
+    k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax_metab_overflow<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
     B.cm[FM_VEL] ^= 1;
-    (*c.launches)++;
+    (*c.launches) += 2;
 }
 
 void sc_phase_relax_partners(ScLaunchCtx &c) {

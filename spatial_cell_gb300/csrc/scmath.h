@@ -498,6 +498,96 @@ SC_HD bool sc_within_lipid_range(float dist, float s) {
 }
 
 // ---------------------------------------------------------------------------
+// Single-precision evaluation of the reference's mixed float/double
+// expressions.  GB300 runs double precision at a small fraction of its float
+// rate, so these are computed as float-float values and rounded once; where
+// the rounding could depend on the last bits, the double expression itself
+// is evaluated.  The results are identical to the double expressions for
+// every input (the tests compare them on random and adversarial inputs).
+// ---------------------------------------------------------------------------
+SC_HD float sc_fmaf(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+
+// Rounds hi + lo (|lo| well below ulp(hi)) to float.  Returns false when a
+// value within 2^-40 * |hi + lo| of it could round differently: the float-float
+// value carries an error below 2^-46 relative, the double expression below
+// 2^-51, so outside that band both round to the same float.
+SC_HD bool sc_round_ff(float hi, float lo, float *out) {
+    float f = hi + lo;
+    float e = (hi - f) + lo;            // hi - f is exact (Sterbenz)
+    uint32_t fb = sc_f2u(f) & 0x7fffffffu;
+    if (fb < 0x18000000u || fb >= 0x7f000000u) return false;   // tiny, huge, inf, nan
+    uint32_t ex = fb & 0x7f800000u;
+    float half = sc_u2f(ex - (24u << 23));                     // ulp(f) / 2
+    if ((fb & 0x007fffffu) == 0 && e != 0.0f && ((e < 0.0f) == (f > 0.0f)))
+        half *= 0.5f;                                           // the gap below a power of two
+    float margin = sc_u2f(ex - (40u << 23));
+    *out = f;
+    return fabsf(e) < half - margin;
+}
+
+// (float)((double)(rp + rt) + 0.8 * (double)rp), the metabolic collision
+// distance (metabolites.cuh:198,237,324).  0.8 (double) = SC_08_HI + SC_08_LO
+// to 2^-50; SC_08_HI * rp is split exactly with an fma.
+#define SC_08_HI 0.800000011920929f
+#define SC_08_LO (-1.1920929132713809e-08f)
+SC_HD float sc_coll_dist(float rp, float rt) {
+    float a = rp + rt;
+    if (rp > 0.0f && a > 0.0f) {
+        float ph = SC_08_HI * rp;
+        float pl = sc_fmaf(SC_08_HI, rp, -ph);
+        float cl = SC_08_LO * rp;
+        float sh = a + ph;
+        float bb = sh - a;
+        float se = (a - (sh - bb)) + (ph - bb);
+        float lo = (se + pl) + cl;
+        float f;
+        if (sc_round_ff(sh, lo, &f)) return f;
+    }
+    return (float)((double)(rp + rt) + 0.8 * (double)rp);
+}
+
+// (float)((double)x / fmax((double)radius / 2.5, 1.0)), the Brownian step
+// length (dynamics.cuh:170): radius <= 2.5 (or NaN) divides by exactly 1.
+SC_HD float sc_noise_mag(float x, float radius) {
+    if (!(radius > 2.5f)) return x;
+    return (float)((double)x / fmax((double)radius / 2.5, 1.0));
+}
+
+// (float)((double)rn / ((double)radius / 2.5)), the Brownian rotation weight
+// (dynamics.cuh:180): rn * 2.5 / radius as a float-float quotient.
+SC_HD float sc_rot_noise(float rn, float radius) {
+    uint32_t rb = sc_f2u(radius), nb = sc_f2u(rn) & 0x7fffffffu;
+    if (rb >= 0x00800000u && rb < 0x7f000000u && nb >= 0x00800000u && nb < 0x7e000000u) {
+        float h = rn * 2.5f;
+        float l = sc_fmaf(rn, 2.5f, -h);        // rn * 2.5 = h + l exactly
+        float q0 = h / radius;
+        float rem = sc_fmaf(-q0, radius, h);    // h - q0 * radius, exact
+        float q1 = (rem + l) / radius;
+        float f;
+        if (sc_round_ff(q0, q1, &f)) return f;
+    }
+    return (float)((double)rn / ((double)radius / 2.5));
+}
+
+// (float)(fmin(fmax((double)L, 1e-6), (double)2.0f) / (double)2.0f), the
+// polar attraction factor (dynamics.cuh:496).  SC_ABOVE_1EM6 is the smallest
+// float above 1e-6 (double); SC_HALF_1EM6 = (float)5e-7.  NaN gives 5e-7
+// (fmax returns the number).
+#define SC_ABOVE_1EM6 1.0000001111620804e-06f
+#define SC_HALF_1EM6 4.999999987376214e-07f
+SC_HD float sc_polar_attr(float L) {
+    if (L >= 2.0f) return 1.0f;
+    if (L >= SC_ABOVE_1EM6) return L * 0.5f;
+    return SC_HALF_1EM6;
+}
+
+// ---------------------------------------------------------------------------
 // Periodic box (an extension; the reference clamps positions to its walls).
 // A neighbour's position is replaced by its nearest periodic image relative
 // to the item, so every pair expression keeps its reference form.

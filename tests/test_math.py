@@ -128,3 +128,56 @@ def test_single_precision_forms_are_exact(lib):
     bad = np.zeros(len(x), np.uint8)
     lib.scp_compare_forms(1, x.ctypes.data, x.ctypes.data, bad.ctypes.data, len(x))
     assert not bad.any()
+
+
+def _forms_bad(lib, kind, a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    bad = np.zeros(len(a), np.uint8)
+    lib.scp_compare_forms(kind, a.ctypes.data, b.ctypes.data, bad.ctypes.data, len(a))
+    return bad
+
+
+def test_collision_distance_single_precision_form(lib):
+    """(float)((double)(rp + rt) + 0.8 * (double)rp) evaluated as a rounded
+    float-float value equals the double expression bit for bit."""
+    rng = np.random.default_rng(11)
+    nice = np.arange(1, 1025, dtype=np.float32) / np.float32(64)     # radii on a fine grid, all pairs
+    ga, gb = np.meshgrid(nice, nice)
+    cases = [
+        (ga.ravel(), gb.ravel()),
+        (rng.uniform(0, 10, 1_000_000), rng.uniform(0, 10, 1_000_000)),
+        (np.exp(rng.uniform(-80, 80, 300_000)), np.exp(rng.uniform(-80, 80, 300_000))),
+        (rng.uniform(-5, 5, 200_000), rng.uniform(-5, 5, 200_000)),
+        (np.array([0, -0.0, 1, np.inf, -np.inf, np.nan, 1e-45, 3e38, 1.0], np.float32),
+         np.array([0, 0, -1, 1, 1, 1, 1e-45, 3e38, np.nan], np.float32)),
+    ]
+    for a, b in cases:
+        a32 = a.astype(np.float32)
+        # neighbours of each value too: nudges that move the sum across float midpoints
+        for da in (0, 1, -1):
+            aa = a32.view(np.uint32).astype(np.int64) + da
+            aa = np.clip(aa, 0, 0xFFFFFFFF).astype(np.uint32).view(np.float32)
+            assert not _forms_bad(lib, 2, aa, b).any()
+
+
+def test_polar_attraction_single_precision_form(lib):
+    rng = np.random.default_rng(12)
+    edge = np.array([1e-6, 2.0, 0.0, -0.0, -1.0, np.inf, -np.inf, np.nan, 1e-45, 3e38], np.float32)
+    around = np.concatenate([np.nextafter(edge, np.float32(np.inf)), np.nextafter(edge, np.float32(-np.inf)), edge])
+    x = np.concatenate([around, rng.uniform(0, 3, 500_000), np.exp(rng.uniform(-20, 2, 300_000)),
+                        rng.uniform(-1, 1, 10_000)]).astype(np.float32)
+    assert not _forms_bad(lib, 3, x, x).any()
+
+
+def test_brownian_scalings_single_precision_forms(lib):
+    rng = np.random.default_rng(13)
+    radii = np.concatenate([np.arange(1, 1025, dtype=np.float32) / np.float32(64), rng.uniform(0, 20, 400_000),
+                            np.exp(rng.uniform(-60, 60, 200_000)),
+                            np.array([2.5, 0, -1, np.inf, -np.inf, np.nan, 1e-45, 3e38], np.float32)]).astype(np.float32)
+    radii = np.concatenate([radii, np.nextafter(radii, np.float32(np.inf)), np.nextafter(radii, np.float32(-np.inf))])
+    for scale in (rng.uniform(0, 3, len(radii)), np.exp(rng.uniform(-60, 60, len(radii))),
+                  np.full(len(radii), 0.05), np.full(len(radii), 0.7)):
+        x = scale.astype(np.float32)
+        assert not _forms_bad(lib, 4, x, radii).any()
+        assert not _forms_bad(lib, 5, x, radii).any()
