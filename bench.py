@@ -143,6 +143,9 @@ def per_phase_times(sim, stream, torch, reps=3):
     before the timed launches: inside a step one build serves every
     sub-iteration of a phase, and the builds are timed with the step."""
     out = {}
+    # as inside a step: both sets sorted, positions in the cells they were sorted into
+    sim.run_phase(abi.PHASE_SORT_PARTICLES, 0)
+    sim.run_phase(abi.PHASE_SORT_METABOLIC, 0)
     for name, ph in PHASES.items():
         if name in ("complexify", "transition", "apply_velocities"):
             continue  # change the state; timed as part of the step only

@@ -105,17 +105,38 @@ struct ScParams {
     int listLimit;            // effective pair-list capacity (<= each list's size; smaller only in tests)
     int periodic;             // periodic box extension (sc_config.periodic)
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
+    int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
 };
+#define SC_BINNED_P 1
+#define SC_BINNED_M 2
 
 // Cells per axis the cell index clamps to: the power-of-two grid of
 // config.cuh:65-74, or in a periodic box the cells the box spans.
 __host__ __device__ __forceinline__ int cell_limit(const ScParams &P) { return P.periodic ? P.nUsed : P.ngrid; }
 
-// A neighbour's position as seen from p: itself, or in a periodic box its
-// nearest image.
-__device__ __forceinline__ sc_f3 img(const ScParams &P, sc_f3 t, sc_f3 p) {
-    return P.periodic ? sc_image3(t, p, P.simSize) : t;
-}
+// A neighbour's position as seen from an item at p: itself, or in a periodic
+// box its nearest image.  When the neighbours' sets (need, SC_BINNED_*) still
+// sit in the cells they were sorted into, neighbours from the 27 cells around
+// p are less than 2.5 cells away per axis; if p's cell is not on a face of a
+// periodic box at least 5 cells wide, that is less than half the box and
+// every neighbour is its own nearest image, so the test is made once per item.
+struct Imager {
+    bool wrap;
+    float L;
+    sc_f3 p;
+    __device__ __forceinline__ Imager(const ScParams &P, sc_f3 pos, int need) : wrap(false), L(P.simSize), p(pos) {
+        if (P.periodic && (P.binned & need) != need) {
+            wrap = true;
+        } else if (P.periodic) {
+            int n = P.nUsed;
+            int cx = (int)sc_grid_idx(pos.x, P.cell, n), cy = (int)sc_grid_idx(pos.y, P.cell, n),
+                cz = (int)sc_grid_idx(pos.z, P.cell, n);
+            wrap = !(P.simSize >= 5.0f * P.cell) || cx == 0 || cy == 0 || cz == 0 || cx == n - 1 || cy == n - 1 ||
+                   cz == n - 1;
+        }
+    }
+    __device__ __forceinline__ sc_f3 operator()(sc_f3 t) const { return wrap ? sc_image3(t, p, L) : t; }
+};
 
 __device__ __forceinline__ sc_f4 ld4(const float4 *p, int i) {
     float4 v = p[i];

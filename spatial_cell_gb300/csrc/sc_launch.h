@@ -111,6 +111,7 @@ struct ScLaunchCtx {
     ScParams P;
     ScBuffers *B;
     long long *launches;
+    int gridCap;  // blocks of SC_THREADS resident on the whole device (grid-stride kernels)
 };
 void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic);
 void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac);

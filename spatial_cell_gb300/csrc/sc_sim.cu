@@ -149,6 +149,7 @@ struct sc_sim {
     ScBuffers B;
     cudaStream_t st = nullptr;
     int device = 0;
+    int gridCap = 0;
     long long launches = 0;
     std::string err;
     std::vector<void *> allocs;
@@ -200,6 +201,7 @@ ScLaunchCtx ctx(sc_sim *s) {
     c.P = s->P;
     c.B = &s->B;
     c.launches = &s->launches;
+    c.gridCap = s->gridCap;
     return c;
 }
 
@@ -248,9 +250,19 @@ void invalidate_after(ScBuffers &B, int phase) {
     }
 }
 
+// Which sets still sit in the cells they were sorted into: a sort bins its
+// set, moving positions unbins both (particles a polymerisation creates are in
+// no cell, so they are never found as neighbours).
+void binned_after(ScParams &P, int phase) {
+    if (phase == SC_PHASE_SORT_PARTICLES) P.binned |= SC_BINNED_P;
+    if (phase == SC_PHASE_SORT_METABOLIC) P.binned |= SC_BINNED_M;
+    if (phase == SC_PHASE_APPLY_VELOCITIES) P.binned = 0;
+}
+
 int run_phase(sc_sim *s, int phase, int arg) {
     ScLaunchCtx c = ctx(s);
     invalidate_after(s->B, phase);
+    binned_after(s->P, phase);
     switch (phase) {
         case SC_PHASE_SORT_PARTICLES: sort_particles(s); break;
         case SC_PHASE_SORT_METABOLIC: sort_metabolic(s); break;
@@ -326,6 +338,9 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     sc_sim *s = new sc_sim();
     s->cfg = *cfg;
     cudaGetDevice(&s->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    s->gridCap = std::max(1, sms) * (2048 / SC_THREADS);
     ScParams &P = s->P;
     memset(&P, 0, sizeof P);
     P.simSize = cfg->sim_size;
@@ -477,6 +492,7 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     if (rc) return rc;
     ScBuffers &B = s->B;
     B.invalidateLists();
+    s->P.binned = 0;
     for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
     if (N > 0) {

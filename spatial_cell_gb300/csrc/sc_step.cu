@@ -122,14 +122,15 @@ struct BondRegs {
 // The position-only tests of relax for candidate j of particle i
 // (dynamics.cuh:452-478, 584-589, 775-777): returns the entry flags, 0 if
 // the pair contributes nothing.
-__device__ __forceinline__ uint32_t pp_flags(const ScParams &P, int i, int j, sc_f3 ppos, float prad, int phydro,
+__device__ __forceinline__ uint32_t pp_flags(const ScParams &P, const Imager &IM, int i, int j, sc_f3 ppos, float prad,
+                                             int phydro,
                                              const BondRegs &B, const float4 *__restrict__ pos,
                                              const int4 *__restrict__ info) {
     if (j == i) return 0;
     int4 tin = info[j];
     if (!(tin.z & SC_ACTIVE)) return 0;
     float4 t4 = pos[j];
-    sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
+    sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
     if (outside_cube(delta, P.maxInt)) return 0;
     float dist = sc_norm3(delta);
     float s = prad + t4.w;
@@ -162,11 +163,12 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
         B.load(nb, bonds, i);
         float4 p4 = pos[i];
         const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, ppos, SC_BINNED_P);
         const int phydro = (int)(int8_t)(in.w & 0xff);
         int c = 0;
         uint32_t any = 0;
         scan27(P, cellStart, ppos, [&](int j) {
-            uint32_t f = pp_flags(P, i, j, ppos, p4.w, phydro, B, pos, info);
+            uint32_t f = pp_flags(P, IM, i, j, ppos, p4.w, phydro, B, pos, info);
             if (f) {
                 if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
                 c++;
@@ -174,7 +176,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
             }
         });
         cnt[i] = c;
-        if (c <= min(SC_LIST_PP, P.listLimit)) cls = (any & SC_PP_PARTNER) ? 0 : (any & SC_PP_POLAR) ? 1 : 2;
+        if (B.n >= 1) cls = 0;
+        else if (c <= min(SC_LIST_PP, P.listLimit) && (any & SC_PP_POLAR)) cls = 1;
     }
     // append i to its class (warp-aggregated; order within a class is free)
     unsigned same = __match_any_sync(__activemask(), cls);
@@ -190,8 +193,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
 template <class F>
 __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__restrict__ cellStart,
                                        const PairList<SC_LIST_PP> &L, int i, sc_f3 ppos, float prad, int phydro,
-                                       const BondRegs &B, const float4 *__restrict__ pos,
-                                       const int4 *__restrict__ info, F &&f) {
+                                       const int *__restrict__ nb, const int *__restrict__ bonds,
+                                       const float4 *__restrict__ pos, const int4 *__restrict__ info, F &&f) {
     int c = L.cnt[i];
     if (c <= min(SC_LIST_PP, P.listLimit)) {
         for (int k = 0; k < c; k++) {
@@ -199,8 +202,11 @@ __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__rest
             f((int)(e & SC_PP_INDEX), e);
         }
     } else {
+        const Imager IM(P, ppos, SC_BINNED_P);
+        BondRegs B;
+        B.load(nb, bonds, i);
         scan27(P, cellStart, ppos, [&](int j) {
-            uint32_t fl = pp_flags(P, i, j, ppos, prad, phydro, B, pos, info);
+            uint32_t fl = pp_flags(P, IM, i, j, ppos, prad, phydro, B, pos, info);
             if (fl) f(j, fl);
         });
     }
@@ -209,13 +215,12 @@ __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__rest
 // ---- dynamics.cuh:288-402 coordinateNoise -----------------------------------
 // Only interaction partners change anything; they are the PARTNER entries of
 // the particle-particle list, in the reference's visiting order.
-__global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
-    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
-    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ nb,
-    const int *__restrict__ bonds, PairList<SC_LIST_PP> L, const float4 *__restrict__ pnIn,
-    const float4 *__restrict__ anIn, float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
+// dynamics.cuh:288-402 for one particle.
+__device__ __forceinline__ void coordinate_noise_item(
+    const ScParams &P, const uint32_t *__restrict__ cellStart, int i, const float4 *__restrict__ pos,
+    const int4 *__restrict__ info, const int *__restrict__ nb, const int *__restrict__ bonds,
+    const PairList<SC_LIST_PP> &L, const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn,
+    float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
     int4 in = info[i];
     float4 pn4 = pnIn[i], an4 = anIn[i];
     if (!(in.z & SC_ACTIVE) || nb[i] < 1) {
@@ -223,8 +228,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
         anOut[i] = an4;
         return;
     }
-    BondRegs B;
-    B.load(nb, bonds, i);
+    const int nbi = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    const int *__restrict__ myBonds = bonds + (size_t)i * 24;
     float4 p4 = pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
     const float prad = p4.w;
@@ -233,15 +238,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
     sc_f3 dPN = sc_zero3();
     sc_f4 dAN = sc_qid();
     float w = 0.0f;
-    for_pp(P, cellStart, L, i, ppos, prad, (int)(int8_t)(in.w & 0xff), B, pos, info, [&](int j, uint32_t fl) {
+    for_pp(P, cellStart, L, i, ppos, prad, (int)(int8_t)(in.w & 0xff), nb, bonds, pos, info, [&](int j, uint32_t fl) {
         if (!(fl & SC_PP_PARTNER)) return;
         const int tid_ = info[j].x;
         const float trad = pos[j].w;
-#pragma unroll
-        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-            if (k >= B.n) break;
-            if (B.t[k] < 10 && frac > 0.25f) continue;
-            if (B.p[k] == tid_) {
+#pragma unroll 1
+        for (int k = 0; k < nbi; k++) {
+            if (myBonds[3 * k] < 10 && frac > 0.25f) continue;
+            if (myBonds[3 * k + 2] == tid_) {
                 sc_f3 tpn = ld3(pnIn, j);
                 sc_f4 tan_ = ld4(anIn, j);
                 float pMag = length(ppn);
@@ -256,6 +260,20 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
     pan = sc_qmul(sc_slerp(sc_qid(), dAN, 1.0f / fmaxf(w, 1.0f)), pan);
     st3(pnOut, i, ppn, pn4.w);
     st4(anOut, i, pan);
+}
+
+
+// Runs over the bonded work class (items with at least one bond); the
+// launcher copies every other item's noise to the output buffers first.
+__global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ classIdx,
+    const int *__restrict__ classCount, const float4 *__restrict__ pos, const int4 *__restrict__ info,
+    const int *__restrict__ nb, const int *__restrict__ bonds, PairList<SC_LIST_PP> L,
+    const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn, float4 *__restrict__ pnOut,
+    float4 *__restrict__ anOut, float frac) {
+    const int n0 = classCount[0];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n0; t += gridDim.x * blockDim.x)
+        coordinate_noise_item(P, cellStart, classIdx[t], pos, info, nb, bonds, L, pnIn, anIn, pnOut, anOut, frac);
 }
 
 // ---- dynamics.cuh:405-822 relax ------------------------------------------------
@@ -275,13 +293,16 @@ struct RelaxArgs {
 
 // One particle's relaxation.  SCAN = false reads the particle's pair list;
 // SCAN = true (list overflow) visits its 27 cells and applies the list's
-// tests to each candidate.  The bond loop reads the particle's bonds from
+// tests to each candidate.  MODE is the particle's work class: 0 all pair
+// kinds, 1 no bond partners, 2 collisions only (the class guarantees the
+// list holds no other kinds).  The bond loop reads the particle's bonds from
 // memory one at a time, so its body is emitted once.
-template <bool SCAN>
+template <bool SCAN, int MODE>
 __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4, float4 r4,
                                            float4 a4) {
     float4 p4 = A.pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, ppos, SC_BINNED_P);
     const float prad = p4.w;
     const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
     sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
@@ -301,10 +322,10 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
     const float flex = SC_PI_REF / 8;
     auto body = [&](int j, uint32_t fl) {
         float4 t4 = A.pos[j];
-        const sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos);
+        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
         const float trad = t4.w;
         const float idist = prad + trad;
-        if (fl & SC_PP_POLAR) {
+        if (MODE <= 1 && (fl & SC_PP_POLAR)) {
             // dynamics.cuh:478-582: polar (lipid) head / tail attraction
             sc_f3 tvel = ld3(A.velIn, j);
             sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(A.rotIn, j)), pav);
@@ -318,7 +339,7 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
             phobSum += pap;
             phobPos += tpPV * pap;
         }
-        if (fl & SC_PP_PARTNER) {
+        if (MODE == 0 && (fl & SC_PP_PARTNER)) {
             // dynamics.cuh:584-771: interaction partners, in bond-slot order
             int4 tin = A.info[j];
             const int tid_ = tin.x, ttype = tin.y;
@@ -406,7 +427,7 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
         BondRegs B;
         B.load(A.nb, A.bonds, i);
         scan27(P, A.cellStart, ppos, [&](int j) {
-            uint32_t fl = pp_flags(P, i, j, ppos, prad, phydro, B, A.pos, A.info);
+            uint32_t fl = pp_flags(P, IM, i, j, ppos, prad, phydro, B, A.pos, A.info);
             if (fl) body(j, fl);
         });
     } else {
@@ -428,24 +449,25 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
     if (dbgTouched) st4(A.dbg, i, pdbg);
 }
 
-// Items whose list fits; the others are left to k_relax_overflow.
+// The items of one work class whose list fits (the others are left to
+// k_relax_overflow), grid-stride over the class's index segment.
+template <int MODE>
 __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n0 = A.classCount[0], n1 = A.classCount[1], n2 = A.classCount[2];
-    if (t >= n0 + n1 + n2) return;
-    const int i = t < n0 ? A.classIdx[t]
-                         : t < n0 + n1 ? A.classIdx[(size_t)A.L.cap + (t - n0)]
-                                       : A.classIdx[2 * (size_t)A.L.cap + (t - n0 - n1)];
-    int4 in = A.info[i];
-    float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
-    if (!(in.z & SC_ACTIVE)) {
-        A.velOut[i] = v4;
-        A.rotOut[i] = r4;
-        A.avOut[i] = a4;
-        return;
+    const int n = A.classCount[MODE];
+    const int *__restrict__ idx = A.classIdx + (size_t)MODE * A.L.cap;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = idx[t];
+        int4 in = A.info[i];
+        float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
+        if (!(in.z & SC_ACTIVE)) {
+            A.velOut[i] = v4;
+            A.rotOut[i] = r4;
+            A.avOut[i] = a4;
+            continue;
+        }
+        if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) continue;
+        relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
     }
-    if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) return;
-    relax_item<false>(P, A, i, in, v4, r4, a4);
 }
 
 // Active items whose list overflowed: their neighbourhood is scanned.  A
@@ -456,7 +478,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, Relax
     if (A.L.cnt[i] <= min(SC_LIST_PP, P.listLimit)) return;
     int4 in = A.info[i];
     if (!(in.z & SC_ACTIVE)) return;
-    relax_item<true>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
+    relax_item<true, 0>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
 }
 
 // (float)((double)(rp + rt) + 0.8 * (double)rp) (metabolites.cuh:198,237,324),
@@ -488,6 +510,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
     if (!(minfo[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
     float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cm, cp;
     int c = 0;
@@ -495,7 +518,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
         for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i || !(minfo[j].z & SC_ACTIVE)) continue;
             float4 t4 = mpos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
             if (sc_norm3(delta) <= cm.get(prad, t4.w)) {
                 if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j;
@@ -506,7 +529,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
             int4 tin = pinfo[j];
             if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
             float4 t4 = ppos_[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
             if (sc_norm3(delta) <= cp.get(prad, t4.w)) {
                 if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j | SC_M_FROM_P;
@@ -532,11 +555,10 @@ struct RelaxMArgs {
 
 // The contribution of one colliding neighbour (a metabolic item, or a lipid
 // with twice the weight) to dV and w, metabolites.cuh:196-203 / 235-242.
-__device__ __forceinline__ void metab_pair(const ScParams &P, sc_f3 pp, sc_f3 ppv, float prad, float4 t4, float4 tv,
-                                           bool fromP, CollisionDistCache &cc, sc_f3 &dV, float &w) {
-    sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+__device__ __forceinline__ void metab_pair(const Imager &IM, sc_f3 pp, sc_f3 ppv, float4 t4, float4 tv, float cd,
+                                           bool fromP, sc_f3 &dV, float &w) {
+    sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
     sc_f3 nd = normalize(tpos - pp);
-    float cd = cc.get(prad, t4.w);
     float k = fromP ? 2.0f : 1.0f;
     w += k;
     dV += (tpos - nd * cd + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * k;
@@ -556,12 +578,13 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
     if (c > min(SC_LIST_M, P.listLimit)) return;
     float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w;
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
     const sc_f3 ppv = pp + pv;
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    CollisionDistCache cc;
+    CollisionDistCache cm, cp;   // neighbours of each kind share a radius
     if (c > 0) {
         uint32_t e = A.L.list[sc_list_at(SC_LIST_M, i, 0)];
         bool fromP = (e & SC_M_FROM_P) != 0;
@@ -578,7 +601,8 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
                 t4n = fn ? A.ppos[jn] : A.mpos[jn];
                 tvn = fn ? A.pvel[jn] : A.mvelIn[jn];
             }
-            metab_pair(P, pp, ppv, prad, t4, tv, fromP, cc, dV, w);
+            float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
+            metab_pair(IM, pp, ppv, t4, tv, cd, fromP, dV, w);
             fromP = (en & SC_M_FROM_P) != 0;
             t4 = t4n;
             tv = tvn;
@@ -596,29 +620,32 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
     float4 v4 = A.mvelIn[i];
     float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w;
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
     const sc_f3 ppv = pp + pv;
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    CollisionDistCache cc;
+    CollisionDistCache cm, cp;
     const float lim = P.maxInt;
     cells27(P, pp, [&](uint32_t key) {
         for (uint32_t j = A.cellStartM[key], e = A.cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i) continue;
             if (!(A.minfo[j].z & SC_ACTIVE)) continue;
             float4 t4 = A.mpos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cc.get(prad, t4.w)) metab_pair(P, pp, ppv, prad, t4, A.mvelIn[j], false, cc, dV, w);
+            if (sc_norm3(delta) <= cm.get(prad, t4.w))
+                metab_pair(IM, pp, ppv, t4, A.mvelIn[j], cm.get(prad, t4.w), false, dV, w);
         }
         for (uint32_t j = A.cellStartP[key], e = A.cellStartP[key + 1]; j < e; j++) {
             int4 tin = A.pinfo[j];
             if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
             float4 t4 = A.ppos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cc.get(prad, t4.w)) metab_pair(P, pp, ppv, prad, t4, A.pvel[j], true, cc, dV, w);
+            if (sc_norm3(delta) <= cp.get(prad, t4.w))
+                metab_pair(IM, pp, ppv, t4, A.pvel[j], cp.get(prad, t4.w), true, dV, w);
         }
     });
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
@@ -638,13 +665,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
     if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) { cnt[i] = 0; return; }
     float4 p4 = ppos_[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cc;
     int c = 0;
     scan27(P, cellStartM, pp, [&](int j) {
         if (!(minfo[j].z & SC_ACTIVE)) return;
         float4 t4 = mpos[j];
-        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+        sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
         if (sc_norm3(delta) <= cc.get(prad, t4.w)) {
             if (c < min(SC_LIST_LM, P.listLimit)) list[sc_list_at(SC_LIST_LM, i, c)] = (uint32_t)j;
@@ -665,6 +693,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) return;
     float4 p4 = ppos_[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M);
     const float prad = p4.w;
     float4 v4 = pvel_[i];
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
@@ -672,7 +701,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     float w = 0.0f;
     CollisionDistCache cc;
     auto body = [&](int j, float4 t4) {
-        sc_f3 tpos = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp);
+        sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
         sc_f3 nd = normalize(tpos - pp);
         float cd = cc.get(prad, t4.w);
         w += 2.0f;
@@ -689,7 +718,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
         scan27(P, cellStartM, pp, [&](int j) {
             if (!(minfo[j].z & SC_ACTIVE)) return;
             float4 t4 = mpos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
             if (sc_norm3(delta) <= cc.get(prad, t4.w)) body(j, t4);
         });
@@ -738,6 +767,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     }
     float4 p4 = pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, ppos, SC_BINNED_P);
     const sc_f4 prot = ld4(rot, i);
     const int pid = in.x, ptype = in.y, pstate = state[i];
     const sc_f3 up = sc_rotate(sc_up(), prot);
@@ -749,7 +779,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
         int4 tin = info[j];
         if (!(tin.z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
-        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
+        sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
         if (outside_cube(delta, lim)) return;
         sc_f4 trot = ld4(rot, j);
         sc_f3 tup = sc_rotate(sc_up(), trot);
@@ -799,6 +829,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
     if ((in.z & SC_ACTIVE) && pnb >= 1) {
         float4 p4 = pos[i];
         const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, ppos, SC_BINNED_P);
         const sc_f4 prot = ld4(rot, i);
         const int pid = in.x, ptype = in.y;
         const sc_f3 up = sc_rotate(sc_up(), prot);
@@ -810,7 +841,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
             int4 tin = info[j];
             if (!(tin.z & SC_ACTIVE)) return;
             float4 t4 = pos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), ppos) - ppos;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
             if (outside_cube(delta, lim)) return;
             bool loaded = false;
             sc_f4 trot;
@@ -1060,12 +1091,13 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
     if (!(info[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
     float4 p4 = pos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
     int c = 0;
     scan27(P, cellStart, pp, [&](int j) {
         if (j == i || !(info[j].z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
-        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+        sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
         if (sc_norm3(delta) <= lim) {
             if (c < min(SC_LIST_D, P.listLimit)) list[sc_list_at(SC_LIST_D, i, c)] = (uint32_t)j;
@@ -1120,12 +1152,13 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
     } else {
         float4 p4 = pos[i];
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_M);
         const float lim = P.maxDiff;
         scan27(P, cellStart, pp, [&](int j) {
             if (j == i) return;
             if (!(info[j].z & SC_ACTIVE)) return;
             float4 t4 = pos[j];
-            sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
             if (sc_norm3(delta) <= lim) body(j);
         });
@@ -1151,6 +1184,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
     if (!(in.z & SC_ACTIVE)) return;
     float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_P);
     const float prad = p4.w;
     int flags = in.z;
     const float lim = P.maxInt;
@@ -1158,7 +1192,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
         int4 tin = pinfo[j];
         if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) return;
         float4 t4 = ppos_[j];
-        sc_f3 delta = img(P, sc_make_f3(t4.x, t4.y, t4.z), pp) - pp;
+        sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
         float dist = sc_norm3(delta);
         float interf = (float)((double)(prad + t4.w) + 0.001);
@@ -1252,9 +1286,11 @@ void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac) {
     if (c.P.N <= 0) return;
     ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
-    k_coordinate_noise<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info,
-                                                                 F.nb, F.bonds, pp_list(c), F.posnoise, F.angnoise,
-                                                                 X.posnoise, X.angnoise, frac);
+    cudaMemcpyAsync(X.posnoise, F.posnoise, (size_t)c.P.N * sizeof(float4), cudaMemcpyDeviceToDevice, c.st);
+    cudaMemcpyAsync(X.angnoise, F.angnoise, (size_t)c.P.N * sizeof(float4), cudaMemcpyDeviceToDevice, c.st);
+    k_coordinate_noise<<<std::min(nblocks(c.P.N), c.gridCap), SC_THREADS, 0, c.st>>>(
+        c.P, B.cellStartP, B.classPP, B.ctr->ppClassCount, F.pos, F.info, F.nb, F.bonds, pp_list(c), F.posnoise,
+        F.angnoise, X.posnoise, X.angnoise, frac);
     B.cp[FP_POSNOISE] ^= 1;
     B.cp[FP_ANGNOISE] ^= 1;
     (*c.launches)++;
@@ -1283,9 +1319,13 @@ void sc_phase_relax(ScLaunchCtx &c) {
     PFields F = B.P(), X = B.Pnext();
     RelaxArgs A{B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds, pp_list(c),
                 F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg, B.classPP, B.ctr->ppClassCount};
-    k_relax<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
+    // heaviest class first; each grid covers the class at most once
+    const int g = std::min(nblocks(c.P.N), c.gridCap);
+    k_relax<0><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax<1><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax<2><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
     k_relax_overflow<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
-    (*c.launches)++;
+    (*c.launches) += 3;
     B.cp[FP_VEL] ^= 1;
     B.cp[FP_ROT] ^= 1;
     B.cp[FP_ANGVEL] ^= 1;
