@@ -54,6 +54,26 @@ def _dist():
     return world, rank, local
 
 
+def replica_seed(workload, rank):
+    """Each rank steps its own replica: the workload's seed offset by the rank."""
+    return scenes.WORKLOADS[workload]["seed"] + rank
+
+
+def aggregate_replicas(items_per_step, steps, seconds, device=None):
+    """Whole-job throughput of independent replicas: the items all ranks
+    stepped over the slowest rank's time.  Returns (rate, slowest seconds).
+    Without an initialised process group it is the local rate."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return items_per_step * steps / seconds, seconds
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    n = torch.tensor([float(items_per_step) * steps], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) / float(t.item()), float(t.item())
+
+
 def _measured_peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -124,6 +144,37 @@ def algorithmic_bytes(phase, N, Nm, S, bbar=0.0):
     }.get(phase)
 
 
+def step_algorithmic_bytes(cfg, bbar):
+    """Compulsory HBM bytes of one whole step: every item's fields read and
+    written once per phase that depends on them, neighbour data served on
+    chip, elementwise phases fused into the adjacent sweeps (per-item
+    figures: particles 6,292 B and metabolic items 2,258 B at the large
+    workload with no bonds)."""
+    import math
+    N, Nm, S = cfg.num_particles, cfg.num_metabolic_particles, cfg.num_metabolites
+    C, R, D = cfg.noise_coordination_steps, cfg.relaxation_steps, cfg.metabolite_diffusion_steps
+    _, bits, cells = abi.grid_dims(cfg)
+    d = math.ceil((3 * bits + 1) / 8)
+    P = 80 + 12 * bbar
+    M = 68 + 4 * S
+    per_p = (20 + 4 + 16 * d + 2 * P + 4 + 4 + 8 * cells / max(N, 1) + C * (84 + 12 * bbar) + 56
+             + R * (104 + 12 * bbar) + (R / 2) * 32 + (R / 2) * 44 + 100 + 24 * bbar)
+    per_m = (20 + 4 + 16 * d + 2 * M + 4 + 4 + 8 * cells / max(Nm, 1) + 120 + (R / 2) * 44 + (R / 2) * 32
+             + D * (16 + 8 * S))
+    return N * per_p + Nm * per_m
+
+
+def measured_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` at `workload` from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t[workload][kernel]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 PHASES = {
     "relax": abi.PHASE_RELAX,
     "relax_metab": abi.PHASE_RELAX_METAB,
@@ -172,8 +223,9 @@ def sub_box(workload, frac):
                 sim_size=float(cfg0.sim_size * frac ** (1.0 / 3.0)))
 
 
-def cpu_sample(args, reps=1):
-    """Times the CPU oracle on a same-density sub-box of the workload."""
+def cpu_sample(args, reps=1, warmup=0):
+    """Times the CPU oracle on a same-density sub-box of the workload:
+    `warmup` untimed steps, then `reps` timed steps."""
     from oracle import engine as oengine
     frac = args.cpu_fraction
     cfg = scenes.workload_config(args.workload, **sub_box(args.workload, frac))
@@ -186,13 +238,15 @@ def cpu_sample(args, reps=1):
     e.load_state(p, m)
     e.prepare()
     threads = oengine.max_threads()
+    if warmup:
+        e.step(warmup)
     t0 = time.perf_counter()
     e.step(reps)
     dt = time.perf_counter() - t0
     e.close()
     rate = (n + nm) * reps / dt
-    sample = (f"{reps} step(s) of a {frac:.4g}-volume sub-box at the workload's density "
-              f"({n} + {nm} items, {box:.1f} nm), {dt:.1f} s")
+    sample = (f"{reps} step(s) (after {warmup} untimed) of a {frac:.4g}-volume sub-box at the workload's "
+              f"density ({n} + {nm} items, {box:.1f} nm), {dt:.1f} s")
     return rate, threads, sample
 
 
@@ -200,7 +254,7 @@ def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
         return
-    rate, threads, sample = cpu_sample(args, reps=max(1, args.steps if args.steps <= 2 else 1))
+    rate, threads, sample = cpu_sample(args, reps=max(1, args.steps), warmup=max(0, args.warmup))
     cfg = scenes.workload_config(args.workload)
     line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -223,7 +277,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
-    cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=scenes.WORKLOADS[args.workload]["seed"] + rank,
+    cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=replica_seed(args.workload, rank),
                                                     **sub_box(args.workload, args.fraction))
     N, Nm, S = cfg.num_particles, cfg.num_metabolic_particles, cfg.num_metabolites
     items = N + Nm
@@ -257,12 +311,9 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     sim.sync()
     launches = sim.counters().kernel_launches - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    value, slowest_s = aggregate_replicas(items, args.steps, ms / 1e3, device="cuda")
+    ms = slowest_s * 1e3
     ms_per_step = ms / args.steps
-    value = items * world * args.steps / (ms / 1e3)
 
     # per-phase breakdown (for the roofline of the dominant kernel)
     phase_ms = per_phase_times(sim, stream, torch)
@@ -278,6 +329,9 @@ def run_ours(args):
     peak, peak_kind = _measured_peaks()
     alg = algorithmic_bytes(dom, N, Nm, S, bbar)
     achieved = alg / (phase_ms[dom] / 1e3) / 1e9
+    step_bytes = step_algorithmic_bytes(cfg, bbar)
+    step_achieved = step_bytes / (ms_per_step / 1e3) / 1e9
+    traffic = measured_traffic(dom, args.workload) if args.fraction == 1.0 else None
 
     # end to end through the C ABI with host buffers
     sim2 = native.Simulation(cfg, types, rules)
@@ -291,7 +345,8 @@ def run_ours(args):
     sim2.sync()
     e2e_s = time.perf_counter() - t0
     sim2.close()
-    e2e = {"value": items * world * args.steps / e2e_s, "unit": UNIT,
+    e2e_rate, _ = aggregate_replicas(items, args.steps, e2e_s, device="cuda")
+    e2e = {"value": e2e_rate, "unit": UNIT,
            "h2d_bytes_per_step": int((p.nbytes + m.nbytes) / args.steps),
            "d2h_bytes_per_step": int(rp_host.numel() + rm_host.numel()),
            "includes": "sc_load_state of the initial AoS state + sc_prepare, then per step sc_step + "
@@ -300,7 +355,7 @@ def run_ours(args):
 
     line = None
     if rank == 0:
-        cpu_rate, cpu_threads, cpu_desc = cpu_sample(args) if not args.no_cpu else (None, 0, "skipped")
+        cpu_rate, cpu_threads, cpu_desc = cpu_sample(args, reps=2) if not args.no_cpu else (None, 0, "skipped")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -316,8 +371,10 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": alg, "launch_ms": phase_ms[dom]},
+            "step_roofline": {"bound": "hbm", "achieved": step_achieved, "peak": peak, "unit": "GB/s",
+                              "frac": step_achieved / peak, "algorithmic_bytes_per_step": step_bytes},
             "phase_ms_per_launch": phase_ms, "phase_share_of_step": share,
             "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                              "sample": cpu_desc},
@@ -337,7 +394,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain_large", choices=sorted(scenes.WORKLOADS))
-    ap.add_argument("--cpu-fraction", type=float, default=1.0 / 16)
+    ap.add_argument("--cpu-fraction", type=float, default=0.25,
+                    help="volume fraction of the workload the CPU oracle steps (its timed sample)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
