@@ -79,6 +79,7 @@ struct ScCounters {
     int step;         // the step loop counter (main.cu:347)
     int tileCounter[4];
     int ppClassCount[4];  // items per relax work class (k_build_pp)
+    int ovfPP, ovfM;      // items whose particle / metabolic list overflowed (k_build_pp, k_build_m)
 };
 
 // Relax work classes: items with bond partners in their list, items with

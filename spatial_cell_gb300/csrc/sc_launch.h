@@ -42,6 +42,9 @@ struct ScBuffers {
     uint32_t *listPP, *listM, *listLM, *listD;
     int *cntPP, *cntM, *cntLM, *cntD;
     int *classPP;  // SC_RELAX_CLASSES segments of N item indices
+    int *permM, *permLM, *permD;  // count-ordered list position -> item
+    uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
+    int *ovfPP, *ovfM;            // overflowed items (PP: item index, M: list position)
     bool validPP, validM, validLM, validD;
     void invalidateLists() { validPP = validM = validLM = validD = false; }
     // polymerisation list

@@ -451,8 +451,15 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
         (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||
-        (rc = dalloc(s, &B.cntD, Nm)))
+        (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
+        (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)))
         return bail(rc);
+    // The LM list is built in the diffusion list's buffer when it fits.
+    if (sc_list_words(SC_LIST_LM, (int)N) <= sc_list_words(SC_LIST_D, (int)Nm)) {
+        B.scratchLM = B.listD;
+    } else if ((rc = dalloc(s, &B.scratchLM, sc_list_words(SC_LIST_LM, (int)N)))) {
+        return bail(rc);
+    }
     B.invalidateLists();
     B.polyCap = 4096;
     cudaMemset(B.ctr, 0, sizeof(ScCounters));

@@ -94,7 +94,58 @@ struct PairList {
     const uint32_t *__restrict__ list;
     const int *__restrict__ cnt;
     int cap;
+    const int *__restrict__ perm;  // position -> item (count-ordered lists; null: identity)
 };
+
+// Count-ordered list layout.  A builder block first writes each item's list
+// at the item's own position of `scratch`; this re-orders the block's items
+// by descending list length and copies the lists to their new positions, so
+// a consumer warp walks lists of similar lengths.  perm[g] is the item at
+// position g (-1 past the last item), cnt[g] its list length.  Every thread
+// of the block must call it.  `scratch` is written earlier in the same kernel
+// by other threads of the block, so it is read through a plain (coherent)
+// pointer after the barrier.
+template <int K>
+__device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit, int cap,
+                                                   const uint32_t *scratch, uint32_t *__restrict__ list,
+                                                   int *__restrict__ cnt, int *__restrict__ perm,
+                                                   int *__restrict__ ovf = nullptr, int *__restrict__ ovfCount = nullptr) {
+    __shared__ int hist[K + 3];
+    __shared__ int s_cnt[SC_THREADS], s_src[SC_THREADS];
+    const int t = threadIdx.x, b0 = blockIdx.x * SC_THREADS;
+    for (int b = t; b < K + 3; b += SC_THREADS) hist[b] = 0;
+    s_cnt[t] = valid ? c : -1;
+    __syncthreads();
+    const int bin = valid ? 1 + min(c, K + 1) : 0;
+    const int idx = atomicAdd(&hist[bin], 1);
+    __syncthreads();
+    if (t < 32) {  // exclusive prefix over bins, highest bin first
+        int carry = 0;
+        for (int top = K + 2; top >= 0; top -= 32) {
+            const int b = top - t;
+            const int v = b >= 0 ? hist[b] : 0;
+            int x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (t >= o) x += y;
+            }
+            if (b >= 0) hist[b] = carry + x - v;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+    }
+    __syncthreads();
+    s_src[hist[bin] + idx] = t;
+    __syncthreads();
+    const int src = s_src[t], cs = s_cnt[src], g = b0 + t;
+    if (g < cap) {
+        perm[g] = cs >= 0 ? b0 + src : -1;
+        cnt[g] = max(cs, 0);
+    }
+    const int n = min(max(cs, 0), min(K, limit));
+    for (int k = 0; k < n; k++) list[sc_list_at(K, g, k)] = scratch[sc_list_at(K, b0 + src, k)];
+    if (ovf && cs > min(K, limit)) ovf[atomicAdd(ovfCount, 1)] = g;
+}
 
 // Bonds of one particle held in registers.
 struct BondRegs {
@@ -151,7 +202,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
                                                          const float4 *__restrict__ pos, const int4 *__restrict__ info,
                                                          const int *__restrict__ nb, const int *__restrict__ bonds,
                                                          uint32_t *__restrict__ list, int *__restrict__ cnt, int cap,
-                                                         int *__restrict__ classIdx, int *__restrict__ classCount) {
+                                                         int *__restrict__ classIdx, int *__restrict__ classCount,
+                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = info[i];
@@ -176,6 +228,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
             }
         });
         cnt[i] = c;
+        if (c > min(SC_LIST_PP, P.listLimit)) ovf[atomicAdd(ovfCount, 1)] = i;
         if (B.n >= 1) cls = 0;
         else if (c <= min(SC_LIST_PP, P.listLimit) && (any & SC_PP_POLAR)) cls = 1;
     }
@@ -472,13 +525,13 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
 
 // Active items whose list overflowed: their neighbourhood is scanned.  A
 // separate kernel keeps the scan code out of k_relax's instruction stream.
-__global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, RelaxArgs A) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *A.nActivePtr) return;
-    if (A.L.cnt[i] <= min(SC_LIST_PP, P.listLimit)) return;
-    int4 in = A.info[i];
-    if (!(in.z & SC_ACTIVE)) return;
-    relax_item<true, 0>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
+__global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, RelaxArgs A, const int *__restrict__ ovf,
+                                                               const int *__restrict__ ovfCount) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
+        const int i = ovf[t];
+        int4 in = A.info[i];
+        if (in.z & SC_ACTIVE) relax_item<true, 0>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
+    }
 }
 
 // (float)((double)(rp + rt) + 0.8 * (double)rp) (metabolites.cuh:198,237,324),
@@ -499,21 +552,17 @@ struct CollisionDistCache {
 // ---- metabolites.cuh:140-264 relaxMetabolicParticles ----------------------
 // List: per metabolic item, cell by cell, the colliding metabolic items then
 // the colliding lipids (SC_M_FROM_P), as the reference's loops visit them.
-__global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
-                                                        const uint32_t *__restrict__ cellStartP,
-                                                        const int *__restrict__ nActivePtr,
-                                                        const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-                                                        const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                        uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    if (!(minfo[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
+// The M list of metabolic item i, written at position i of `list`.
+__device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *__restrict__ cellStartM,
+                                             const uint32_t *__restrict__ cellStartP, int i,
+                                             const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                             const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                             uint32_t *list, int &c) {
     float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cm, cp;
-    int c = 0;
     cells27(P, pp, [&](uint32_t key) {
         for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i || !(minfo[j].z & SC_ACTIVE)) continue;
@@ -537,8 +586,23 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
             }
         }
     });
-    cnt[i] = c;
 }
+
+__global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
+                                                        const uint32_t *__restrict__ cellStartP,
+                                                        const int *__restrict__ nActivePtr,
+                                                        const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                                        const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                        uint32_t *__restrict__ list, uint32_t *scratch,
+                                                        int *__restrict__ cnt, int *__restrict__ perm, int cap,
+                                                        int *__restrict__ ovf, int *__restrict__ ovfCount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < *nActivePtr;
+    int c = 0;
+    if (valid && (minfo[i].z & SC_ACTIVE)) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
+    emit_count_ordered<SC_LIST_M>(valid, c, P.listLimit, cap, scratch, list, cnt, perm, ovf, ovfCount);
+}
+
 
 struct RelaxMArgs {
     const uint32_t *__restrict__ cellStartM, *__restrict__ cellStartP;
@@ -567,14 +631,16 @@ __device__ __forceinline__ void metab_pair(const Imager &IM, sc_f3 pp, sc_f3 ppv
 // Items whose list fits.  The next entry's neighbour data is loaded while the
 // current one is evaluated (the loop is bound by the latency of those loads).
 __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, RelaxMArgs A) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *A.nActivePtr) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
+    if (g >= *A.nActivePtr) return;
+    const int i = A.L.perm[g];
+    if (i < 0) return;
     float4 v4 = A.mvelIn[i];
     if (!(A.minfo[i].z & SC_ACTIVE)) {
         A.mvelOut[i] = v4;
         return;
     }
-    const int c = A.L.cnt[i];
+    const int c = A.L.cnt[g];
     if (c > min(SC_LIST_M, P.listLimit)) return;
     float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -586,7 +652,7 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
     float w = 0.0f;
     CollisionDistCache cm, cp;   // neighbours of each kind share a radius
     if (c > 0) {
-        uint32_t e = A.L.list[sc_list_at(SC_LIST_M, i, 0)];
+        uint32_t e = A.L.list[sc_list_at(SC_LIST_M, g, 0)];
         bool fromP = (e & SC_M_FROM_P) != 0;
         int j = (int)(e & SC_M_INDEX);
         float4 t4 = fromP ? A.ppos[j] : A.mpos[j];
@@ -595,7 +661,7 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
             uint32_t en = 0;
             float4 t4n = t4, tvn = tv;
             if (k < c) {
-                en = A.L.list[sc_list_at(SC_LIST_M, i, k)];
+                en = A.L.list[sc_list_at(SC_LIST_M, g, k)];
                 int jn = (int)(en & SC_M_INDEX);
                 bool fn = (en & SC_M_FROM_P) != 0;
                 t4n = fn ? A.ppos[jn] : A.mpos[jn];
@@ -611,12 +677,9 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
-// Active items whose list overflowed: the reference's loops over the 27 cells.
-__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *A.nActivePtr) return;
-    if (A.L.cnt[i] <= min(SC_LIST_M, P.listLimit)) return;
-    if (!(A.minfo[i].z & SC_ACTIVE)) return;
+// An item whose list overflowed: the reference's loops over the 27 cells.
+__device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const RelaxMArgs &A, int i) {
+    if (i < 0 || !(A.minfo[i].z & SC_ACTIVE)) return;
     float4 v4 = A.mvelIn[i];
     float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -651,24 +714,25 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
+// The items whose list overflowed (listed by k_build_m), grid-stride.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A,
+                                                                     const int *__restrict__ ovf,
+                                                                     const int *__restrict__ ovfCount) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x)
+        relax_metab_scan_item(P, A, A.L.perm[ovf[t]]);
+}
+
 // ---- metabolites.cuh:266-350 relaxMetabolicParticlePartners ----------------
 // Only lipids change, and only their own velocity, which no other thread of
 // this kernel reads: updated in place.  List: the colliding metabolic items.
-__global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
-                                                         const int *__restrict__ nActivePtr,
-                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-                                                         uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    int4 in = pinfo[i];
-    if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) { cnt[i] = 0; return; }
+__device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t *__restrict__ cellStartM, int i,
+                                              const float4 *__restrict__ ppos_, const float4 *__restrict__ mpos,
+                                              const int4 *__restrict__ minfo, uint32_t *list, int &c) {
     float4 p4 = ppos_[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cc;
-    int c = 0;
     scan27(P, cellStartM, pp, [&](int j) {
         if (!(minfo[j].z & SC_ACTIVE)) return;
         float4 t4 = mpos[j];
@@ -679,7 +743,23 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
             c++;
         }
     });
-    cnt[i] = c;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
+                                                         const int *__restrict__ nActivePtr,
+                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                                         uint32_t *__restrict__ list, uint32_t *scratch,
+                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < *nActivePtr;
+    int c = 0;
+    if (valid) {
+        int4 in = pinfo[i];
+        if ((in.z & SC_ACTIVE) && in.y == SC_PARTICLE_TYPE_LIPID)
+            build_lm_item(P, cellStartM, i, ppos_, mpos, minfo, scratch, c);
+    }
+    emit_count_ordered<SC_LIST_LM>(valid, c, P.listLimit, cap, scratch, list, cnt, perm);
 }
 
 __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
@@ -687,8 +767,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
     PairList<SC_LIST_LM> L, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
     const float4 *__restrict__ mvel) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
+    if (g >= *nActivePtr) return;
+    const int i = L.perm[g];
+    if (i < 0) return;
     int4 in = pinfo[i];
     if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) return;
     float4 p4 = ppos_[i];
@@ -707,10 +789,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
         w += 2.0f;
         dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
     };
-    const int c = L.cnt[i];
+    const int c = L.cnt[g];
     if (c <= min(SC_LIST_LM, P.listLimit)) {
         for (int k = 0; k < c; k++) {
-            int j = (int)L.list[sc_list_at(SC_LIST_LM, i, k)];
+            int j = (int)L.list[sc_list_at(SC_LIST_LM, g, k)];
             body(j, mpos[j]);
         }
     } else {
@@ -1082,18 +1164,13 @@ __global__ void __launch_bounds__(1024) k_polymerize(ScParams P, const uint32_t 
 // ---- metabolites.cuh:352-431 diffuseMetabolites ------------------------------
 // List: the metabolic items within maxDiffusionDistance (cube, then sphere),
 // built after applyVelocities and read by all diffusion sub-iterations.
-__global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32_t *__restrict__ cellStart,
-                                                        const int *__restrict__ nActivePtr,
-                                                        const float4 *__restrict__ pos, const int4 *__restrict__ info,
-                                                        uint32_t *__restrict__ list, int *__restrict__ cnt, int cap) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    if (!(info[i].z & SC_ACTIVE)) { cnt[i] = 0; return; }
+__device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *__restrict__ cellStart, int i,
+                                             const float4 *__restrict__ pos, const int4 *__restrict__ info,
+                                             uint32_t *list, int &c) {
     float4 p4 = pos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
-    int c = 0;
     scan27(P, cellStart, pp, [&](int j) {
         if (j == i || !(info[j].z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
@@ -1104,7 +1181,18 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
             c++;
         }
     });
-    cnt[i] = c;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32_t *__restrict__ cellStart,
+                                                        const int *__restrict__ nActivePtr,
+                                                        const float4 *__restrict__ pos, const int4 *__restrict__ info,
+                                                        uint32_t *__restrict__ list, uint32_t *scratch,
+                                                        int *__restrict__ cnt, int *__restrict__ perm, int cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < *nActivePtr;
+    int c = 0;
+    if (valid && (info[i].z & SC_ACTIVE)) build_d_item(P, cellStart, i, pos, info, scratch, c);
+    emit_count_ordered<SC_LIST_D>(valid, c, P.listLimit, cap, scratch, list, cnt, perm);
 }
 
 template <int SP>
@@ -1114,8 +1202,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
                                                         PairList<SC_LIST_D> L, const float4 *__restrict__ metIn,
                                                         float4 *__restrict__ metOut) {
     constexpr int Q = SP / 4;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
+    if (g >= *nActivePtr) return;
+    const int i = L.perm[g];
+    if (i < 0) return;
     float pm[SP];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -1131,11 +1221,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
 #pragma unroll
     for (int k = 0; k < SP; k++) dm[k] = 0.0f;
     const int S = P.S;
-    auto body = [&](int j) {
+    auto apply = [&](const float4 *v) {
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            float4 v = metIn[(size_t)j * Q + q];
-            float tm[4] = {v.x, v.y, v.z, v.w};
+            float tm[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 int k = 4 * q + c;
@@ -1146,9 +1235,31 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
             }
         }
     };
-    const int c = L.cnt[i];
+    auto body = [&](int j) {
+        float4 v[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) v[q] = metIn[(size_t)j * Q + q];
+        apply(v);
+    };
+    const int c = L.cnt[g];
     if (c <= min(SC_LIST_D, P.listLimit)) {
-        for (int k = 0; k < c; k++) body((int)L.list[sc_list_at(SC_LIST_D, i, k)]);
+        // the next neighbour's amounts are loaded while the current ones are applied
+        float4 cur[Q], nxt[Q];
+        if (c > 0) {
+            const int j0 = (int)L.list[sc_list_at(SC_LIST_D, g, 0)];
+#pragma unroll
+            for (int q = 0; q < Q; q++) cur[q] = metIn[(size_t)j0 * Q + q];
+        }
+        for (int k = 1; k <= c; k++) {
+            if (k < c) {
+                const int jn = (int)L.list[sc_list_at(SC_LIST_D, g, k)];
+#pragma unroll
+                for (int q = 0; q < Q; q++) nxt[q] = metIn[(size_t)jn * Q + q];
+            }
+            apply(cur);
+#pragma unroll
+            for (int q = 0; q < Q; q++) cur[q] = nxt[q];
+        }
     } else {
         float4 p4 = pos[i];
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -1266,9 +1377,10 @@ static void ensure_pp(ScLaunchCtx &c) {
     if (B.validPP) return;
     PFields F = B.P();
     cudaMemsetAsync(B.ctr->ppClassCount, 0, sizeof(B.ctr->ppClassCount), c.st);
+    cudaMemsetAsync(&B.ctr->ovfPP, 0, sizeof(int), c.st);
     k_build_pp<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
                                                          F.bonds, B.listPP, B.cntPP, c.P.N, B.classPP,
-                                                         B.ctr->ppClassCount);
+                                                         B.ctr->ppClassCount, B.ovfPP, &B.ctr->ovfPP);
     (*c.launches)++;
     B.validPP = true;
 }
@@ -1278,6 +1390,7 @@ static PairList<SC_LIST_PP> pp_list(const ScLaunchCtx &c) {
     L.list = c.B->listPP;
     L.cnt = c.B->cntPP;
     L.cap = c.P.N;
+    L.perm = nullptr;
     return L;
 }
 
@@ -1324,7 +1437,7 @@ void sc_phase_relax(ScLaunchCtx &c) {
     k_relax<0><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
     k_relax<1><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
     k_relax<2><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
-    k_relax_overflow<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax_overflow<<<std::min(nblocks(c.P.N), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfPP, &B.ctr->ovfPP);
     (*c.launches) += 3;
     B.cp[FP_VEL] ^= 1;
     B.cp[FP_ROT] ^= 1;
@@ -1338,8 +1451,12 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     MFields M = B.M(), X = B.Mnext();
     PFields F = B.P();
     if (!B.validM) {
+        // the diffusion list's buffer is the build scratch (that list is rebuilt after the next move anyway)
+        B.validD = false;
+        cudaMemsetAsync(&B.ctr->ovfM, 0, sizeof(int), c.st);
         k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
-                                                             M.info, F.pos, F.info, B.listM, B.cntM, c.P.Nm);
+                                                             M.info, F.pos, F.info, B.listM, B.listD, B.cntM, B.permM,
+                                                             c.P.Nm, B.ovfM, &B.ctr->ovfM);
         (*c.launches)++;
         B.validM = true;
     }
@@ -1347,9 +1464,11 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     L.list = B.listM;
     L.cnt = B.cntM;
     L.cap = c.P.Nm;
+    L.perm = B.permM;
     RelaxMArgs A{B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, L, M.vel, X.vel, F.pos, F.info, F.vel};
     k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
-    k_relax_metab_overflow<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax_metab_overflow<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,
+                                                                                             &B.ctr->ovfM);
     B.cm[FM_VEL] ^= 1;
     (*c.launches) += 2;
 }
@@ -1360,8 +1479,9 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     MFields M = B.M();
     PFields F = B.P();
     if (!B.validLM) {
+        if (B.scratchLM == B.listD) B.validD = false;
         k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos,
-                                                             M.info, B.listLM, B.cntLM, c.P.N);
+                                                             M.info, B.listLM, B.scratchLM, B.cntLM, B.permLM, c.P.N);
         (*c.launches)++;
         B.validLM = true;
     }
@@ -1369,6 +1489,7 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     L.list = B.listLM;
     L.cnt = B.cntLM;
     L.cap = c.P.N;
+    L.perm = B.permLM;
     k_relax_partners<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
                                                                F.vel, L, M.pos, M.info, M.vel);
     (*c.launches)++;
@@ -1428,8 +1549,10 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     if (c.P.Nm <= 0) return;
     MFields M = B.M(), X = B.Mnext();
     if (!B.validD) {
+        // the metabolic relaxation list's buffer is the build scratch
+        B.validM = false;
         k_build_d<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                             B.listD, B.cntD, c.P.Nm);
+                                                             B.listD, B.listM, B.cntD, B.permD, c.P.Nm);
         (*c.launches)++;
         B.validD = true;
     }
@@ -1437,6 +1560,7 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     L.list = B.listD;
     L.cnt = B.cntD;
     L.cap = c.P.Nm;
+    L.perm = B.permD;
     switch (c.P.SP) {
         case 4:
             k_diffuse<4><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
