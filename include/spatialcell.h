@@ -281,6 +281,18 @@ void *sc_get_stream(sc_sim *sim);
  * counters' ranges, zero beyond), into capacity-sized host buffers. */
 int sc_reduce_frame(sc_sim *sim, sc_reduced_particle *particles,
                     sc_reduced_metabolic_particle *metabolic);
+/* The same frame, streamed: the reduction is enqueued on the sim's stream
+ * behind the work already there and the copy to the host runs on a second
+ * stream, so the steps enqueued next overlap it (the reference hands each
+ * frame to a std::async writer thread, main.cu:95-126).  Two frames can be in
+ * flight; a third waits on the device for the first one's copy.  The host
+ * buffers must stay valid until the frame has landed, and must be pinned
+ * (cudaHostAlloc / cudaHostRegister) for the copy to overlap the steps.
+ * Returns the frame's ticket (>= 0) or a negative SC_E_* code. */
+int64_t sc_reduce_frame_async(sc_sim *sim, sc_reduced_particle *particles,
+                              sc_reduced_metabolic_particle *metabolic);
+/* Blocks until frame `ticket` (and every earlier frame) is in host memory. */
+int sc_frame_wait(sc_sim *sim, int64_t ticket);
 
 /* ---- allocation-free cell sort (no counterpart in the reference) ----
  * For callers that cannot let a library allocate device memory: a framework

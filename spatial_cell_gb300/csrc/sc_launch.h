@@ -52,8 +52,8 @@ struct ScBuffers {
     int polyCap;
     ScCounters *ctr;
     // frames
-    sc_reduced_particle *redP;
-    sc_reduced_metabolic_particle *redM;
+    sc_reduced_particle *redP, *redP2;                // frame staging, two slots
+    sc_reduced_metabolic_particle *redM, *redM2;
 
     // current view of every particle / metabolic field
     PFields P() const {
@@ -128,4 +128,4 @@ void sc_phase_transition(ScLaunchCtx &c);
 void sc_phase_polymerize(ScLaunchCtx &c);
 void sc_phase_diffuse(ScLaunchCtx &c);
 void sc_phase_remove_interfering(ScLaunchCtx &c);
-void sc_phase_reduce(ScLaunchCtx &c);
+void sc_phase_reduce(ScLaunchCtx &c, int slot);

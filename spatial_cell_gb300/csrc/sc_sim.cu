@@ -148,6 +148,9 @@ struct sc_sim {
     ScParams P;
     ScBuffers B;
     cudaStream_t st = nullptr;
+    cudaStream_t copySt = nullptr;          // frame copies to the host
+    cudaEvent_t reduced[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    int64_t frames = 0;                     // frames enqueued by sc_reduce_frame_async
     int device = 0;
     int gridCap = 0;
     long long launches = 0;
@@ -445,7 +448,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
         (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.redP, N)) ||
-        (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
+        (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.redP2, N)) || (rc = dalloc(s, &B.redM2, Nm)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
         (rc = dalloc(s, &B.cntPP, N)) ||
         (rc = dalloc(s, &B.classPP, (size_t)SC_RELAX_CLASSES * N)) ||
         (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
@@ -466,6 +469,11 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     cudaMemset(B.cellStartP, 0, ((size_t)P.cells + 1) * 4);
     cudaMemset(B.cellStartM, 0, ((size_t)P.cells + 1) * 4);
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copySt, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        e = cudaEventCreateWithFlags(&s->reduced[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copied[k], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
@@ -479,6 +487,14 @@ void sc_destroy(sc_sim *s) {
     if (s->st) {
         cudaStreamSynchronize(s->st);
         cudaStreamDestroy(s->st);
+    }
+    if (s->copySt) {
+        cudaStreamSynchronize(s->copySt);
+        cudaStreamDestroy(s->copySt);
+    }
+    for (int k = 0; k < 2; k++) {
+        if (s->reduced[k]) cudaEventDestroy(s->reduced[k]);
+        if (s->copied[k]) cudaEventDestroy(s->copied[k]);
     }
     for (void *p : s->allocs) cudaFree(p);
     delete s;
@@ -581,6 +597,7 @@ int sc_sync(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);
     SC_CK(s, cudaStreamSynchronize(s->st));
+    SC_CK(s, cudaStreamSynchronize(s->copySt));
     int derr = 0;
     SC_CK(s, cudaMemcpy(&derr, &s->B.ctr->error, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr) return set_err(s, SC_E_DEVICE, "device-side error code " + std::to_string(derr));
@@ -654,7 +671,9 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);
     ScLaunchCtx c = ctx(s);
-    sc_phase_reduce(c);
+    // the synchronous form uses slot 0 once the frames in flight have landed
+    if (s->frames > 0) SC_CK(s, cudaStreamSynchronize(s->copySt));
+    sc_phase_reduce(c, 0);
     int rc = check_launch(s);
     if (rc) return rc;
     if (particles && s->P.N > 0)
@@ -665,6 +684,39 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
                                  cudaMemcpyDeviceToHost, s->st));
     SC_CK(s, cudaStreamSynchronize(s->st));
     return SC_OK;
+}
+
+int64_t sc_reduce_frame_async(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabolic_particle *metabolic) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    const int slot = (int)(s->frames & 1);
+    // the slot's previous frame must have left the device before it is rewritten
+    if (s->frames >= 2) SC_CK(s, cudaStreamWaitEvent(s->st, s->copied[slot], 0));
+    ScLaunchCtx c = ctx(s);
+    sc_phase_reduce(c, slot);
+    int rc = check_launch(s);
+    if (rc) return rc;
+    SC_CK(s, cudaEventRecord(s->reduced[slot], s->st));
+    SC_CK(s, cudaStreamWaitEvent(s->copySt, s->reduced[slot], 0));
+    if (particles && s->P.N > 0)
+        SC_CK(s, cudaMemcpyAsync(particles, slot ? s->B.redP2 : s->B.redP,
+                                 (size_t)s->P.N * sizeof(sc_reduced_particle), cudaMemcpyDeviceToHost, s->copySt));
+    if (metabolic && s->P.Nm > 0)
+        SC_CK(s, cudaMemcpyAsync(metabolic, slot ? s->B.redM2 : s->B.redM,
+                                 (size_t)s->P.Nm * sizeof(sc_reduced_metabolic_particle), cudaMemcpyDeviceToHost,
+                                 s->copySt));
+    SC_CK(s, cudaEventRecord(s->copied[slot], s->copySt));
+    return s->frames++;
+}
+
+int sc_frame_wait(sc_sim *s, int64_t ticket) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (ticket < 0 || ticket >= s->frames) return set_err(s, SC_E_INVALID, "no such frame");
+    cudaSetDevice(s->device);
+    // The slot's event records this frame's copy or a later one on the same
+    // in-order copy stream; either way this frame has landed when it fires.
+    SC_CK(s, cudaEventSynchronize(s->copied[ticket & 1]));
+    return check_launch(s);
 }
 
 }  // extern "C"

@@ -1589,15 +1589,16 @@ void sc_phase_remove_interfering(ScLaunchCtx &c) {
     (*c.launches)++;
 }
 
-void sc_phase_reduce(ScLaunchCtx &c) {
+void sc_phase_reduce(ScLaunchCtx &c, int slot) {
     ScBuffers &B = *c.B;
     if (c.P.N > 0) {
-        k_reduce_particles<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, c.P.N, B.P(), B.redP);
+        k_reduce_particles<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, c.P.N, B.P(),
+                                                                     slot ? B.redP2 : B.redP);
         (*c.launches)++;
     }
     if (c.P.Nm > 0) {
         k_reduce_metabolic<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, c.P.Nm, c.P.SP / 4, B.M(),
-                                                                      B.redM);
+                                                                      slot ? B.redM2 : B.redM);
         (*c.launches)++;
     }
 }

@@ -36,6 +36,8 @@ _SIGS = {
     "sc_export_grid": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "sc_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(abi.Counters)]),
     "sc_reduce_frame": (ctypes.c_int, [_P, _P, _P]),
+    "sc_reduce_frame_async": (ctypes.c_int64, [_P, _P, _P]),
+    "sc_frame_wait": (ctypes.c_int, [_P, ctypes.c_int64]),
     "sc_get_stream": (ctypes.c_void_p, [_P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
     "sc_frames_write_frame": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config), _P, _P]),
@@ -181,3 +183,13 @@ class Simulation:
 
     def reduce_frame_ptr(self, p_ptr, m_ptr):
         _check(self.L.sc_reduce_frame(self.h, p_ptr, m_ptr), self.h, "sc_reduce_frame")
+
+    def reduce_frame_async_ptr(self, p_ptr, m_ptr):
+        """Streams the current frame into (pinned) host buffers; returns its ticket."""
+        t = self.L.sc_reduce_frame_async(self.h, p_ptr, m_ptr)
+        if t < 0:
+            _check(int(t), self.h, "sc_reduce_frame_async")
+        return t
+
+    def frame_wait(self, ticket):
+        _check(self.L.sc_frame_wait(self.h, ticket), self.h, "sc_frame_wait")
