@@ -107,6 +107,7 @@ struct ScParams {
     int periodic;             // periodic box extension (sc_config.periodic)
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
     int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
+    int tileCapM, tileCapP;   // tile capacities (slots) of the metabolic sweeps; 0: tiles off
 };
 #define SC_BINNED_P 1
 #define SC_BINNED_M 2

@@ -129,3 +129,5 @@ void sc_phase_polymerize(ScLaunchCtx &c);
 void sc_phase_diffuse(ScLaunchCtx &c);
 void sc_phase_remove_interfering(ScLaunchCtx &c);
 void sc_phase_reduce(ScLaunchCtx &c, int slot);
+void sc_tile_init();
+size_t sc_tile_bytes(int capM, int capP, int perSlot);

@@ -7,10 +7,12 @@
 
 #include <algorithm>
 #include <map>
+#include <cmath>
 #include <string>
 #include <vector>
 
 #include "sc_launch.h"
+#include "sc_tile.cuh"
 
 extern "C" const char *sc_host_last_error(void);
 
@@ -343,6 +345,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     cudaGetDevice(&s->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    sc_tile_init();
     s->gridCap = std::max(1, sms) * (2048 / SC_THREADS);
     ScParams &P = s->P;
     memset(&P, 0, sizeof P);
@@ -370,6 +373,24 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.periodic = cfg->periodic != 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
     if (const char *lim = getenv("SC_PAIR_LIST_LIMIT")) P.listLimit = std::max(0, atoi(lim));
+    // Tile capacities of the metabolic sweeps from the mean occupancy of the
+    // cells a tile spans, with room for fluctuations.  The tiled sweep is
+    // selected with SC_TILES=1 (the per-item list sweep is faster at present);
+    // it is off when the tile would not fit in shared memory.
+    {
+        const double cells = std::pow((double)std::max(P.nUsed, 1), 3.0);
+        const double tileCells = (double)SC_TILE_NCOL * (SC_TILE_SZ + 3);
+        auto cap = [&](double items) {
+            const double mean = items / cells * tileCells;
+            return (int)((1.1 * mean + 4.0 * std::sqrt(mean) + 32.0 + 31.0) / 32.0) * 32;
+        };
+        P.tileCapM = cap((double)P.Nm);
+        P.tileCapP = cap((double)P.N);
+        const char *tilesEnv = getenv("SC_TILES");
+        if (!(tilesEnv && atoi(tilesEnv) == 1) || P.tileCapM + P.tileCapP > 65535 ||
+            sc_tile_bytes(P.tileCapM, P.tileCapP, 32) > 200 * 1024)
+            P.tileCapM = P.tileCapP = 0;
+    }
 
     auto bail = [&](int rc) {
         sc_destroy(s);

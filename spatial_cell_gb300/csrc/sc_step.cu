@@ -15,6 +15,7 @@
 // between kernels (the reference reads nActiveParticles back three times per
 // step, main.cu:369,399,616).
 #include "sc_launch.h"
+#include "sc_tile.cuh"
 
 __device__ __forceinline__ bool p_order(int ta, int ia, int tb, int ib) { return ta < tb || (ta == tb && ia < ib); }
 
@@ -97,10 +98,21 @@ struct PairList {
     const int *__restrict__ perm;  // position -> item (count-ordered lists; null: identity)
 };
 
+// Packed 32-bit list entries: 4 consecutive entries of an item share one
+// 16-byte chunk, chunks warp-tiled (chunk q of position g at
+// ((g/32) * K/4 + q) * 32 + g%32), so one load brings 4 entries.
+__host__ __device__ __forceinline__ size_t sc_list4_at(int K, int g, int k) {
+    return (((size_t)(g >> 5) * (size_t)(K / 4) + (size_t)(k >> 2)) * 32 + (size_t)(g & 31)) * 4 + (size_t)(k & 3);
+}
+__device__ __forceinline__ const uint4 *sc_list4_chunks(const uint32_t *list, int K, int g) {
+    return reinterpret_cast<const uint4 *>(list) + (size_t)(g >> 5) * (size_t)(K / 4) * 32 + (size_t)(g & 31);
+}
+
 // Count-ordered list layout.  A builder block first writes each item's list
 // at the item's own position of `scratch`; this re-orders the block's items
 // by descending list length and copies the lists to their new positions, so
-// a consumer warp walks lists of similar lengths.  perm[g] is the item at
+// a consumer warp walks lists of similar lengths; the lists are written
+// packed (sc_list4_at).  perm[g] is the item at
 // position g (-1 past the last item), cnt[g] its list length.  Every thread
 // of the block must call it.  `scratch` is written earlier in the same kernel
 // by other threads of the block, so it is read through a plain (coherent)
@@ -143,7 +155,7 @@ __device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit,
         cnt[g] = max(cs, 0);
     }
     const int n = min(max(cs, 0), min(K, limit));
-    for (int k = 0; k < n; k++) list[sc_list_at(K, g, k)] = scratch[sc_list_at(K, b0 + src, k)];
+    for (int k = 0; k < n; k++) list[sc_list4_at(K, g, k)] = scratch[sc_list_at(K, b0 + src, k)];
     if (ovf && cs > min(K, limit)) ovf[atomicAdd(ovfCount, 1)] = g;
 }
 
@@ -630,7 +642,7 @@ __device__ __forceinline__ void metab_pair(const Imager &IM, sc_f3 pp, sc_f3 ppv
 
 // Items whose list fits.  The next entry's neighbour data is loaded while the
 // current one is evaluated (the loop is bound by the latency of those loads).
-__global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, RelaxMArgs A) {
+__global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, RelaxMArgs A) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *A.nActivePtr) return;
     const int i = A.L.perm[g];
@@ -651,28 +663,31 @@ __global__ void __launch_bounds__(SC_THREADS, 5) k_relax_metab(ScParams P, Relax
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
     CollisionDistCache cm, cp;   // neighbours of each kind share a radius
-    if (c > 0) {
-        uint32_t e = A.L.list[sc_list_at(SC_LIST_M, g, 0)];
-        bool fromP = (e & SC_M_FROM_P) != 0;
-        int j = (int)(e & SC_M_INDEX);
-        float4 t4 = fromP ? A.ppos[j] : A.mpos[j];
-        float4 tv = fromP ? A.pvel[j] : A.mvelIn[j];
-        for (int k = 1; k <= c; k++) {
-            uint32_t en = 0;
-            float4 t4n = t4, tvn = tv;
-            if (k < c) {
-                en = A.L.list[sc_list_at(SC_LIST_M, g, k)];
-                int jn = (int)(en & SC_M_INDEX);
-                bool fn = (en & SC_M_FROM_P) != 0;
-                t4n = fn ? A.ppos[jn] : A.mpos[jn];
-                tvn = fn ? A.pvel[jn] : A.mvelIn[jn];
+    // Four entries per list load; their neighbours are gathered together, and
+    // the next chunk of the list is loaded while this one is evaluated.
+    const uint4 *__restrict__ chunks = sc_list4_chunks(A.L.list, SC_LIST_M, g);
+    uint4 E = c > 0 ? chunks[0] : make_uint4(0, 0, 0, 0);
+    for (int k0 = 0; k0 < c; k0 += 4) {
+        const uint4 En = k0 + 4 < c ? chunks[(size_t)(k0 / 4 + 1) * 32] : make_uint4(0, 0, 0, 0);
+        const uint32_t e[4] = {E.x, E.y, E.z, E.w};
+        float4 t4[4], tv[4];
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+            if (k0 + kk < c) {
+                const int j = (int)(e[kk] & SC_M_INDEX);
+                const bool fp = (e[kk] & SC_M_FROM_P) != 0;
+                t4[kk] = fp ? A.ppos[j] : A.mpos[j];
+                tv[kk] = fp ? A.pvel[j] : A.mvelIn[j];
             }
-            float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
-            metab_pair(IM, pp, ppv, t4, tv, cd, fromP, dV, w);
-            fromP = (en & SC_M_FROM_P) != 0;
-            t4 = t4n;
-            tv = tvn;
         }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+            if (k0 + kk >= c) break;
+            const bool fp = (e[kk] & SC_M_FROM_P) != 0;
+            const float cd = fp ? cp.get(prad, t4[kk].w) : cm.get(prad, t4[kk].w);
+            metab_pair(IM, pp, ppv, t4[kk], tv[kk], cd, fp, dV, w);
+        }
+        E = En;
     }
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
@@ -719,7 +734,260 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
                                                                      const int *__restrict__ ovf,
                                                                      const int *__restrict__ ovfCount) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x)
-        relax_metab_scan_item(P, A, A.L.perm[ovf[t]]);
+        relax_metab_scan_item(P, A, A.L.perm ? A.L.perm[ovf[t]] : ovf[t]);
+}
+
+// ---- the same sweep on column-segment tiles (sc_tile.cuh) ---------------------
+// Shared-memory header of a tile block; the tile arrays follow it.
+struct TileMHeader {
+    uint64_t bar;
+    int nItems;
+    int runBase[SC_TILE_NITEMCOL], runStart[SC_TILE_NITEMCOL + 1];
+    TileRanges RM, RP;
+};
+#define SC_TILE_HDR_BYTES ((sizeof(TileMHeader) + 127) / 128 * 128)
+
+// The block's geometry, both range tables and its item runs (the inner
+// columns over [z0, z1)); ends with a block barrier.
+__device__ __forceinline__ void tile_m_setup(const ScParams &P, const TileGeom &G, const uint32_t *__restrict__ cellStartM,
+                                             const uint32_t *__restrict__ cellStartP, TileMHeader &H) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) tile_ranges(P, G, cellStartM, 0, P.tileCapM, H.RM);
+    if (warp == 1) tile_ranges(P, G, cellStartP, P.tileCapM, P.tileCapP, H.RP);
+    if (warp == 2) {
+        int b = 0, l = 0;
+        if (lane < SC_TILE_NITEMCOL) {
+            const int gx = G.x0 + lane / SC_TILE_TY, gy = G.y0 + lane % SC_TILE_TY;
+            if (gx < G.n && gy < G.n) {
+                const uint32_t k0 = cell_key(P, (uint32_t)gx, (uint32_t)gy, 0);
+                b = (int)cellStartM[k0 + (uint32_t)G.z0];
+                l = (int)cellStartM[k0 + (uint32_t)G.z1] - b;
+            }
+        }
+        int x = l;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < SC_TILE_NITEMCOL) {
+            H.runBase[lane] = b;
+            H.runStart[lane] = x - l;
+        }
+        if (lane == SC_TILE_NITEMCOL - 1) {
+            H.runStart[SC_TILE_NITEMCOL] = x;
+            H.nItems = x;
+        }
+    }
+    __syncthreads();
+}
+// Slot of the block's t-th item.
+__device__ __forceinline__ int tile_item(const TileMHeader &H, int t) {
+    int q = 0;
+#pragma unroll
+    for (int k = 1; k < SC_TILE_NITEMCOL; k++) q += t >= H.runStart[k];
+    return H.runBase[q] + (t - H.runStart[q]);
+}
+
+// Packed 16-bit list entries: 8 consecutive entries of an item share one
+// 16-byte chunk, chunks warp-tiled (chunk q of item i at
+// ((i/32) * K/8 + q) * 32 + i%32), so one load brings 8 entries.
+__host__ __device__ __forceinline__ size_t sc_list16_at(int K, int i, int k) {
+    return (((size_t)(i >> 5) * (size_t)(K / 8) + (size_t)(k >> 3)) * 32 + (size_t)(i & 31)) * 8 + (size_t)(k & 7);
+}
+
+// M list on tiles: entries are 16-bit tile offsets (metabolic slots first,
+// then particle slots), in the reference's visiting order, packed.  An item whose
+// neighbourhood leaves the tile, or whose list would overflow, is listed in
+// `ovf` for the scanning kernel.
+__global__ void __launch_bounds__(SC_THREADS) k_build_m_tile(ScParams P, const uint32_t *__restrict__ cellStartM,
+                                                             const uint32_t *__restrict__ cellStartP,
+                                                             const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                                             const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                             uint16_t *__restrict__ list, int *__restrict__ cnt,
+                                                             int *__restrict__ ovf, int *__restrict__ ovfCount) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    TileMHeader &H = *reinterpret_cast<TileMHeader *>(smraw);
+    const int cap = P.tileCapM + P.tileCapP;
+    float4 *spos = reinterpret_cast<float4 *>(smraw + SC_TILE_HDR_BYTES);
+    uint8_t *sok = reinterpret_cast<uint8_t *>(spos + cap);
+    TileGeom G;
+    G.init(P, blockIdx.x);
+    tile_m_setup(P, G, cellStartM, cellStartP, H);
+    for (int r = 0; r < SC_TILE_NRANGE; r++) {
+        for (int k = threadIdx.x; k < H.RM.len[r]; k += blockDim.x) {
+            const int j = H.RM.base[r] + k, o = H.RM.off[r] + k;
+            spos[o] = mpos[j];
+            sok[o] = (minfo[j].z & SC_ACTIVE) ? 1 : 0;
+        }
+        for (int k = threadIdx.x; k < H.RP.len[r]; k += blockDim.x) {
+            const int j = H.RP.base[r] + k, o = H.RP.off[r] + k;
+            const int4 tin = pinfo[j];
+            spos[o] = ppos_[j];
+            sok[o] = ((tin.z & SC_ACTIVE) && tin.y == SC_PARTICLE_TYPE_LIPID) ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    const int bits = P.bits;
+    const uint32_t zmask = (1u << bits) - 1u;
+    for (int t = threadIdx.x; t < H.nItems; t += blockDim.x) {
+        const int i = tile_item(H, t);
+        if (!(minfo[i].z & SC_ACTIVE)) {
+            cnt[i] = 0;
+            continue;
+        }
+        float4 p4 = mpos[i];
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
+        const float prad = p4.w, lim = P.maxInt;
+        CollisionDistCache cm, cp;
+        int c = 0;
+        bool miss = false;
+        const int climit = min(SC_LIST_M, P.listLimit);
+        cells27(P, pp, [&](uint32_t key) {
+            if (miss) return;
+            const int r = G.range_of((int)(key >> (2 * bits)), (int)((key >> bits) & zmask), (int)(key & zmask));
+            const int am = (int)cellStartM[key], em = (int)cellStartM[key + 1];
+            const int ap = (int)cellStartP[key], ep = (int)cellStartP[key + 1];
+            // a non-empty cell outside the tile, or clipped by its capacity
+            if ((em > am && (r < 0 || am - H.RM.base[r] + (em - am) > H.RM.len[r])) ||
+                (ep > ap && (r < 0 || ap - H.RP.base[r] + (ep - ap) > H.RP.len[r]))) {
+                miss = true;
+                return;
+            }
+            for (int j = am; j < em; j++) {
+                const int o = H.RM.off[r] + (j - H.RM.base[r]);
+                if (j == i || !sok[o]) continue;
+                float4 t4 = spos[o];
+                sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+                if (outside_cube(delta, lim)) continue;
+                if (sc_norm3(delta) <= cm.get(prad, t4.w)) {
+                    if (c < climit) list[sc_list16_at(SC_LIST_M, i, c)] = (uint16_t)o;
+                    c++;
+                }
+            }
+            for (int j = ap; j < ep; j++) {
+                const int o = H.RP.off[r] + (j - H.RP.base[r]);
+                if (!sok[o]) continue;
+                float4 t4 = spos[o];
+                sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+                if (outside_cube(delta, lim)) continue;
+                if (sc_norm3(delta) <= cp.get(prad, t4.w)) {
+                    if (c < climit) list[sc_list16_at(SC_LIST_M, i, c)] = (uint16_t)o;
+                    c++;
+                }
+            }
+        });
+        if (miss || c > climit) {
+            cnt[i] = INT_MAX;
+            ovf[atomicAdd(ovfCount, 1)] = i;
+        } else {
+            cnt[i] = c;
+        }
+    }
+}
+
+// relaxMetabolicParticles on tiles: the block bulk-copies the positions and
+// velocities of its tile, then walks each item's list in shared memory.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_tile(ScParams P, RelaxMArgs A,
+                                                                 const uint16_t *__restrict__ list,
+                                                                 int *__restrict__ errorFlag) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    TileMHeader &H = *reinterpret_cast<TileMHeader *>(smraw);
+    const int capM = P.tileCapM, cap = P.tileCapM + P.tileCapP;
+    float4 *spos = reinterpret_cast<float4 *>(smraw + SC_TILE_HDR_BYTES);
+    float4 *svel = spos + cap;
+    // after an expired wait anywhere, the remaining blocks do nothing
+    if (*(volatile int *)errorFlag == SC_DERR_TILE_TIMEOUT) return;
+    TileGeom G;
+    G.init(P, blockIdx.x);
+    if (threadIdx.x == 0) mbar_init(&H.bar);
+    tile_m_setup(P, G, A.cellStartM, A.cellStartP, H);
+    if (threadIdx.x < 32) {  // warp 0 issues the bulk copies, a lane per range
+        const int lane = threadIdx.x;
+        uint32_t bytes = 0;
+        for (int r = lane; r < SC_TILE_NRANGE; r += 32)
+            bytes += 32u * (uint32_t)(max(H.RM.len[r], 0) + max(H.RP.len[r], 0));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+        if (lane == 0) mbar_expect_tx(&H.bar, bytes);
+        __syncwarp();
+        for (int r = lane; r < SC_TILE_NRANGE; r += 32) {
+            if (H.RM.len[r] > 0) {
+                const uint32_t nb = (uint32_t)H.RM.len[r] * 16u;
+                bulk_copy(spos + H.RM.off[r], A.mpos + H.RM.base[r], nb, &H.bar);
+                bulk_copy(svel + H.RM.off[r], A.mvelIn + H.RM.base[r], nb, &H.bar);
+            }
+            if (H.RP.len[r] > 0) {
+                const uint32_t nb = (uint32_t)H.RP.len[r] * 16u;
+                bulk_copy(spos + H.RP.off[r], A.ppos + H.RP.base[r], nb, &H.bar);
+                bulk_copy(svel + H.RP.off[r], A.pvel + H.RP.base[r], nb, &H.bar);
+            }
+        }
+    }
+    // the thread's first item is loaded while the tile is in flight
+    const int climit = min(SC_LIST_M, P.listLimit);
+    int t = threadIdx.x;
+    int i = t < H.nItems ? tile_item(H, t) : -1;
+    int4 in = i >= 0 ? A.minfo[i] : make_int4(0, 0, 0, 0);
+    int c = i >= 0 ? A.L.cnt[i] : 0;
+    float4 v4 = i >= 0 ? A.mvelIn[i] : make_float4(0, 0, 0, 0);
+    float4 p4 = i >= 0 ? A.mpos[i] : make_float4(0, 0, 0, 0);
+    if (!mbar_wait_bounded(&H.bar, 1ll << 31)) {
+        if (threadIdx.x == 0) atomicCAS(errorFlag, 0, SC_DERR_TILE_TIMEOUT);
+        mbar_wait_bounded(&H.bar, 1ll << 31);   // let the copies in flight land before the block exits
+        return;
+    }
+    for (; t < H.nItems; t += blockDim.x) {
+        if (t != (int)threadIdx.x) {
+            i = tile_item(H, t);
+            in = A.minfo[i];
+            c = A.L.cnt[i];
+            v4 = A.mvelIn[i];
+            p4 = A.mpos[i];
+        }
+        if (!(in.z & SC_ACTIVE)) {
+            A.mvelOut[i] = v4;
+            continue;
+        }
+        if (c > climit) continue;
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
+        const float prad = p4.w;
+        const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+        const sc_f3 ppv = pp + pv;
+        sc_f3 dV = sc_zero3();
+        float w = 0.0f;
+        CollisionDistCache cm, cp;
+        // 8 entries per load; the next chunk is loaded while this one is walked
+        const uint4 *__restrict__ chunks = reinterpret_cast<const uint4 *>(list) +
+                                           (size_t)(i >> 5) * (SC_LIST_M / 8) * 32 + (i & 31);
+        uint4 cur = c > 0 ? chunks[0] : make_uint4(0, 0, 0, 0);
+        for (int q = 0; 8 * q < c; q++) {
+            const uint4 nxt = 8 * (q + 1) < c ? chunks[(size_t)(q + 1) * 32] : make_uint4(0, 0, 0, 0);
+            const uint32_t words[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+            for (int kk = 0; kk < 8; kk++) {
+                if (8 * q + kk >= c) break;
+                const uint32_t e = (words[kk >> 1] >> (16 * (kk & 1))) & 0xffffu;
+                const float4 t4 = spos[e], tv = svel[e];
+                const bool fromP = (int)e >= capM;
+                const float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
+                metab_pair(IM, pp, ppv, t4, tv, cd, fromP, dV, w);
+            }
+            cur = nxt;
+        }
+        st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+    }
+}
+
+// Velocities of the slots past the binned items (inactive since the sort).
+__global__ void __launch_bounds__(SC_THREADS) k_copy_tail(const uint32_t *__restrict__ binnedEnd,
+                                                          const int *__restrict__ nActivePtr,
+                                                          const float4 *__restrict__ in, float4 *__restrict__ out) {
+    const int n = *nActivePtr;
+    for (int i = (int)*binnedEnd + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = in[i];
 }
 
 // ---- metabolites.cuh:266-350 relaxMetabolicParticlePartners ----------------
@@ -791,9 +1059,20 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     };
     const int c = L.cnt[g];
     if (c <= min(SC_LIST_LM, P.listLimit)) {
-        for (int k = 0; k < c; k++) {
-            int j = (int)L.list[sc_list_at(SC_LIST_LM, g, k)];
-            body(j, mpos[j]);
+        // four entries per list load, their positions gathered together
+        const uint4 *__restrict__ chunks = sc_list4_chunks(L.list, SC_LIST_LM, g);
+        for (int k0 = 0; k0 < c; k0 += 4) {
+            const uint4 E = chunks[(size_t)(k0 / 4) * 32];
+            const int e[4] = {(int)E.x, (int)E.y, (int)E.z, (int)E.w};
+            float4 t4[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+                if (k0 + kk < c) t4[kk] = mpos[e[kk]];
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                if (k0 + kk >= c) break;
+                body(e[kk], t4[kk]);
+            }
         }
     } else {
         const float lim = P.maxInt;
@@ -1243,22 +1522,26 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
     };
     const int c = L.cnt[g];
     if (c <= min(SC_LIST_D, P.listLimit)) {
-        // the next neighbour's amounts are loaded while the current ones are applied
-        float4 cur[Q], nxt[Q];
-        if (c > 0) {
-            const int j0 = (int)L.list[sc_list_at(SC_LIST_D, g, 0)];
+        // four entries per list load; their amounts are gathered together and
+        // the next chunk of the list is loaded while this one is applied
+        const uint4 *__restrict__ chunks = sc_list4_chunks(L.list, SC_LIST_D, g);
+        uint4 E = c > 0 ? chunks[0] : make_uint4(0, 0, 0, 0);
+        for (int k0 = 0; k0 < c; k0 += 4) {
+            const uint4 En = k0 + 4 < c ? chunks[(size_t)(k0 / 4 + 1) * 32] : make_uint4(0, 0, 0, 0);
+            const int e[4] = {(int)E.x, (int)E.y, (int)E.z, (int)E.w};
+            float4 v[4][Q];
 #pragma unroll
-            for (int q = 0; q < Q; q++) cur[q] = metIn[(size_t)j0 * Q + q];
-        }
-        for (int k = 1; k <= c; k++) {
-            if (k < c) {
-                const int jn = (int)L.list[sc_list_at(SC_LIST_D, g, k)];
+            for (int kk = 0; kk < 4; kk++)
+                if (k0 + kk < c) {
 #pragma unroll
-                for (int q = 0; q < Q; q++) nxt[q] = metIn[(size_t)jn * Q + q];
+                    for (int q = 0; q < Q; q++) v[kk][q] = metIn[(size_t)e[kk] * Q + q];
+                }
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                if (k0 + kk >= c) break;
+                apply(v[kk]);
             }
-            apply(cur);
-#pragma unroll
-            for (int q = 0; q < Q; q++) cur[q] = nxt[q];
+            E = En;
         }
     } else {
         float4 p4 = pos[i];
@@ -1445,18 +1728,33 @@ void sc_phase_relax(ScLaunchCtx &c) {
     (*c.launches)++;
 }
 
+// Largest dynamic shared memory of the tile kernels; called once per device.
+void sc_tile_init() {
+    const int most = 227 * 1024;
+    cudaFuncSetAttribute(k_build_m_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    cudaFuncSetAttribute(k_relax_metab_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+}
+size_t sc_tile_bytes(int capM, int capP, int perSlot) { return SC_TILE_HDR_BYTES + (size_t)(capM + capP) * perSlot; }
+
 void sc_phase_relax_metab(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.Nm <= 0) return;
     MFields M = B.M(), X = B.Mnext();
     PFields F = B.P();
+    const bool tiles = c.P.tileCapM > 0;
     if (!B.validM) {
         // the diffusion list's buffer is the build scratch (that list is rebuilt after the next move anyway)
         B.validD = false;
         cudaMemsetAsync(&B.ctr->ovfM, 0, sizeof(int), c.st);
-        k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos,
-                                                             M.info, F.pos, F.info, B.listM, B.listD, B.cntM, B.permM,
-                                                             c.P.Nm, B.ovfM, &B.ctr->ovfM);
+        if (tiles) {
+            k_build_m_tile<<<tile_blocks(c.P), SC_THREADS, sc_tile_bytes(c.P.tileCapM, c.P.tileCapP, 17), c.st>>>(
+                c.P, B.cellStartM, B.cellStartP, M.pos, M.info, F.pos, F.info, reinterpret_cast<uint16_t *>(B.listM),
+                B.cntM, B.ovfM, &B.ctr->ovfM);
+        } else {
+            k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM,
+                                                                 M.pos, M.info, F.pos, F.info, B.listM, B.listD, B.cntM,
+                                                                 B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
+        }
         (*c.launches)++;
         B.validM = true;
     }
@@ -1464,13 +1762,22 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     L.list = B.listM;
     L.cnt = B.cntM;
     L.cap = c.P.Nm;
-    L.perm = B.permM;
+    L.perm = tiles ? nullptr : B.permM;
     RelaxMArgs A{B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, L, M.vel, X.vel, F.pos, F.info, F.vel};
-    k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+    if (tiles) {
+        k_relax_metab_tile<<<tile_blocks(c.P), SC_THREADS, sc_tile_bytes(c.P.tileCapM, c.P.tileCapP, 32), c.st>>>(
+            c.P, A, reinterpret_cast<const uint16_t *>(B.listM), &B.ctr->error);
+        k_copy_tail<<<std::max(1, c.gridCap / 8), SC_THREADS, 0, c.st>>>(
+            B.cellStartM + c.P.cells, &B.ctr->nActiveM, M.vel, X.vel);
+        (*c.launches) += 2;
+    } else {
+        k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+        (*c.launches)++;
+    }
     k_relax_metab_overflow<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,
                                                                                              &B.ctr->ovfM);
     B.cm[FM_VEL] ^= 1;
-    (*c.launches) += 2;
+    (*c.launches)++;
 }
 
 void sc_phase_relax_partners(ScLaunchCtx &c) {

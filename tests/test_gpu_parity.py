@@ -77,9 +77,11 @@ def test_whole_steps(product, species, periodic):
     assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
 
 
-@pytest.mark.parametrize("periodic", [1, 0])
-def test_measured_workload_small(product, periodic):
-    """The measured workload's physics at a reduced size (same density)."""
+@pytest.mark.parametrize("periodic,tiles", [(1, "1"), (0, "1"), (1, "0"), (0, "0")])
+def test_measured_workload_small(product, monkeypatch, periodic, tiles):
+    """The measured workload's physics at a reduced size (same density), with
+    the metabolic sweeps on shared-memory tiles and on per-item lists."""
+    monkeypatch.setenv("SC_TILES", tiles)
     cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
                                  seed=3, periodic=periodic)
     rng = np.random.default_rng(3)
@@ -110,12 +112,13 @@ def test_deterministic(product):
     assert runs[0][1].tobytes() == runs[1][1].tobytes()
 
 
-@pytest.mark.parametrize("limit,periodic", [("0", 0), ("2", 0), ("2", 1)])
-def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic):
+@pytest.mark.parametrize("limit,periodic,tiles", [("0", 0, "1"), ("2", 0, "1"), ("2", 1, "1"), ("2", 1, "0")])
+def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic, tiles):
     """Items whose pair list overflows are handled by scanning their
     neighbourhood; with the list capacity capped, both paths run side by side
     and must still match the oracle bit for bit."""
     monkeypatch.setenv("SC_PAIR_LIST_LIMIT", limit)
+    monkeypatch.setenv("SC_TILES", tiles)
     cfg, gpu, cpu = _engines(product, scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic))
     for e in (gpu, cpu):
         e.prepare()
