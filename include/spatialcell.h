@@ -319,6 +319,17 @@ int sc_frame_wait(sc_sim *sim, int64_t ticket);
 int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info, int32_t n, uint32_t *perm,
                          uint32_t *cell_start, void *stream);
 
+/* ---- checkpoint / resume (no counterpart in the reference) ----
+ * A checkpoint holds the whole state -- the active particle and metabolic
+ * records in the reference's layouts, the step counter and the next particle
+ * id -- after a 24-byte header: "SCCKPT01", then the particle and metabolic
+ * record counts, the step and the next particle id as int32.  Reading it into a sim created with the same configuration and
+ * tables and calling sc_step continues the run bit for bit: noise is keyed by
+ * (seed, particle id, step) and every pair list is rebuilt.  `file` is a
+ * FILE* open for binary writing / reading. */
+int sc_checkpoint_write(sc_sim *sim, void *file);
+int sc_checkpoint_read(sc_sim *sim, void *file);
+
 /* ---- frames.dat (storage.cuh:9-44) ---- */
 int sc_frames_write_header(void *file /* FILE* */, const sc_config *cfg);
 int sc_frames_write_frame(void *file /* FILE* */, const sc_config *cfg,

@@ -707,6 +707,43 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
     return SC_OK;
 }
 
+int sc_checkpoint_write(sc_sim *s, void *file) {
+    if (!s || !file) return set_err(s, SC_E_INVALID, "null argument");
+    sc_counters c;
+    int rc = sc_get_counters(s, &c);
+    if (rc) return rc;
+    std::vector<sc_particle> p((size_t)std::max(s->P.N, 1));
+    std::vector<sc_metabolic_particle> m((size_t)std::max(s->P.Nm, 1));
+    if ((rc = sc_export_state(s, p.data(), m.data()))) return rc;
+    FILE *f = (FILE *)file;
+    const int32_t hdr[6] = {0, 0, c.n_active_particles, c.n_active_metabolic_particles, c.step, c.next_particle_id};
+    char magic[8] = {'S', 'C', 'C', 'K', 'P', 'T', '0', '1'};
+    if (fwrite(magic, 1, 8, f) != 8 || fwrite(hdr + 2, sizeof(int32_t), 4, f) != 4 ||
+        fwrite(p.data(), sizeof(sc_particle), (size_t)c.n_active_particles, f) != (size_t)c.n_active_particles ||
+        fwrite(m.data(), sizeof(sc_metabolic_particle), (size_t)c.n_active_metabolic_particles, f) !=
+            (size_t)c.n_active_metabolic_particles)
+        return set_err(s, SC_E_IO, "checkpoint write failed");
+    return SC_OK;
+}
+
+int sc_checkpoint_read(sc_sim *s, void *file) {
+    if (!s || !file) return set_err(s, SC_E_INVALID, "null argument");
+    FILE *f = (FILE *)file;
+    char magic[8];
+    int32_t hdr[4];
+    if (fread(magic, 1, 8, f) != 8 || memcmp(magic, "SCCKPT01", 8) != 0 || fread(hdr, sizeof(int32_t), 4, f) != 4)
+        return set_err(s, SC_E_IO, "not a checkpoint");
+    const int32_t n = hdr[0], nm = hdr[1];
+    if (n < 0 || nm < 0 || n > s->P.N || nm > s->P.Nm)
+        return set_err(s, SC_E_INVALID, "checkpoint holds more items than the sim's capacity");
+    std::vector<sc_particle> p((size_t)std::max(n, 1));
+    std::vector<sc_metabolic_particle> m((size_t)std::max(nm, 1));
+    if (fread(p.data(), sizeof(sc_particle), (size_t)n, f) != (size_t)n ||
+        fread(m.data(), sizeof(sc_metabolic_particle), (size_t)nm, f) != (size_t)nm)
+        return set_err(s, SC_E_IO, "truncated checkpoint");
+    return sc_load_state(s, p.data(), n, m.data(), nm, hdr[2], hdr[3]);
+}
+
 int64_t sc_reduce_frame_async(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);

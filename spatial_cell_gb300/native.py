@@ -39,6 +39,8 @@ _SIGS = {
     "sc_reduce_frame_async": (ctypes.c_int64, [_P, _P, _P]),
     "sc_frame_wait": (ctypes.c_int, [_P, ctypes.c_int64]),
     "sc_get_stream": (ctypes.c_void_p, [_P]),
+    "sc_checkpoint_write": (ctypes.c_int, [_P, _P]),
+    "sc_checkpoint_read": (ctypes.c_int, [_P, _P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
     "sc_frames_write_frame": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config), _P, _P]),
     "sc_sort_cells_static": (ctypes.c_int, [ctypes.POINTER(abi.Config), _P, _P, ctypes.c_int32, _P, _P, _P]),
@@ -65,6 +67,25 @@ def lib():
 
 class ScError(RuntimeError):
     pass
+
+
+class _cfile:
+    """A C FILE* for the ABI's file functions."""
+
+    def __init__(self, path, mode):
+        self.libc = ctypes.CDLL(None)
+        self.libc.fopen.restype = ctypes.c_void_p
+        self.libc.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        self.libc.fclose.argtypes = [ctypes.c_void_p]
+        self.f = self.libc.fopen(str(path).encode(), mode)
+        if not self.f:
+            raise OSError(f"cannot open {path}")
+
+    def __enter__(self):
+        return ctypes.c_void_p(self.f)
+
+    def __exit__(self, *a):
+        self.libc.fclose(self.f)
 
 
 def _check(rc, sim=None, what=""):
@@ -193,3 +214,13 @@ class Simulation:
 
     def frame_wait(self, ticket):
         _check(self.L.sc_frame_wait(self.h, ticket), self.h, "sc_frame_wait")
+
+    def checkpoint(self, path):
+        """Writes the whole state to `path` (sc_checkpoint_write)."""
+        with _cfile(path, b"wb") as f:
+            _check(self.L.sc_checkpoint_write(self.h, f), self.h, "sc_checkpoint_write")
+
+    def resume(self, path):
+        """Loads a checkpoint; the next step continues the saved run."""
+        with _cfile(path, b"rb") as f:
+            _check(self.L.sc_checkpoint_read(self.h, f), self.h, "sc_checkpoint_read")

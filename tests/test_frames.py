@@ -43,3 +43,27 @@ def test_streamed_frames_equal_synchronous_frames(product):
     assert rp0.tobytes() == rp.tobytes() and rm0.tobytes() == rm.tobytes()
     for s in sims:
         s.close()
+
+
+def test_checkpoint_resume_continues_bit_for_bit(product, tmp_path):
+    """Four steps straight == two steps, checkpoint, a new sim resumes, two
+    more steps (same bytes of the whole state and the same counters)."""
+    scene = scenes.test_scene(23, n=900, nm=1800, box=42.0, periodic=1)
+    cfg, types, rules, p, m, nid = scene
+    a = product.Simulation(cfg, types, rules)
+    a.load_state(p, m, next_particle_id=nid)
+    a.prepare()
+    a.step(2)
+    a.checkpoint(tmp_path / "ck.bin")
+    a.step(2)
+    b = product.Simulation(cfg, types, rules)
+    b.resume(tmp_path / "ck.bin")
+    b.step(2)
+    sa, sb = a.export_state(), b.export_state()
+    assert sa[0].tobytes() == sb[0].tobytes()
+    assert sa[1].tobytes() == sb[1].tobytes()
+    ca, cb = a.counters(), b.counters()
+    assert (ca.n_active_particles, ca.next_particle_id, ca.step) == (cb.n_active_particles, cb.next_particle_id,
+                                                                      cb.step)
+    a.close()
+    b.close()
