@@ -514,6 +514,185 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
     if (dbgTouched) st4(A.dbg, i, pdbg);
 }
 
+// A bonded particle's relaxation (work class 0, list path).  The pose terms
+// of its rule and chain bonds do not depend on the running sums, so they are
+// evaluated first, bond by bond in the order the reference meets them, with
+// every lane of a warp on its own first bond, then its second ...; the list
+// is then walked once more to add every term in the reference's order (the
+// slerps of dAV and the float sums are order-dependent).  A test bond rotates
+// the particle itself, which later terms read: such particles take the
+// in-order path.
+struct BondTerm {
+    sc_f3 dv;   // velocity term
+    sc_f4 q;    // dAV slerp target
+    float t;    // dAV slerp weight
+    sc_f3 dbg;  // chain bonds: rrp - ppos for the debug vector
+};
+
+__device__ __forceinline__ void relax_bonded_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4,
+                                                  float4 r4, float4 a4) {
+    const int nbi = min(max(A.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    const int *__restrict__ myBonds = A.bonds + (size_t)i * 24;
+    for (int k = 0; k < nbi; k++)
+        if (myBonds[3 * k] == 0) {
+            relax_item<false, 0>(P, A, i, in, v4, r4, a4);
+            return;
+        }
+    float4 p4 = A.pos[i];
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, ppos, SC_BINNED_P);
+    const float prad = p4.w;
+    const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
+    const sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
+    sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
+    const int pid = in.x, ptype = in.y;
+    const sc_f3 up = sc_rotate(sc_up(), prot);
+    const sc_f3 nextUp = sc_rotate(up, pav);
+    const float flex = SC_PI_REF / 8;
+    const int c = A.L.cnt[i];
+    // 1. the partner entries of the list
+    int pj[SC_MAX_ACTIVE_INTERACTIONS];
+    int np = 0;
+    for (int k = 0; k < c; k++) {
+        const uint32_t e = A.L.list[sc_list_at(SC_LIST_PP, i, k)];
+        if ((e & SC_PP_PARTNER) && np < SC_MAX_ACTIVE_INTERACTIONS) pj[np++] = (int)(e & SC_PP_INDEX);
+    }
+    // 2. their bonds' terms, in list order, then bond-slot order
+    BondTerm T[SC_MAX_ACTIVE_INTERACTIONS];
+    int nt = 0;
+    for (int q = 0; q < np; q++) {
+        const int j = pj[q];
+        const int4 tin = A.info[j];
+        const int tid_ = tin.x, ttype = tin.y;
+        const float4 t4 = A.pos[j];
+        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+        const float trad = t4.w, idist = prad + trad;
+        const sc_f4 trot = ld4(A.rotIn, j), tav = ld4(A.avIn, j);
+        const sc_f3 tvel = ld3(A.velIn, j);
+#pragma unroll 1
+        for (int k = 0; k < nbi; k++) {
+            if (myBonds[3 * k + 2] != tid_) continue;
+            const int it = myBonds[3 * k];
+            if (it >= 10 && nt < SC_MAX_ACTIVE_INTERACTIONS) {
+                // dynamics.cuh:591-655
+                const sc_rule &pii = rule_at(P, it);
+                sc_f4 ro = rule_ori(pii);
+                sc_f3 rp = rule_pos(pii);
+                bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
+                sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
+                sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
+                sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
+                sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
+                BondTerm &b = T[nt++];
+                b.q = sc_qmul(sc_slerp(rro, orro, 0.5f), rro);
+                b.t = 0.9f * trad / (prad + trad);
+                sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot)))
+                               : sc_rotate(rp, sc_qmul(tav, trot));
+                rrp += tpos;
+                sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot)))
+                                : sc_rotate(rp, sc_qmul(pav, prot));
+                orrp += ppos;
+                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+            } else if (it == SC_INTERACTION_TYPE_CHAIN && nt < SC_MAX_ACTIVE_INTERACTIONS) {
+                // dynamics.cuh:692-769
+                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), trot), pav);
+                sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
+                bool fwd = myBonds[3 * k + 1] == SC_INTERACTION_GROUP_FORWARD;
+                BondTerm &b = T[nt++];
+                b.q = sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd);
+                b.t = 0.9f * trad / (prad + trad);
+                sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
+                sc_f3 axis = sc_safe_cross(relUp, -nnd);
+                float ang = sc_angle3(relUp, -nnd);
+                sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
+                rrp *= idist;
+                rrp += tpos;
+                sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
+                sc_f3 oaxis = sc_safe_cross(oUp, nnd);
+                float oang = sc_angle3(oUp, nnd);
+                sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
+                orrp *= idist;
+                orrp += ppos;
+                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+                b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+                b.dbg = rrp - ppos;
+            }
+        }
+    }
+    // 3. every term in the reference's order
+    sc_f4 pdbg = sc_make_f4(0, 0, 0, 0);
+    bool dbgTouched = false;
+    sc_f3 dV = sc_zero3();
+    sc_f4 dAV = sc_qid();
+    sc_f3 phobPos = sc_zero3();
+    float phobSum = 0.0f;
+    float w = 0.0f;
+    int ut = 0;
+    for (int kk = 0; kk < c; kk++) {
+        const uint32_t fl = A.L.list[sc_list_at(SC_LIST_PP, i, kk)];
+        const int j = (int)(fl & SC_PP_INDEX);
+        float4 t4 = A.pos[j];
+        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+        const float trad = t4.w;
+        if (fl & SC_PP_POLAR) {
+            sc_f3 tvel = ld3(A.velIn, j);
+            sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), ld4(A.rotIn, j)), pav);
+            sc_f3 pPV = -nextUp * prad + ppos + pvel;
+            sc_f3 tpPV = -nextTup * trad + tpos + tvel;
+            float Lr = length(tpPV - pPV) / (prad + trad);
+            float attr = sc_polar_attr(Lr);
+            w += 1.0f;
+            dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
+            float pap = sc_powf(fminf(1.0f / fmaxf(Lr, 1e-6f), 10.0f) / 10.0f, 0.2f);
+            phobSum += pap;
+            phobPos += tpPV * pap;
+        }
+        if (fl & SC_PP_PARTNER) {
+            const int tid_ = A.info[j].x;
+#pragma unroll 1
+            for (int k = 0; k < nbi; k++) {
+                if (myBonds[3 * k + 2] != tid_) continue;
+                const int it = myBonds[3 * k];
+                if ((it >= 10 || it == SC_INTERACTION_TYPE_CHAIN) && ut < nt) {
+                    const BondTerm &b = T[ut++];
+                    if (it == SC_INTERACTION_TYPE_CHAIN && !dbgTouched) {
+                        pdbg = ld4(A.dbg, i);
+                        dbgTouched = true;
+                    }
+                    dAV = sc_slerp(dAV, b.q, b.t);
+                    w += 1.0f;
+                    dV += b.dv;
+                    if (it == SC_INTERACTION_TYPE_CHAIN) {
+                        pdbg.x = (float)((double)pdbg.x + (double)b.dbg.x * (1.0 - (double)0.9f));
+                        pdbg.y = (float)((double)pdbg.y + (double)b.dbg.y * (1.0 - (double)0.9f));
+                        pdbg.z = (float)((double)pdbg.z + (double)b.dbg.z * (1.0 - (double)0.9f));
+                    }
+                }
+            }
+        }
+        if (fl & SC_PP_COLLIDE) {
+            sc_f3 nd = normalize(tpos - ppos);
+            float cd = prad + trad;
+            sc_f3 tvel = ld3(A.velIn, j);
+            w += 1.0f;
+            dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+        }
+    }
+    sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
+    pav = sc_qmul(sc_slerp(sc_qid(), dAV, 1.0f / fmaxf(w, 1.0f)), pav);
+    if (phobSum > 0.0f) {
+        sc_f3 dir = normalize(phobPos / phobSum - (ppos + nv));
+        pav = sc_slerp(pav, sc_quat_from_to(-up, dir), 0.2f);
+    }
+    st3(A.velOut, i, nv, v4.w);
+    st4(A.rotOut, i, prot);
+    st4(A.avOut, i, pav);
+    if (dbgTouched) st4(A.dbg, i, pdbg);
+}
+
 // The items of one work class whose list fits (the others are left to
 // k_relax_overflow), grid-stride over the class's index segment.
 template <int MODE>
@@ -531,7 +710,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
             continue;
         }
         if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) continue;
-        relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
+        if (MODE == 0)
+            relax_bonded_item(P, A, i, in, v4, r4, a4);
+        else
+            relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
     }
 }
 
