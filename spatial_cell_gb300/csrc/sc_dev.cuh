@@ -182,23 +182,54 @@ __device__ __forceinline__ uint32_t cell_key(const ScParams &P, uint32_t gx, uin
 // are consecutive, so with the exclusive cell-start table (cellStart[c] =
 // first sorted slot with key >= c) that run of cells is one slot range, and
 // the visiting order is exactly the reference's.
+// Offsets (-1..1 per axis) of the neighbour cells a scan visits.  All 27 by
+// default; reach() drops a neighbour layer when no item in it can pass the
+// interaction cube |delta| <= lim on that axis, which every caller tests
+// before anything else, so the visits that remain are the reference's, in its
+// order, and the results are unchanged.  The bound needs the neighbours to
+// sit in the cells they were sorted into (P.binned covers `need`), lim at
+// most the cell size, and a periodic box of at least 5 cells (no nearest image
+// crosses back into the cube).  Candidates of cell c - 1 lie below c * cell
+// and those of cell c + 1 at or above (c + 1) * cell (or at the box size
+// past the top periodic cell), up to the rounding of the cell index; the
+// margin covers that and the rounding of delta.
+struct Reach {
+    int xl = -1, xh = 1, yl = -1, yh = 1, zl = -1, zh = 1;
+};
+__device__ __forceinline__ void reach_axis(const ScParams &P, float p, int c, int n, float lim, int &lo, int &hi) {
+    const float m = lim + 1e-3f + 4e-6f * (fabsf(p) + P.cell * (float)(c + 1));
+    lo = (p - (float)c * P.cell > m) ? 0 : -1;
+    const float upper = (P.periodic && c == n - 1) ? P.simSize : (float)(c + 1) * P.cell;
+    hi = (upper - p > m) ? 0 : 1;
+}
+__device__ __forceinline__ Reach reach(const ScParams &P, sc_f3 pos, float lim, int need) {
+    Reach r;
+    if ((P.binned & need) != need || !(lim <= P.cell) || (P.periodic && !(P.simSize >= 5.0f * P.cell))) return r;
+    const int n = cell_limit(P);
+    reach_axis(P, pos.x, (int)sc_grid_idx(pos.x, P.cell, n), n, lim, r.xl, r.xh);
+    reach_axis(P, pos.y, (int)sc_grid_idx(pos.y, P.cell, n), n, lim, r.yl, r.yh);
+    reach_axis(P, pos.z, (int)sc_grid_idx(pos.z, P.cell, n), n, lim, r.zl, r.zh);
+    return r;
+}
+
 template <class F>
-__device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__restrict__ cellStart, sc_f3 pos, F &&f) {
+__device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__restrict__ cellStart, sc_f3 pos,
+                                       const Reach &R, F &&f) {
     int n = cell_limit(P);
     int cx = (int)sc_grid_idx(pos.x, P.cell, n), cy = (int)sc_grid_idx(pos.y, P.cell, n),
         cz = (int)sc_grid_idx(pos.z, P.cell, n);
     if (P.periodic) {
-        // offsets -1, 0, +1 per axis, wrapped; the z run of a column is one
-        // slot range unless it wraps
-        for (int ox = -1; ox <= 1; ox++) {
-            for (int oy = -1; oy <= 1; oy++) {
+        // the z run of a column is one slot range unless it wraps
+        for (int ox = R.xl; ox <= R.xh; ox++) {
+            for (int oy = R.yl; oy <= R.yh; oy++) {
                 uint32_t base = cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n), 0);
-                if (cz >= 1 && cz <= n - 2) {
-                    for (uint32_t j = cellStart[base | (uint32_t)(cz - 1)], e = cellStart[(base | (uint32_t)(cz + 1)) + 1];
+                if (cz + R.zl >= 0 && cz + R.zh <= n - 1) {
+                    for (uint32_t j = cellStart[base | (uint32_t)(cz + R.zl)],
+                                  e = cellStart[(base | (uint32_t)(cz + R.zh)) + 1];
                          j < e; j++)
                         f((int)j);
                 } else {
-                    for (int oz = -1; oz <= 1; oz++) {
+                    for (int oz = R.zl; oz <= R.zh; oz++) {
                         uint32_t key = base | (uint32_t)((cz + oz + n) % n);
                         for (uint32_t j = cellStart[key], e = cellStart[key + 1]; j < e; j++) f((int)j);
                     }
@@ -207,9 +238,9 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
         }
         return;
     }
-    int x0 = max(cx - 1, 0), x1 = min(cx + 1, n - 1);
-    int y0 = max(cy - 1, 0), y1 = min(cy + 1, n - 1);
-    uint32_t z0 = (uint32_t)max(cz - 1, 0), z1 = (uint32_t)min(cz + 1, n - 1);
+    int x0 = max(cx + R.xl, 0), x1 = min(cx + R.xh, n - 1);
+    int y0 = max(cy + R.yl, 0), y1 = min(cy + R.yh, n - 1);
+    uint32_t z0 = (uint32_t)max(cz + R.zl, 0), z1 = (uint32_t)min(cz + R.zh, n - 1);
     for (int gx = x0; gx <= x1; gx++) {
         for (int gy = y0; gy <= y1; gy++) {
             uint32_t base = cell_key(P, (uint32_t)gx, (uint32_t)gy, 0);
@@ -218,26 +249,34 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
         }
     }
 }
+template <class F>
+__device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__restrict__ cellStart, sc_f3 pos, F &&f) {
+    scan27(P, cellStart, pos, Reach(), f);
+}
 
 // Same neighbourhood, one cell at a time (for kernels that interleave two
 // arrays cell by cell, metabolites.cuh:174-248).
 template <class F>
-__device__ __forceinline__ void cells27(const ScParams &P, sc_f3 pos, F &&f) {
+__device__ __forceinline__ void cells27(const ScParams &P, sc_f3 pos, const Reach &R, F &&f) {
     int n = cell_limit(P);
     int cx = (int)sc_grid_idx(pos.x, P.cell, n), cy = (int)sc_grid_idx(pos.y, P.cell, n),
         cz = (int)sc_grid_idx(pos.z, P.cell, n);
     if (P.periodic) {
-        for (int ox = -1; ox <= 1; ox++)
-            for (int oy = -1; oy <= 1; oy++)
-                for (int oz = -1; oz <= 1; oz++)
+        for (int ox = R.xl; ox <= R.xh; ox++)
+            for (int oy = R.yl; oy <= R.yh; oy++)
+                for (int oz = R.zl; oz <= R.zh; oz++)
                     f(cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n),
                                (uint32_t)((cz + oz + n) % n)));
         return;
     }
-    for (int gx = max(cx - 1, 0); gx <= min(cx + 1, n - 1); gx++)
-        for (int gy = max(cy - 1, 0); gy <= min(cy + 1, n - 1); gy++)
-            for (int gz = max(cz - 1, 0); gz <= min(cz + 1, n - 1); gz++)
+    for (int gx = max(cx + R.xl, 0); gx <= min(cx + R.xh, n - 1); gx++)
+        for (int gy = max(cy + R.yl, 0); gy <= min(cy + R.yh, n - 1); gy++)
+            for (int gz = max(cz + R.zl, 0); gz <= min(cz + R.zh, n - 1); gz++)
                 f(cell_key(P, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz));
+}
+template <class F>
+__device__ __forceinline__ void cells27(const ScParams &P, sc_f3 pos, F &&f) {
+    cells27(P, pos, Reach(), f);
 }
 
 __device__ __forceinline__ void set_error(ScCounters *c, int code) { atomicCAS(&c->error, 0, code); }

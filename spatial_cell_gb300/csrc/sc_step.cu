@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
         const int phydro = (int)(int8_t)(in.w & 0xff);
         int c = 0;
         uint32_t any = 0;
-        scan27(P, cellStart, ppos, [&](int j) {
+        scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
             uint32_t f = pp_flags(P, IM, i, j, ppos, p4.w, phydro, B, pos, info);
             if (f) {
                 if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
@@ -270,7 +270,7 @@ __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__rest
         const Imager IM(P, ppos, SC_BINNED_P);
         BondRegs B;
         B.load(nb, bonds, i);
-        scan27(P, cellStart, ppos, [&](int j) {
+        scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
             uint32_t fl = pp_flags(P, IM, i, j, ppos, prad, phydro, B, pos, info);
             if (fl) f(j, fl);
         });
@@ -491,7 +491,7 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
     if (SCAN) {
         BondRegs B;
         B.load(A.nb, A.bonds, i);
-        scan27(P, A.cellStart, ppos, [&](int j) {
+        scan27(P, A.cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
             uint32_t fl = pp_flags(P, IM, i, j, ppos, prad, phydro, B, A.pos, A.info);
             if (fl) body(j, fl);
         });
@@ -757,7 +757,7 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cm, cp;
-    cells27(P, pp, [&](uint32_t key) {
+    cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
         for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i || !(minfo[j].z & SC_ACTIVE)) continue;
             float4 t4 = mpos[j];
@@ -888,7 +888,7 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
     float w = 0.0f;
     CollisionDistCache cm, cp;
     const float lim = P.maxInt;
-    cells27(P, pp, [&](uint32_t key) {
+    cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
         for (uint32_t j = A.cellStartM[key], e = A.cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i) continue;
             if (!(A.minfo[j].z & SC_ACTIVE)) continue;
@@ -1026,7 +1026,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m_tile(ScParams P, const u
         int c = 0;
         bool miss = false;
         const int climit = min(SC_LIST_M, P.listLimit);
-        cells27(P, pp, [&](uint32_t key) {
+        cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
             if (miss) return;
             const int r = G.range_of((int)(key >> (2 * bits)), (int)((key >> bits) & zmask), (int)(key & zmask));
             const int am = (int)cellStartM[key], em = (int)cellStartM[key + 1];
@@ -1183,7 +1183,7 @@ __device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t 
     const Imager IM(P, pp, SC_BINNED_M);
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cc;
-    scan27(P, cellStartM, pp, [&](int j) {
+    scan27(P, cellStartM, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
         if (!(minfo[j].z & SC_ACTIVE)) return;
         float4 t4 = mpos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
@@ -1258,7 +1258,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
         }
     } else {
         const float lim = P.maxInt;
-        scan27(P, cellStartM, pp, [&](int j) {
+        scan27(P, cellStartM, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
             if (!(minfo[j].z & SC_ACTIVE)) return;
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
@@ -1317,7 +1317,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     int *pb = bonds + (size_t)i * 24;
     const int nb0 = pnb;
     const float lim = P.maxInt;
-    scan27(P, cellStart, ppos, [&](int j) {
+    scan27(P, cellStart, ppos, reach(P, ppos, lim, SC_BINNED_P), [&](int j) {
         if (j == i) return;
         int4 tin = info[j];
         if (!(tin.z & SC_ACTIVE)) return;
@@ -1379,7 +1379,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
         int src = -1;
         int tId = 0, tGroup = 0, tSet = 0, tFirst = 0, tSecond = 0, tFs = 0, tSs = 0, tPoly = 0;
         const float lim = P.maxInt;
-        scan27(P, cellStart, ppos, [&](int j) {
+        scan27(P, cellStart, ppos, reach(P, ppos, lim, SC_BINNED_P), [&](int j) {
             if (j == i) return;
             int4 tin = info[j];
             if (!(tin.z & SC_ACTIVE)) return;
@@ -1632,7 +1632,7 @@ __device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
-    scan27(P, cellStart, pp, [&](int j) {
+    scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
         if (j == i || !(info[j].z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
@@ -1730,7 +1730,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
         const Imager IM(P, pp, SC_BINNED_M);
         const float lim = P.maxDiff;
-        scan27(P, cellStart, pp, [&](int j) {
+        scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
             if (j == i) return;
             if (!(info[j].z & SC_ACTIVE)) return;
             float4 t4 = pos[j];
@@ -1764,7 +1764,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
     const float prad = p4.w;
     int flags = in.z;
     const float lim = P.maxInt;
-    scan27(P, cellStartP, pp, [&](int j) {
+    scan27(P, cellStartP, pp, reach(P, pp, lim, SC_BINNED_P), [&](int j) {
         int4 tin = pinfo[j];
         if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) return;
         float4 t4 = ppos_[j];
