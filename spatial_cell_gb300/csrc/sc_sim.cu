@@ -153,6 +153,16 @@ struct sc_sim {
     cudaStream_t copySt = nullptr;          // frame copies to the host
     cudaEvent_t reduced[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
     int64_t frames = 0;                     // frames enqueued by sc_reduce_frame_async
+    // One step as a CUDA graph, per host-side buffer state at the step's start
+    // (which of each field's two buffers is current, sort buffers, list
+    // validity, binning): the graph and the state the step leaves behind.
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<int> after;
+        long long launches = 0;
+    };
+    std::map<std::vector<int>, StepGraph> graphs;
+    bool useGraphs = true;
     int device = 0;
     int gridCap = 0;
     long long launches = 0;
@@ -264,6 +274,29 @@ void binned_after(ScParams &P, int phase) {
     if (phase == SC_PHASE_APPLY_VELOCITIES) P.binned = 0;
 }
 
+// The host-side state a step reads and changes.
+std::vector<int> host_state(const sc_sim *s) {
+    const ScBuffers &B = s->B;
+    std::vector<int> v(B.cp, B.cp + FP_COUNT);
+    v.insert(v.end(), B.cm, B.cm + FM_COUNT);
+    v.insert(v.end(), {B.sortCurP, B.sortCurM, (int)B.validPP, (int)B.validM, (int)B.validLM, (int)B.validD,
+                       s->P.binned});
+    return v;
+}
+void set_host_state(sc_sim *s, const std::vector<int> &v) {
+    ScBuffers &B = s->B;
+    size_t k = 0;
+    for (int f = 0; f < FP_COUNT; f++) B.cp[f] = v[k++];
+    for (int f = 0; f < FM_COUNT; f++) B.cm[f] = v[k++];
+    B.sortCurP = v[k++];
+    B.sortCurM = v[k++];
+    B.validPP = v[k++] != 0;
+    B.validM = v[k++] != 0;
+    B.validLM = v[k++] != 0;
+    B.validD = v[k++] != 0;
+    s->P.binned = v[k++];
+}
+
 int run_phase(sc_sim *s, int phase, int arg) {
     ScLaunchCtx c = ctx(s);
     invalidate_after(s->B, phase);
@@ -293,6 +326,67 @@ int run_phase(sc_sim *s, int phase, int arg) {
         default: return set_err(s, SC_E_INVALID, "unknown phase " + std::to_string(phase));
     }
     return check_launch(s);
+}
+
+// One iteration of the step loop (main.cu:347-661), launched phase by phase.
+int step_direct(sc_sim *s) {
+    const sc_config &c = s->cfg;
+    {
+        run_phase(s, SC_PHASE_SORT_PARTICLES, 0);
+        run_phase(s, SC_PHASE_SORT_METABOLIC, 0);
+        run_phase(s, SC_PHASE_MOVE_BROWNIAN, 0);
+        run_phase(s, SC_PHASE_MOVE_BROWNIAN_METAB, 0);
+        for (int j = 0; j < c.noise_coordination_steps; j++) run_phase(s, SC_PHASE_COORDINATE_NOISE, j);
+        run_phase(s, SC_PHASE_APPLY_NOISE, 0);
+        for (int j = 0; j < c.relaxation_steps; j++) {
+            run_phase(s, SC_PHASE_RELAX, j);
+            if (j % 2 == 0) {
+                run_phase(s, SC_PHASE_RELAX_METAB, j);
+                run_phase(s, SC_PHASE_RELAX_PARTNERS, j);
+            }
+        }
+        run_phase(s, SC_PHASE_APPLY_VELOCITIES, 0);
+        run_phase(s, SC_PHASE_COMPLEXIFY, 0);
+        run_phase(s, SC_PHASE_TRANSITION, 0);
+        run_phase(s, SC_PHASE_POLYMERIZE, 0);
+        for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
+        return run_phase(s, SC_PHASE_END_STEP, 0);
+    }
+}
+
+// The same step as one graph launch: the first step from a given host-side
+// state is captured and instantiated, later ones relaunch it.  A capture that
+// fails turns graphs off for the sim and runs the step directly.
+int step_graph(sc_sim *s) {
+    const std::vector<int> before = host_state(s);
+    auto it = s->graphs.find(before);
+    if (it == s->graphs.end()) {
+        const long long l0 = s->launches;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? step_direct(s) : SC_E_CUDA;
+        cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(s->st, &g) : e;
+        if (rc == SC_OK && e2 == cudaSuccess) e2 = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (rc != SC_OK || e2 != cudaSuccess) {
+            cudaGetLastError();
+            s->useGraphs = false;
+            s->launches = l0;
+            set_host_state(s, before);
+            return step_direct(s);
+        }
+        sc_sim::StepGraph sg;
+        sg.exec = exec;
+        sg.after = host_state(s);
+        sg.launches = s->launches - l0;
+        s->launches = l0;
+        it = s->graphs.emplace(before, std::move(sg)).first;
+    }
+    SC_CK(s, cudaGraphLaunch(it->second.exec, s->st));
+    set_host_state(s, it->second.after);
+    s->launches += it->second.launches;
+    return SC_OK;
 }
 
 int ensure_staging(sc_sim *s, size_t bytes) {
@@ -345,6 +439,8 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     cudaGetDevice(&s->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    // SC_GRAPHS=0 launches every step phase by phase instead of as a CUDA graph
+    if (const char *g = getenv("SC_GRAPHS")) s->useGraphs = atoi(g) != 0;
     sc_tile_init();
     s->gridCap = std::max(1, sms) * (2048 / SC_THREADS);
     ScParams &P = s->P;
@@ -517,6 +613,7 @@ void sc_destroy(sc_sim *s) {
         if (s->reduced[k]) cudaEventDestroy(s->reduced[k]);
         if (s->copied[k]) cudaEventDestroy(s->copied[k]);
     }
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
     for (void *p : s->allocs) cudaFree(p);
     delete s;
 }
@@ -588,31 +685,13 @@ int sc_step(sc_sim *s, int32_t n_steps) {
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
     if (n_steps < 0) return set_err(s, SC_E_INVALID, "negative step count");
     cudaSetDevice(s->device);
-    const sc_config &c = s->cfg;
     for (int k = 0; k < n_steps; k++) {
-        run_phase(s, SC_PHASE_SORT_PARTICLES, 0);
-        run_phase(s, SC_PHASE_SORT_METABOLIC, 0);
-        run_phase(s, SC_PHASE_MOVE_BROWNIAN, 0);
-        run_phase(s, SC_PHASE_MOVE_BROWNIAN_METAB, 0);
-        for (int j = 0; j < c.noise_coordination_steps; j++) run_phase(s, SC_PHASE_COORDINATE_NOISE, j);
-        run_phase(s, SC_PHASE_APPLY_NOISE, 0);
-        for (int j = 0; j < c.relaxation_steps; j++) {
-            run_phase(s, SC_PHASE_RELAX, j);
-            if (j % 2 == 0) {
-                run_phase(s, SC_PHASE_RELAX_METAB, j);
-                run_phase(s, SC_PHASE_RELAX_PARTNERS, j);
-            }
-        }
-        run_phase(s, SC_PHASE_APPLY_VELOCITIES, 0);
-        run_phase(s, SC_PHASE_COMPLEXIFY, 0);
-        run_phase(s, SC_PHASE_TRANSITION, 0);
-        run_phase(s, SC_PHASE_POLYMERIZE, 0);
-        for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
-        int rc = run_phase(s, SC_PHASE_END_STEP, 0);
+        int rc = s->useGraphs ? step_graph(s) : step_direct(s);
         if (rc) return rc;
     }
     return SC_OK;
 }
+
 
 int sc_sync(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
