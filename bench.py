@@ -250,6 +250,48 @@ def cpu_sample(args, reps=1, warmup=0):
     return rate, threads, sample
 
 
+def batched_sample(args, native, torch):
+    """Many independent replica cells (the batched workload's size and mix
+    distribution, a sample of its 512 replicas): every replica steps on its own
+    stream as a captured graph, all in flight together, against the same
+    replicas stepped one at a time.  Wall-clock with the device synchronised
+    on both sides; particle-steps/s of all replicas."""
+    reps = scenes.batch_replicas(args.batch_replicas)
+    sims = []
+    for cfg, types, rules, p, m in reps:
+        s = native.Simulation(cfg, types, rules)
+        s.load_state(p, m)
+        s.prepare()
+        s.step(1)  # warm-up: captures the step graphs
+        sims.append(s)
+    items = sum(c.num_particles + c.num_metabolic_particles for c, *_ in reps)
+    for s in sims:
+        s.sync()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.batch_steps):
+        for s in sims:
+            s.step(1)
+    for s in sims:
+        s.sync()
+    batched_s = time.perf_counter() - t0
+    alone_s = 0.0
+    for s in sims:
+        t0 = time.perf_counter()
+        s.step(args.batch_steps)
+        s.sync()
+        alone_s += time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    batched = items * args.batch_steps / batched_s
+    alone = items * args.batch_steps / alone_s
+    return {"replicas": len(reps), "particles_and_metabolic": items, "steps": args.batch_steps,
+            "value": batched, "unit": UNIT, "one_at_a_time": alone, "speedup": batched / alone,
+            "sizes": "particles log-uniform in [2048, 262144] (seed 3), metabolic x2, cubes at 65,536 per "
+                     "(200 nm)^3, mix Dirichlet(2,2,1,1), periodic, 6 nm cells",
+            "timing": "wall clock, device synchronised before and after"}
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
@@ -358,6 +400,7 @@ def run_ours(args):
                        "sc_reduce_frame_async into pinned host memory (the copy overlaps the next step); "
                        "ends when the last frame has landed"}
     sim.close()
+    batched = batched_sample(args, native, torch) if args.batch_replicas > 0 and world == 1 else None
 
     line = None
     if rank == 0:
@@ -387,6 +430,7 @@ def run_ours(args):
             "state_finite": finite, "bonds_per_particle": bbar,
             "clocks": clocks.summary(),
             "gpu_launches": launches,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -403,6 +447,9 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.25,
                     help="volume fraction of the workload the CPU oracle steps (its timed sample)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-replicas", type=int, default=64,
+                    help="replica cells in the batched sample (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=4)
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()

@@ -127,6 +127,29 @@ def workload_config(name, **overrides):
     return abi.make_config(**kw)
 
 
+def batch_replicas(count, seed=3, n_lo=2048, n_hi=262144):
+    """Replica cells of the batched workload: particle counts log-uniform in
+    [n_lo, n_hi], twice as many metabolic items, each periodic cube scaled to
+    the small workload's number density (65,536 particles in 200 nm), type mix
+    (lipid, dummy, A, B) ~ Dirichlet(2, 2, 1, 1).  Returns a list of
+    (config, types, rules, particles, metabolic) for seeds seed*1000 + r."""
+    rng = np.random.default_rng(seed)
+    types, rules = baseline_types(), baseline_rules()
+    out = []
+    for r in range(count):
+        n = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        nm = 2 * n
+        box = float(200.0 * (n / 65536.0) ** (1.0 / 3.0))
+        mix = rng.dirichlet([2.0, 2.0, 1.0, 1.0])
+        cfg = workload_config("plain_small", num_particles=n, num_metabolic_particles=nm, sim_size=box,
+                              seed=seed * 1000 + r)
+        rr = np.random.default_rng(seed * 1000 + r)
+        p = uniform_particles(rr, n, box, types, fractions=tuple(zip((LIPID, DUMMY, TYPE_A, TYPE_B), mix)))
+        m = uniform_metabolic(rr, nm, box, types, cfg.num_metabolites)
+        out.append((cfg, types, rules, p, m))
+    return out
+
+
 def build_workload(name, **overrides):
     """Config, tables and initial state of a measured workload."""
     cfg = workload_config(name, **overrides)
