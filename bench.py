@@ -292,6 +292,28 @@ def batched_sample(args, native, torch):
             "timing": "wall clock, device synchronised before and after"}
 
 
+def serving_sample(args, capacity):
+    """The request loop on a scaled-down request stream: Poisson arrivals at
+    80 % of the measured batched capacity, particle counts log-uniform in
+    [4096, 131072], horizons uniform in [10, 60] steps, mix ~ Dirichlet(1,1,1,1),
+    a 160 GB budget; against the same stream served one request at a time."""
+    from spatial_cell_gb300 import serving
+    probe = serving.poisson_requests(args.serve_requests, 1.0, n_lo=4096, n_hi=131072, h_lo=10, h_hi=60)
+    mean_work = sum(3 * r.n * r.horizon for r in probe) / len(probe)
+    rate = 0.8 * capacity / mean_work
+    reqs = serving.poisson_requests(args.serve_requests, rate, n_lo=4096, n_hi=131072, h_lo=10, h_hi=60)
+    res = serving.Server(budget_bytes=160 << 30).run(reqs)
+    p50, p99 = serving.percentiles(res)
+    one = serving.Server(budget_bytes=max(r.bytes for r in reqs)).run(reqs)
+    q50, q99 = serving.percentiles(one)
+    return {"requests": len(reqs), "arrival_rate_per_s": rate, "p50_latency_s": p50, "p99_latency_s": p99,
+            "value": serving.throughput(res, reqs), "unit": UNIT,
+            "one_at_a_time": {"value": serving.throughput(one, reqs), "p50_latency_s": q50, "p99_latency_s": q99},
+            "stream": "Poisson at 80% of the batched capacity; particles log-uniform [4096, 131072], horizon "
+                      "uniform [10, 60] steps, metabolic x2, mix Dirichlet(1,1,1,1), 160 GB budget "
+                      "(scaled down from 10,000 requests of up to 1M particles and 5,000 steps)"}
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
@@ -401,6 +423,8 @@ def run_ours(args):
                        "ends when the last frame has landed"}
     sim.close()
     batched = batched_sample(args, native, torch) if args.batch_replicas > 0 and world == 1 else None
+    served = (serving_sample(args, batched["value"] if batched else value)
+              if args.serve_requests > 0 and world == 1 else None)
 
     line = None
     if rank == 0:
@@ -431,6 +455,7 @@ def run_ours(args):
             "clocks": clocks.summary(),
             "gpu_launches": launches,
             "batched": batched,
+            "serving": served,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -450,6 +475,7 @@ def main():
     ap.add_argument("--batch-replicas", type=int, default=64,
                     help="replica cells in the batched sample (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=4)
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving sample (0: skip it)")
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()

@@ -263,6 +263,9 @@ int sc_step(sc_sim *sim, int32_t n_steps);
 int sc_run_phase(sc_sim *sim, int32_t phase, int32_t arg);
 /* Waits for the sim's stream and reports kernel-side errors. */
 int sc_sync(sc_sim *sim);
+/* 1 when all work enqueued on the sim has finished, 0 while some is still
+ * running (does not wait; for loops that drive many sims at once). */
+int sc_idle(sc_sim *sim);
 
 /* Downloads the state in the reference layout, capacity-sized buffers (either
  * may be NULL).  Interaction slots at and beyond n_active_interactions are
@@ -318,6 +321,18 @@ int sc_frame_wait(sc_sim *sim, int64_t ticket);
  * are in perm / cell_start; SC_E_DEVICE if the sort reported an error. */
 int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info, int32_t n, uint32_t *perm,
                          uint32_t *cell_start, void *stream);
+
+/* ---- device scene generation (no counterpart in the reference) ----
+ * Replaces host-side uniform scene setup (setup/particle_setup.cuh) for
+ * callers that create many sims: fills the sim on the device with n
+ * particles (kind k of kinds[] with probability fractions[k], k < nkinds <= 4,
+ * position uniform in the box, uniform random orientation) and nm metabolic
+ * particles (type 1000, uniform, species 0 seeded at 100 in x < 0.2 * box,
+ * the other species uniform in [0, 10)), every record a function of (seed,
+ * index) only; radii and hydrophobicity come from the sim's type table.
+ * Counters as sc_load_state with step 0 and next particle id n. */
+int sc_generate_uniform(sc_sim *sim, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
+                        int32_t nkinds, uint64_t seed);
 
 /* ---- checkpoint / resume (no counterpart in the reference) ----
  * A checkpoint holds the whole state -- the active particle and metabolic

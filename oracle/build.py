@@ -47,7 +47,8 @@ def ref_path():
 
 def build_port(force=False):
     out = port_path()
-    srcs = [os.path.join(HERE, "scport.cpp"), os.path.join(CSRC, "scmath.h"), os.path.join(INCLUDE, "spatialcell.h")]
+    srcs = [os.path.join(HERE, "scport.cpp"), os.path.join(CSRC, "scmath.h"), os.path.join(CSRC, "sc_gen.h"),
+            os.path.join(INCLUDE, "spatialcell.h")]
     if not force and _newer(out, srcs):
         return out
     os.makedirs(os.path.dirname(out), exist_ok=True)

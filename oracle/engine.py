@@ -142,3 +142,23 @@ def set_threads(n):
 def max_threads():
     lib, f = load("port")
     return f["max_threads"]()
+
+
+def generate_uniform(n, nm, kinds, fractions, types, box, species, seed):
+    """The device scene generator's records built by the CPU oracle
+    (spatial_cell_gb300/csrc/sc_gen.h): (particles, metabolic) arrays."""
+    lib = ctypes.CDLL(build.build_port())
+    f = lib.scp_generate_uniform
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                  ctypes.c_int32, ctypes.c_float, ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    k = np.ascontiguousarray(kinds, np.int32)
+    fr = np.ascontiguousarray(fractions, np.float32)
+    t = np.ascontiguousarray(types, abi.TYPE_INFO_DTYPE)
+    p = np.zeros(max(n, 1), abi.PARTICLE_DTYPE)
+    m = np.zeros(max(nm, 1), abi.METABOLIC_DTYPE)
+    rc = f(n, nm, k.ctypes.data, fr.ctypes.data, len(k), t.ctypes.data, len(t), box, species, seed, p.ctypes.data,
+           m.ctypes.data)
+    if rc != 0:
+        raise ValueError("bad mix")
+    return p[:n], m[:nm]

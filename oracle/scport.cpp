@@ -30,6 +30,7 @@
 
 #include "scmath.h"
 #include "spatialcell.h"
+#include "sc_gen.h"
 
 #if defined(_OPENMP)
 #include <omp.h>
@@ -844,6 +845,19 @@ void scp_philox(const uint32_t *ctr, uint32_t k0, uint32_t k1, uint32_t *out) {
     sc_u4 o = sc_philox4x32_10(c, k0, k1);
     out[0] = o.x; out[1] = o.y; out[2] = o.z; out[3] = o.w;
 }
+// The device scene generator's records (sc_gen.h) built on the host.
+int scp_generate_uniform(int32_t n, int32_t nm, const int32_t *kinds, const float *fractions, int32_t nkinds,
+                         const sc_type_info *types, int32_t ntypes, float box, int32_t species, uint64_t seed,
+                         sc_particle *p, sc_metabolic_particle *m) {
+    sc_gen_mix mix;
+    if (n > 0 && sc_gen_make_mix(&mix, kinds, fractions, nkinds, types, ntypes)) return -1;
+    for (int32_t i = 0; i < n; i++) sc_gen_particle(&p[i], i, box, &mix, seed);
+    for (int32_t j = 0; j < nm; j++)
+        sc_gen_metabolic(&m[j], j, box, species, types[SC_PARTICLE_TYPE_METABOLIC].radius,
+                         types[SC_PARTICLE_TYPE_METABOLIC].hydrophobic, seed);
+    return 0;
+}
+
 void scp_f2h(const float *x, uint16_t *out, int n) {
     for (int i = 0; i < n; i++) out[i] = sc_f2h(x[i]);
 }

@@ -7,10 +7,12 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <cmath>
 #include <string>
 #include <vector>
 
+#include "sc_gen.h"
 #include "sc_launch.h"
 #include "sc_tile.cuh"
 
@@ -26,6 +28,18 @@ __device__ __forceinline__ float4 rd4(const uint8_t *r, int off) { return *(cons
 __device__ __forceinline__ float rdf(const uint8_t *r, int off) { return *(const float *)(r + off); }
 __device__ __forceinline__ int rdi(const uint8_t *r, int off) { return *(const int *)(r + off); }
 __device__ __forceinline__ int rdb(const uint8_t *r, int off) { return (int)*(const int8_t *)(r + off); }
+
+__global__ void k_gen_particles(uint8_t *aos, int n, float box, sc_gen_mix mix, uint64_t seed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sc_gen_particle(reinterpret_cast<sc_particle *>(aos + (size_t)i * sizeof(sc_particle)), i, box, &mix, seed);
+}
+__global__ void k_gen_metabolic(uint8_t *aos, int nm, float box, int species, float radius, int8_t hydrophobic,
+                                uint64_t seed) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nm)
+        sc_gen_metabolic(reinterpret_cast<sc_metabolic_particle *>(aos + (size_t)j * sizeof(sc_metabolic_particle)), j,
+                         box, species, radius, hydrophobic, seed);
+}
 
 __global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int cap, PFields F) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -168,6 +182,7 @@ struct sc_sim {
     long long launches = 0;
     std::string err;
     std::vector<void *> allocs;
+    std::vector<sc_type_info> types;        // host copy of the type table
     uint8_t *staging = nullptr;
     size_t stagingBytes = 0;
     bool loaded = false;
@@ -189,14 +204,17 @@ int set_err(sc_sim *s, int code, const std::string &m) {
                            std::string(#call) + ": " + cudaGetErrorString(e_));                           \
     } while (0)
 
+// Device memory comes from the device's stream-ordered pool on the sim's
+// stream: creating or destroying a sim does not synchronise the device, so
+// sims can come and go while others run (the request loop relies on it).
 template <class T>
 int dalloc(sc_sim *s, T **p, size_t count) {
     size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-    cudaError_t e = cudaMalloc((void **)p, bytes);
+    cudaError_t e = cudaMallocAsync((void **)p, bytes, s->st);
     if (e != cudaSuccess) {
         *p = nullptr;
         return set_err(s, e == cudaErrorMemoryAllocation ? SC_E_OOM : SC_E_CUDA,
-                       "cudaMalloc of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+                       "cudaMallocAsync of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
     }
     s->allocs.push_back((void *)*p);
     return SC_OK;
@@ -389,10 +407,28 @@ int step_graph(sc_sim *s) {
     return SC_OK;
 }
 
+// Once per device: the default memory pool keeps what sims free for the next
+// ones (no release back to the driver at synchronisations), and the tile
+// kernels may use large dynamic shared memory.
+void device_init(int device) {
+    static std::mutex mu;
+    static std::vector<char> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= device) done.resize((size_t)device + 1, 0);
+    if (done[(size_t)device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    sc_tile_init();
+    done[(size_t)device] = 1;
+}
+
 int ensure_staging(sc_sim *s, size_t bytes) {
     if (s->stagingBytes >= bytes) return SC_OK;
     if (s->staging) {
-        cudaFree(s->staging);
+        cudaFreeAsync(s->staging, s->st);
         s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->staging));
         s->staging = nullptr;
         s->stagingBytes = 0;
@@ -436,12 +472,25 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
 
     sc_sim *s = new sc_sim();
     s->cfg = *cfg;
+    if (n_types > 0) s->types.assign(types, types + n_types);
     cudaGetDevice(&s->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     // SC_GRAPHS=0 launches every step phase by phase instead of as a CUDA graph
     if (const char *g = getenv("SC_GRAPHS")) s->useGraphs = atoi(g) != 0;
-    sc_tile_init();
+    device_init(s->device);
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copySt, cudaStreamNonBlocking);
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            e = cudaEventCreateWithFlags(&s->reduced[k], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copied[k], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            sc_destroy(s);
+            return set_err(nullptr, SC_E_CUDA, cudaGetErrorString(e));
+        }
+    }
     s->gridCap = std::max(1, sms) * (2048 / SC_THREADS);
     ScParams &P = s->P;
     memset(&P, 0, sizeof P);
@@ -529,10 +578,13 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &dPrules, std::max<size_t>(prules.size(), 1))) ||
         (rc = dalloc(s, &dTypes, std::max<int>(n_types, 1))))
         return bail(rc);
-    cudaMemcpy(dFlat, flat.data(), flat.size() * sizeof(sc_rule), cudaMemcpyHostToDevice);
-    cudaMemcpy(dPidx, pidx.data(), pidx.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (!prules.empty()) cudaMemcpy(dPrules, prules.data(), prules.size() * sizeof(sc_rule), cudaMemcpyHostToDevice);
-    if (n_types > 0) cudaMemcpy(dTypes, types, (size_t)n_types * sizeof(sc_type_info), cudaMemcpyHostToDevice);
+    // (the host vectors live until the stream is synchronised below)
+    cudaMemcpyAsync(dFlat, flat.data(), flat.size() * sizeof(sc_rule), cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(dPidx, pidx.data(), pidx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+    if (!prules.empty())
+        cudaMemcpyAsync(dPrules, prules.data(), prules.size() * sizeof(sc_rule), cudaMemcpyHostToDevice, s->st);
+    if (n_types > 0)
+        cudaMemcpyAsync(dTypes, types, (size_t)n_types * sizeof(sc_type_info), cudaMemcpyHostToDevice, s->st);
     P.flat = dFlat;
     P.nFlat = maxId + 1;
     P.pidx = dPidx;
@@ -582,17 +634,10 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     }
     B.invalidateLists();
     B.polyCap = 4096;
-    cudaMemset(B.ctr, 0, sizeof(ScCounters));
-    cudaMemset(B.cellStartP, 0, ((size_t)P.cells + 1) * 4);
-    cudaMemset(B.cellStartM, 0, ((size_t)P.cells + 1) * 4);
-    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copySt, cudaStreamNonBlocking);
-    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
-        e = cudaEventCreateWithFlags(&s->reduced[k], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copied[k], cudaEventDisableTiming);
-    }
-    if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
-    e = cudaDeviceSynchronize();
+    cudaMemsetAsync(B.ctr, 0, sizeof(ScCounters), s->st);
+    cudaMemsetAsync(B.cellStartP, 0, ((size_t)P.cells + 1) * 4, s->st);
+    cudaMemsetAsync(B.cellStartM, 0, ((size_t)P.cells + 1) * 4, s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) return bail(set_err(s, SC_E_CUDA, cudaGetErrorString(e)));
     *out = s;
     return SC_OK;
@@ -601,20 +646,20 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
 void sc_destroy(sc_sim *s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    if (s->st) {
-        cudaStreamSynchronize(s->st);
-        cudaStreamDestroy(s->st);
-    }
     if (s->copySt) {
         cudaStreamSynchronize(s->copySt);
         cudaStreamDestroy(s->copySt);
+    }
+    if (s->st) {
+        for (void *p : s->allocs) cudaFreeAsync(p, s->st);  // after the sim's own work
+        cudaStreamSynchronize(s->st);
+        cudaStreamDestroy(s->st);
     }
     for (int k = 0; k < 2; k++) {
         if (s->reduced[k]) cudaEventDestroy(s->reduced[k]);
         if (s->copied[k]) cudaEventDestroy(s->copied[k]);
     }
     for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
-    for (void *p : s->allocs) cudaFree(p);
     delete s;
 }
 
@@ -704,6 +749,17 @@ int sc_sync(sc_sim *s) {
     return SC_OK;
 }
 
+int sc_idle(sc_sim *s) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    for (cudaStream_t st : {s->st, s->copySt}) {
+        cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaErrorNotReady) return 0;
+        if (e != cudaSuccess) return set_err(s, SC_E_CUDA, cudaGetErrorString(e));
+    }
+    return 1;
+}
+
 int sc_get_counters(sc_sim *s, sc_counters *out) {
     if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
     int rc = sc_sync(s);
@@ -783,6 +839,55 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
         SC_CK(s, cudaMemcpyAsync(metabolic, s->B.redM, (size_t)s->P.Nm * sizeof(sc_reduced_metabolic_particle),
                                  cudaMemcpyDeviceToHost, s->st));
     SC_CK(s, cudaStreamSynchronize(s->st));
+    return SC_OK;
+}
+
+int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
+                        int32_t nkinds, uint64_t seed) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    const int N = s->P.N, Nm = s->P.Nm;
+    if (n < 0 || nm < 0 || n > N || nm > Nm) return set_err(s, SC_E_INVALID, "scene larger than the capacity");
+    const int ntypes = (int)s->types.size();
+    sc_gen_mix mix;
+    memset(&mix, 0, sizeof mix);
+    if (n > 0 && (!kinds || !fractions || sc_gen_make_mix(&mix, kinds, fractions, nkinds, s->types.data(), ntypes)))
+        return set_err(s, SC_E_INVALID, "the particle mix needs 1 to 4 kinds of the type table, weights >= 0");
+    if (nm > 0 && ntypes <= SC_PARTICLE_TYPE_METABOLIC)
+        return set_err(s, SC_E_INVALID, "the type table has no metabolic particle type (1000)");
+    size_t bytes = std::max((size_t)n * sizeof(sc_particle), (size_t)nm * sizeof(sc_metabolic_particle));
+    int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    B.invalidateLists();
+    s->P.binned = 0;
+    for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
+    for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
+    const float box = s->cfg.sim_size;
+    if (N > 0) {
+        if (n) k_gen_particles<<<nb_of(n), SC_THREADS, 0, s->st>>>(s->staging, n, box, mix, seed);
+        k_unpack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, n, N, B.p[0]);
+    }
+    if (Nm > 0) {
+        if (nm) {
+            const sc_type_info &mt = s->types[SC_PARTICLE_TYPE_METABOLIC];
+            k_gen_metabolic<<<nb_of(nm), SC_THREADS, 0, s->st>>>(s->staging, nm, box, s->cfg.num_metabolites,
+                                                                 mt.radius, mt.hydrophobic, seed);
+        }
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], B.mcLscs,
+                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+    }
+    ScCounters c;
+    memset(&c, 0, sizeof c);
+    c.nActive = n;
+    c.lastActive = n - 1;
+    c.nextId = n;
+    c.nActiveM = nm;
+    SC_CK(s, cudaMemcpyAsync(B.ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    rc = check_launch(s);
+    if (rc) return rc;
+    s->loaded = true;
     return SC_OK;
 }
 

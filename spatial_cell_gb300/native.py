@@ -32,6 +32,7 @@ _SIGS = {
     "sc_step": (ctypes.c_int, [_P, ctypes.c_int32]),
     "sc_run_phase": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "sc_sync": (ctypes.c_int, [_P]),
+    "sc_idle": (ctypes.c_int, [_P]),
     "sc_export_state": (ctypes.c_int, [_P, _P, _P]),
     "sc_export_grid": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "sc_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(abi.Counters)]),
@@ -39,6 +40,8 @@ _SIGS = {
     "sc_reduce_frame_async": (ctypes.c_int64, [_P, _P, _P]),
     "sc_frame_wait": (ctypes.c_int, [_P, ctypes.c_int64]),
     "sc_get_stream": (ctypes.c_void_p, [_P]),
+    "sc_generate_uniform": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P, ctypes.c_int32,
+                                           ctypes.c_uint64]),
     "sc_checkpoint_write": (ctypes.c_int, [_P, _P]),
     "sc_checkpoint_read": (ctypes.c_int, [_P, _P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
@@ -162,11 +165,26 @@ class Simulation:
         """Loads from raw host pointers (e.g. pinned buffers)."""
         _check(self.L.sc_load_state(self.h, p_ptr, n, m_ptr, nm, step, next_particle_id), self.h, "sc_load_state")
 
+    def generate_uniform(self, n, nm, kinds, fractions, seed):
+        """Fills the sim on the device (sc_generate_uniform): n particles of the
+        given kinds / weights and nm metabolic particles, uniform in the box."""
+        k = np.ascontiguousarray(kinds, np.int32)
+        f = np.ascontiguousarray(fractions, np.float32)
+        _check(self.L.sc_generate_uniform(self.h, n, nm, abi.ptr(k), abi.ptr(f), len(k), seed), self.h,
+               "sc_generate_uniform")
+
     def prepare(self):
         _check(self.L.sc_prepare(self.h), self.h, "sc_prepare")
 
     def step(self, n=1):
         _check(self.L.sc_step(self.h, n), self.h, "sc_step")
+
+    def idle(self):
+        """True when all work enqueued on this sim has finished (does not wait)."""
+        rc = self.L.sc_idle(self.h)
+        if rc < 0:
+            _check(rc, self.h, "sc_idle")
+        return rc == 1
 
     def run_phase(self, phase, arg=0):
         _check(self.L.sc_run_phase(self.h, phase, arg), self.h, f"sc_run_phase({phase})")
