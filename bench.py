@@ -210,6 +210,8 @@ def per_phase_times(sim, stream, torch, reps=3):
         e1.record(stream)
         e1.synchronize()
         out[name] = e0.elapsed_time(e1) / (2 * reps)
+        if name == "relax_metab":
+            out["_pairs_metabolic"] = sim.pair_counts()[1]  # the list the timed launches walked
     return out
 
 
@@ -383,6 +385,8 @@ def run_ours(args):
 
     # per-phase breakdown (for the roofline of the dominant kernel)
     phase_ms = per_phase_times(sim, stream, torch)
+    pairs = list(sim.pair_counts())  # lists as the per-phase timing left them
+    pairs[1] = phase_ms.pop("_pairs_metabolic")
     counts = {"relax": cfg.relaxation_steps, "relax_metab": (cfg.relaxation_steps + 1) // 2,
               "relax_partners": (cfg.relaxation_steps + 1) // 2, "diffuse": cfg.metabolite_diffusion_steps,
               "coordinate_noise": cfg.noise_coordination_steps}
@@ -398,6 +402,18 @@ def run_ours(args):
     step_bytes = step_algorithmic_bytes(cfg, bbar)
     step_achieved = step_bytes / (ms_per_step / 1e3) / 1e9
     traffic = measured_traffic(dom, args.workload) if args.fraction == 1.0 else None
+    # The metabolic relaxation's neighbour data moves through the SM's L1 /
+    # shared-memory data pipe: a position and a velocity (2 x 16 B) and a
+    # 4-byte list entry per pair, the item's own 3 records and its output.
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_hz = (clocks.summary().get("sm_mhz") or 2070.0) * 1e6
+    l1_peak = sms * 128 * sm_hz / 1e9
+    l1_bytes = pairs[1] * 36 + Nm * 64 if pairs[1] >= 0 else None
+    l1 = None if l1_bytes is None else {
+        "kernel": "relax_metab", "pairs_per_launch": pairs[1], "bytes_per_launch": l1_bytes,
+        "achieved": l1_bytes / (phase_ms["relax_metab"] / 1e3) / 1e9, "peak": l1_peak, "unit": "GB/s",
+        "frac": l1_bytes / (phase_ms["relax_metab"] / 1e3) / 1e9 / l1_peak,
+        "peak_is": f"{sms} SMs x 128 B/clock at the sampled SM clock"}
 
     # end to end through the C ABI with host buffers
     sim2 = native.Simulation(cfg, types, rules)
@@ -448,6 +464,9 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": alg, "launch_ms": phase_ms[dom]},
             "step_roofline": {"bound": "hbm", "achieved": step_achieved, "peak": peak, "unit": "GB/s",
                               "frac": step_achieved / peak, "algorithmic_bytes_per_step": step_bytes},
+            "l1_roofline": l1,
+            "pairs_per_list": {"particle": pairs[0], "metabolic": pairs[1], "lipid_metabolic": pairs[2],
+                               "diffusion": pairs[3]},
             "phase_ms_per_launch": phase_ms, "phase_share_of_step": share,
             "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                              "sample": cpu_desc},

@@ -263,6 +263,11 @@ int sc_step(sc_sim *sim, int32_t n_steps);
 int sc_run_phase(sc_sim *sim, int32_t phase, int32_t arg);
 /* Waits for the sim's stream and reports kernel-side errors. */
 int sc_sync(sc_sim *sim);
+/* Pairs held by the current pair lists (no counterpart in the reference; for
+ * measurement): out[0] particle pairs (coordinateNoise / relax), out[1]
+ * metabolic relaxation, out[2] lipid-metabolic, out[3] diffusion; -1 for a
+ * list not built since its inputs last changed.  Waits for the sim. */
+int sc_pair_counts(sc_sim *sim, int64_t out[4]);
 /* 1 when all work enqueued on the sim has finished, 0 while some is still
  * running (does not wait; for loops that drive many sims at once). */
 int sc_idle(sc_sim *sim);

@@ -44,7 +44,8 @@ struct ScBuffers {
     int *classPP;  // SC_RELAX_CLASSES segments of N item indices
     int *permM, *permLM, *permD;  // count-ordered list position -> item
     uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
-    int *ovfPP, *ovfM;            // overflowed items (PP: item index, M: list position)
+    int *ovfPP, *ovfM;            // overflowed items
+    int *warpOffM;                // metabolic pair pool: first entry of every warp's region
     bool validPP, validM, validLM, validD;
     void invalidateLists() { validPP = validM = validLM = validD = false; }
     // polymerisation list

@@ -29,6 +29,18 @@ __device__ __forceinline__ float rdf(const uint8_t *r, int off) { return *(const
 __device__ __forceinline__ int rdi(const uint8_t *r, int off) { return *(const int *)(r + off); }
 __device__ __forceinline__ int rdb(const uint8_t *r, int off) { return (int)*(const int8_t *)(r + off); }
 
+// Sum of list counts over the active items (counts above a list's capacity
+// are overflowed items, counted as they are).
+__global__ void k_sum_counts(const int *__restrict__ cnt, const int *__restrict__ nActivePtr, long long *out) {
+    const int n = *nActivePtr;
+    long long acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        acc += cnt[i] == INT_MAX ? 0 : cnt[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)out, (unsigned long long)acc);
+}
+
 __global__ void k_gen_particles(uint8_t *aos, int n, float box, sc_gen_mix mix, uint64_t seed) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) sc_gen_particle(reinterpret_cast<sc_particle *>(aos + (size_t)i * sizeof(sc_particle)), i, box, &mix, seed);
@@ -624,7 +636,8 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
-        (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)))
+        (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)) ||
+        (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)))
         return bail(rc);
     // The LM list is built in the diffusion list's buffer when it fits.
     if (sc_list_words(SC_LIST_LM, (int)N) <= sc_list_words(SC_LIST_D, (int)Nm)) {
@@ -747,6 +760,28 @@ int sc_sync(sc_sim *s) {
     SC_CK(s, cudaMemcpy(&derr, &s->B.ctr->error, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr) return set_err(s, SC_E_DEVICE, "device-side error code " + std::to_string(derr));
     return SC_OK;
+}
+
+int sc_pair_counts(sc_sim *s, int64_t out[4]) {
+    if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
+    cudaSetDevice(s->device);
+    const ScBuffers &B = s->B;
+    const int *cnt[4] = {B.cntPP, B.cntM, B.cntLM, B.cntD};
+    const bool valid[4] = {B.validPP, B.validM, B.validLM, B.validD};
+    const int cap[4] = {s->P.N, s->P.Nm, s->P.N, s->P.Nm};
+    const int *nact[4] = {&B.ctr->nActive, &B.ctr->nActiveM, &B.ctr->nActive, &B.ctr->nActiveM};
+    long long *d = nullptr;
+    SC_CK(s, cudaMallocAsync((void **)&d, 4 * sizeof(long long), s->st));
+    SC_CK(s, cudaMemsetAsync(d, 0, 4 * sizeof(long long), s->st));
+    for (int k = 0; k < 4; k++)
+        if (valid[k] && cap[k] > 0)
+            k_sum_counts<<<std::max(1, std::min(nb_of(cap[k]), 1024)), SC_THREADS, 0, s->st>>>(cnt[k], nact[k], d + k);
+    long long h[4] = {0, 0, 0, 0};
+    SC_CK(s, cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, s->st));
+    SC_CK(s, cudaFreeAsync(d, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    for (int k = 0; k < 4; k++) out[k] = valid[k] ? (int64_t)h[k] : -1;
+    return check_launch(s);
 }
 
 int sc_idle(sc_sim *s) {

@@ -117,14 +117,13 @@ __device__ __forceinline__ const uint4 *sc_list4_chunks(const uint32_t *list, in
 // of the block must call it.  `scratch` is written earlier in the same kernel
 // by other threads of the block, so it is read through a plain (coherent)
 // pointer after the barrier.
+// The block's ranking by descending list length: thread t takes position
+// b0 + t, whose item is b0 + *src (list length *cs, -1 past the last item).
 template <int K>
-__device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit, int cap,
-                                                   const uint32_t *scratch, uint32_t *__restrict__ list,
-                                                   int *__restrict__ cnt, int *__restrict__ perm,
-                                                   int *__restrict__ ovf = nullptr, int *__restrict__ ovfCount = nullptr) {
+__device__ __forceinline__ void count_rank(bool valid, int c, int *src, int *cs) {
     __shared__ int hist[K + 3];
     __shared__ int s_cnt[SC_THREADS], s_src[SC_THREADS];
-    const int t = threadIdx.x, b0 = blockIdx.x * SC_THREADS;
+    const int t = threadIdx.x;
     for (int b = t; b < K + 3; b += SC_THREADS) hist[b] = 0;
     s_cnt[t] = valid ? c : -1;
     __syncthreads();
@@ -149,7 +148,19 @@ __device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit,
     __syncthreads();
     s_src[hist[bin] + idx] = t;
     __syncthreads();
-    const int src = s_src[t], cs = s_cnt[src], g = b0 + t;
+    *src = s_src[t];
+    *cs = s_cnt[*src];
+}
+
+template <int K>
+__device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit, int cap,
+                                                   const uint32_t *scratch, uint32_t *__restrict__ list,
+                                                   int *__restrict__ cnt, int *__restrict__ perm,
+                                                   int *__restrict__ ovf = nullptr, int *__restrict__ ovfCount = nullptr) {
+    const int b0 = blockIdx.x * SC_THREADS;
+    int src, cs;
+    count_rank<K>(valid, c, &src, &cs);
+    const int g = b0 + threadIdx.x;
     if (g < cap) {
         perm[g] = cs >= 0 ? b0 + src : -1;
         cnt[g] = max(cs, 0);
@@ -782,19 +793,89 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     });
 }
 
+// M pairs with their frozen geometry.  Positions do not change between the
+// sort and applyVelocities, so for every listed pair the part of the
+// reference's velocity term that depends on positions only,
+// A = tpos - normalize(tpos - pos) * collisionDistance (metabolites.cuh:
+// 196-203, 235-242), is the same in every relaxation sub-iteration.  It is
+// evaluated here, once per step, and each sub-iteration adds
+// ((A + tvel) - (pos + vel)) * 0.9 * weight: A is exactly the float3 the
+// reference's expression evaluates first, so sums and rounding are its own.
+// Layout: the pairs of a warp's 32 positions share one region of the pool,
+// entry k of lane l at warpOff[w] + 32 k + l, 16 bytes {neighbour | kind,
+// A.x, A.y, A.z}; a region is sized by the warp's longest list (its first
+// position: lists are count-ordered).  An overflowed item, or every item of
+// a block the pool has no room for, is listed in `ovf` for the scan.
+__device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int c, const uint32_t *scratch,
+                                             const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
+                                             uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
+                                             int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
+                                             int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
+    __shared__ int s_n[SC_THREADS / 32];
+    __shared__ int s_base;
+    const int b0 = blockIdx.x * SC_THREADS, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int src, cs;
+    count_rank<SC_LIST_M>(valid, c, &src, &cs);
+    const int limit = min(SC_LIST_M, P.listLimit);
+    bool ovfl = cs > limit;
+    int n = ovfl ? 0 : max(cs, 0);
+    if (lane == 0) s_n[warp] = n;  // the warp's longest stored list (descending order)
+    __syncthreads();
+    if (t == 0) {
+        int total = 0;
+        for (int w = 0; w < SC_THREADS / 32; w++) total += s_n[w] * 32;
+        const int base = total ? atomicAdd(poolUsed, total) : 0;
+        s_base = base + total <= poolCap ? base : -1;
+    }
+    __syncthreads();
+    if (s_base < 0 && cs > 0) {
+        ovfl = true;
+        n = 0;
+    }
+    int off = s_base;
+    for (int w = 0; w < warp; w++) off += s_n[w] * 32;
+    const int g = b0 + t;
+    if (g < cap) {
+        perm[g] = cs >= 0 ? b0 + src : -1;
+        cnt[g] = ovfl ? INT_MAX : max(cs, 0);
+        if (lane == 0) warpOff[g >> 5] = s_base < 0 ? 0 : off;
+    }
+    if (ovfl) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
+    if (n == 0) return;
+    const int i = b0 + src;
+    const float4 p4 = mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
+    const float prad = p4.w;
+    CollisionDistCache cm, cp;
+    uint4 *__restrict__ out = pool + off + lane;
+    for (int k = 0; k < n; k++) {
+        const uint32_t e = scratch[sc_list_at(SC_LIST_M, i, k)];
+        const int j = (int)(e & SC_M_INDEX);
+        const bool fromP = (e & SC_M_FROM_P) != 0;
+        const float4 t4 = fromP ? ppos_[j] : mpos[j];
+        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+        const sc_f3 nd = normalize(tpos - pp);
+        const float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
+        const sc_f3 a = tpos - nd * cd;
+        out[(size_t)k * 32] = make_uint4(e, __float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z));
+    }
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
                                                         const uint32_t *__restrict__ cellStartP,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                        uint32_t *__restrict__ list, uint32_t *scratch,
+                                                        uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
+                                                        int *__restrict__ warpOff, uint32_t *scratch,
                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
     if (valid && (minfo[i].z & SC_ACTIVE)) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
-    emit_count_ordered<SC_LIST_M>(valid, c, P.listLimit, cap, scratch, list, cnt, perm, ovf, ovfCount);
+    emit_m_pairs(P, valid, c, scratch, mpos, ppos_, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
 }
 
 
@@ -809,6 +890,8 @@ struct RelaxMArgs {
     const float4 *__restrict__ ppos;
     const int4 *__restrict__ pinfo;
     const float4 *__restrict__ pvel;
+    const uint4 *__restrict__ pool;     // pairs with their geometry (emit_m_pairs)
+    const int *__restrict__ warpOff;
 };
 
 // The contribution of one colliding neighbour (a metabolic item, or a lipid
@@ -824,52 +907,42 @@ __device__ __forceinline__ void metab_pair(const Imager &IM, sc_f3 pp, sc_f3 ppv
 
 // Items whose list fits.  The next entry's neighbour data is loaded while the
 // current one is evaluated (the loop is bound by the latency of those loads).
+// Items whose list fits, in count order: each pair adds its precomputed
+// geometry and the neighbour's current velocity; the next pair's entry and
+// velocity are loaded while the current one is added.
 __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, RelaxMArgs A) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *A.nActivePtr) return;
     const int i = A.L.perm[g];
     if (i < 0) return;
-    float4 v4 = A.mvelIn[i];
+    const float4 v4 = A.mvelIn[i];
     if (!(A.minfo[i].z & SC_ACTIVE)) {
         A.mvelOut[i] = v4;
         return;
     }
     const int c = A.L.cnt[g];
     if (c > min(SC_LIST_M, P.listLimit)) return;
-    float4 p4 = A.mpos[i];
-    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
-    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
-    const float prad = p4.w;
+    const float4 p4 = A.mpos[i];
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
-    const sc_f3 ppv = pp + pv;
+    const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    CollisionDistCache cm, cp;   // neighbours of each kind share a radius
-    // Four entries per list load; their neighbours are gathered together, and
-    // the next chunk of the list is loaded while this one is evaluated.
-    const uint4 *__restrict__ chunks = sc_list4_chunks(A.L.list, SC_LIST_M, g);
-    uint4 E = c > 0 ? chunks[0] : make_uint4(0, 0, 0, 0);
-    for (int k0 = 0; k0 < c; k0 += 4) {
-        const uint4 En = k0 + 4 < c ? chunks[(size_t)(k0 / 4 + 1) * 32] : make_uint4(0, 0, 0, 0);
-        const uint32_t e[4] = {E.x, E.y, E.z, E.w};
-        float4 t4[4], tv[4];
-#pragma unroll
-        for (int kk = 0; kk < 4; kk++) {
-            if (k0 + kk < c) {
-                const int j = (int)(e[kk] & SC_M_INDEX);
-                const bool fp = (e[kk] & SC_M_FROM_P) != 0;
-                t4[kk] = fp ? A.ppos[j] : A.mpos[j];
-                tv[kk] = fp ? A.pvel[j] : A.mvelIn[j];
-            }
+    const uint4 *__restrict__ pairs = A.pool + A.warpOff[g >> 5] + (g & 31);
+    uint4 E = c > 0 ? pairs[0] : make_uint4(0, 0, 0, 0);
+    float4 tv = c > 0 ? ((E.x & SC_M_FROM_P) ? A.pvel : A.mvelIn)[E.x & SC_M_INDEX] : make_float4(0, 0, 0, 0);
+    for (int k = 0; k < c; k++) {
+        uint4 En = E;
+        float4 tvn = tv;
+        if (k + 1 < c) {
+            En = pairs[(size_t)(k + 1) * 32];
+            tvn = ((En.x & SC_M_FROM_P) ? A.pvel : A.mvelIn)[En.x & SC_M_INDEX];
         }
-#pragma unroll
-        for (int kk = 0; kk < 4; kk++) {
-            if (k0 + kk >= c) break;
-            const bool fp = (e[kk] & SC_M_FROM_P) != 0;
-            const float cd = fp ? cp.get(prad, t4[kk].w) : cm.get(prad, t4[kk].w);
-            metab_pair(IM, pp, ppv, t4[kk], tv[kk], cd, fp, dV, w);
-        }
+        const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
+        const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
+        w += kw;
+        dV += (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
         E = En;
+        tv = tvn;
     }
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
@@ -916,7 +989,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
                                                                      const int *__restrict__ ovf,
                                                                      const int *__restrict__ ovfCount) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x)
-        relax_metab_scan_item(P, A, A.L.perm ? A.L.perm[ovf[t]] : ovf[t]);
+        relax_metab_scan_item(P, A, ovf[t]);
 }
 
 // ---- the same sweep on column-segment tiles (sc_tile.cuh) ---------------------
@@ -1933,9 +2006,11 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
                 c.P, B.cellStartM, B.cellStartP, M.pos, M.info, F.pos, F.info, reinterpret_cast<uint16_t *>(B.listM),
                 B.cntM, B.ovfM, &B.ctr->ovfM);
         } else {
-            k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM,
-                                                                 M.pos, M.info, F.pos, F.info, B.listM, B.listD, B.cntM,
-                                                                 B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
+            cudaMemsetAsync(&B.ctr->poolM, 0, sizeof(int), c.st);
+            k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
+                c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info,
+                reinterpret_cast<uint4 *>(B.listM), (int)(sc_list_words(SC_LIST_M, c.P.Nm) / 4), &B.ctr->poolM,
+                B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
         }
         (*c.launches)++;
         B.validM = true;
@@ -1945,7 +2020,8 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     L.cnt = B.cntM;
     L.cap = c.P.Nm;
     L.perm = tiles ? nullptr : B.permM;
-    RelaxMArgs A{B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, L, M.vel, X.vel, F.pos, F.info, F.vel};
+    RelaxMArgs A{B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, L, M.vel, X.vel, F.pos, F.info, F.vel,
+                 reinterpret_cast<const uint4 *>(B.listM), B.warpOffM};
     if (tiles) {
         k_relax_metab_tile<<<tile_blocks(c.P), SC_THREADS, sc_tile_bytes(c.P.tileCapM, c.P.tileCapP, 32), c.st>>>(
             c.P, A, reinterpret_cast<const uint16_t *>(B.listM), &B.ctr->error);

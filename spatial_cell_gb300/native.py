@@ -33,6 +33,7 @@ _SIGS = {
     "sc_run_phase": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "sc_sync": (ctypes.c_int, [_P]),
     "sc_idle": (ctypes.c_int, [_P]),
+    "sc_pair_counts": (ctypes.c_int, [_P, _P]),
     "sc_export_state": (ctypes.c_int, [_P, _P, _P]),
     "sc_export_grid": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "sc_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(abi.Counters)]),
@@ -178,6 +179,12 @@ class Simulation:
 
     def step(self, n=1):
         _check(self.L.sc_step(self.h, n), self.h, "sc_step")
+
+    def pair_counts(self):
+        """Pairs in the current lists: (particle, metabolic, lipid-metabolic, diffusion), -1 if not built."""
+        out = np.zeros(4, np.int64)
+        _check(self.L.sc_pair_counts(self.h, abi.ptr(out)), self.h, "sc_pair_counts")
+        return tuple(int(x) for x in out)
 
     def idle(self):
         """True when all work enqueued on this sim has finished (does not wait)."""

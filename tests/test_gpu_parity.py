@@ -144,3 +144,46 @@ def test_step_graphs_equal_direct_launches(product, monkeypatch):
     assert a[0].tobytes() == b[0].tobytes()
     assert a[1].tobytes() == b[1].tobytes()
     assert (ca.step, ca.n_active_particles, ca.kernel_launches) == (cb.step, cb.n_active_particles, cb.kernel_launches)
+
+
+@pytest.mark.parametrize("drop", ["metabolic", "particles", "both"])
+def test_empty_sets(product, drop):
+    """A state without metabolic items, without particles, or with neither:
+    the step runs and matches the oracle (capacities stay non-zero)."""
+    cfg, types, rules, p, m, nid = scenes.test_scene(14, n=900, nm=1800, box=42.0, periodic=1)
+    if drop in ("metabolic", "both"):
+        m = m[:0]
+    if drop in ("particles", "both"):
+        p = p[:0]
+        nid = 0
+    cfg_, gpu, cpu = _engines(product, (cfg, types, rules, p, m, nid))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, f"2 steps without {drop}")
+
+
+def test_inactive_items_inside_the_range(product):
+    """Items flagged inactive among active ones (the reference's gaps after
+    removals) are sorted past the cells and left untouched."""
+    cfg, types, rules, p, m, nid = scenes.test_scene(15, n=900, nm=1800, box=42.0)
+    p = p.copy()
+    m = m.copy()
+    p["flags"][::7] &= ~abi.PARTICLE_FLAG_ACTIVE
+    m["flags"][::5] &= ~abi.PARTICLE_FLAG_ACTIVE
+    cfg_, gpu, cpu = _engines(product, (cfg, types, rules, p, m, nid))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, "2 steps with inactive items")
+
+
+def test_capacity_exactly_full(product):
+    """Active counts equal to the capacities (no slack slot anywhere)."""
+    cfg, types, rules, p, m, nid = scenes.test_scene(16, n=700, nm=1300, box=40.0, capacity_slack=0)
+    cfg.num_metabolic_particles = len(m)
+    cfg_, gpu, cpu = _engines(product, (cfg, types, rules, p, m, nid))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, "2 steps at full capacity")
