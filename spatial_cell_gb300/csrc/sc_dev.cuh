@@ -109,7 +109,26 @@ struct ScParams {
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
     int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
     int tileCapM, tileCapP;   // tile capacities (slots) of the metabolic sweeps; 0: tiles off
+    // Candidate tests that need no record load: after a metabolic sort every
+    // binned metabolic item is active (inactive ones sort past the cells)
+    // until removeInterferingMetabolicParticles; after a particle sort
+    // lipidP[slot] says "active lipid" (types and particle flags do not
+    // change between sorts).
+    int mAllActive;
+    int lipidValid;
+    const uint8_t *lipidP;
 };
+
+// Whether sorted particle j is an active lipid.
+__device__ __forceinline__ bool active_lipid(const ScParams &P, const int4 *__restrict__ pinfo, int j) {
+    if (P.lipidValid) return P.lipidP[j] != 0;
+    const int4 tin = pinfo[j];
+    return (tin.z & SC_ACTIVE) && tin.y == SC_PARTICLE_TYPE_LIPID;
+}
+// Whether sorted metabolic item j is active.
+__device__ __forceinline__ bool active_m(const ScParams &P, const int4 *__restrict__ minfo, int j) {
+    return P.mAllActive || (minfo[j].z & SC_ACTIVE);
+}
 #define SC_BINNED_P 1
 #define SC_BINNED_M 2
 

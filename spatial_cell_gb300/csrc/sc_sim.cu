@@ -167,6 +167,15 @@ __global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePt
 }
 
 __global__ void k_after_sort(ScCounters *c) { c->lastActive = c->nActive - 1; }
+// Per sorted particle slot: 1 for an active lipid (the metabolic kernels'
+// candidate test); slots past the active ones are cleared.
+__global__ void k_mark_lipids(const int *__restrict__ nActivePtr, int cap, const int4 *__restrict__ info,
+                              uint8_t *__restrict__ lipid) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    const int4 in = info[i];
+    lipid[i] = (i < *nActivePtr && (in.z & SC_ACTIVE) && in.y == SC_PARTICLE_TYPE_LIPID) ? 1 : 0;
+}
 __global__ void k_end_step(ScCounters *c) { c->step++; }
 
 }  // namespace
@@ -266,7 +275,8 @@ void sort_particles(sc_sim *s) {
     sc_launch_gather_particles(s->st, B.valsP[cur], N, B.P(), B.Pnext(), &s->launches);
     B.flipAllP();
     k_after_sort<<<1, 1, 0, s->st>>>(B.ctr);
-    s->launches++;
+    k_mark_lipids<<<nb_of(N), SC_THREADS, 0, s->st>>>(&B.ctr->nActive, N, B.P().info, B.lipidP);
+    s->launches += 2;
 }
 
 void sort_metabolic(sc_sim *s) {
@@ -302,6 +312,9 @@ void binned_after(ScParams &P, int phase) {
     if (phase == SC_PHASE_SORT_PARTICLES) P.binned |= SC_BINNED_P;
     if (phase == SC_PHASE_SORT_METABOLIC) P.binned |= SC_BINNED_M;
     if (phase == SC_PHASE_APPLY_VELOCITIES) P.binned = 0;
+    if (phase == SC_PHASE_SORT_METABOLIC) P.mAllActive = 1;  // inactive items sort past the cells
+    if (phase == SC_PHASE_REMOVE_INTERFERING) P.mAllActive = 0;
+    if (phase == SC_PHASE_SORT_PARTICLES) P.lipidValid = 1;  // marked by sort_particles
 }
 
 // The host-side state a step reads and changes.
@@ -310,7 +323,7 @@ std::vector<int> host_state(const sc_sim *s) {
     std::vector<int> v(B.cp, B.cp + FP_COUNT);
     v.insert(v.end(), B.cm, B.cm + FM_COUNT);
     v.insert(v.end(), {B.sortCurP, B.sortCurM, (int)B.validPP, (int)B.validM, (int)B.validLM, (int)B.validD,
-                       s->P.binned});
+                       s->P.binned, s->P.mAllActive, s->P.lipidValid});
     return v;
 }
 void set_host_state(sc_sim *s, const std::vector<int> &v) {
@@ -325,6 +338,8 @@ void set_host_state(sc_sim *s, const std::vector<int> &v) {
     B.validLM = v[k++] != 0;
     B.validD = v[k++] != 0;
     s->P.binned = v[k++];
+    s->P.mAllActive = v[k++];
+    s->P.lipidValid = v[k++];
 }
 
 int run_phase(sc_sim *s, int phase, int arg) {
@@ -637,7 +652,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
         (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)) ||
-        (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)))
+        (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)) || (rc = dalloc(s, &B.lipidP, N)))
         return bail(rc);
     // The LM list is built in the diffusion list's buffer when it fits.
     if (sc_list_words(SC_LIST_LM, (int)N) <= sc_list_words(SC_LIST_D, (int)Nm)) {
@@ -647,6 +662,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     }
     B.invalidateLists();
     B.polyCap = 4096;
+    P.lipidP = B.lipidP;
     cudaMemsetAsync(B.ctr, 0, sizeof(ScCounters), s->st);
     cudaMemsetAsync(B.cellStartP, 0, ((size_t)P.cells + 1) * 4, s->st);
     cudaMemsetAsync(B.cellStartM, 0, ((size_t)P.cells + 1) * 4, s->st);
@@ -692,6 +708,8 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     ScBuffers &B = s->B;
     B.invalidateLists();
     s->P.binned = 0;
+    s->P.mAllActive = 0;
+    s->P.lipidValid = 0;
     for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
     if (N > 0) {
@@ -896,6 +914,8 @@ int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, 
     ScBuffers &B = s->B;
     B.invalidateLists();
     s->P.binned = 0;
+    s->P.mAllActive = 0;
+    s->P.lipidValid = 0;
     for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
     const float box = s->cfg.sim_size;

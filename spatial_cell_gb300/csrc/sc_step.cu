@@ -770,7 +770,7 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     CollisionDistCache cm, cp;
     cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
         for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
-            if ((int)j == i || !(minfo[j].z & SC_ACTIVE)) continue;
+            if ((int)j == i || !active_m(P, minfo, (int)j)) continue;
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
@@ -780,8 +780,7 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
             }
         }
         for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
-            int4 tin = pinfo[j];
-            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+            if (!active_lipid(P, pinfo, (int)j)) continue;
             float4 t4 = ppos_[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
@@ -964,7 +963,7 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
     cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
         for (uint32_t j = A.cellStartM[key], e = A.cellStartM[key + 1]; j < e; j++) {
             if ((int)j == i) continue;
-            if (!(A.minfo[j].z & SC_ACTIVE)) continue;
+            if (!active_m(P, A.minfo, (int)j)) continue;
             float4 t4 = A.mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
@@ -972,8 +971,7 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
                 metab_pair(IM, pp, ppv, t4, A.mvelIn[j], cm.get(prad, t4.w), false, dV, w);
         }
         for (uint32_t j = A.cellStartP[key], e = A.cellStartP[key + 1]; j < e; j++) {
-            int4 tin = A.pinfo[j];
-            if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) continue;
+            if (!active_lipid(P, A.pinfo, (int)j)) continue;
             float4 t4 = A.ppos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
@@ -1257,7 +1255,7 @@ __device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t 
     const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cc;
     scan27(P, cellStartM, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
-        if (!(minfo[j].z & SC_ACTIVE)) return;
+        if (!active_m(P, minfo, j)) return;
         float4 t4 = mpos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
@@ -1332,7 +1330,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     } else {
         const float lim = P.maxInt;
         scan27(P, cellStartM, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
-            if (!(minfo[j].z & SC_ACTIVE)) return;
+            if (!active_m(P, minfo, j)) return;
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
@@ -1706,7 +1704,7 @@ __device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *
     const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
     scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
-        if (j == i || !(info[j].z & SC_ACTIVE)) return;
+        if (j == i || !active_m(P, info, j)) return;
         float4 t4 = pos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
@@ -1805,7 +1803,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
         const float lim = P.maxDiff;
         scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
             if (j == i) return;
-            if (!(info[j].z & SC_ACTIVE)) return;
+            if (!active_m(P, info, j)) return;
             float4 t4 = pos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
@@ -1838,8 +1836,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
     int flags = in.z;
     const float lim = P.maxInt;
     scan27(P, cellStartP, pp, reach(P, pp, lim, SC_BINNED_P), [&](int j) {
-        int4 tin = pinfo[j];
-        if (!(tin.z & SC_ACTIVE) || tin.y != SC_PARTICLE_TYPE_LIPID) return;
+        if (!active_lipid(P, pinfo, j)) return;
         float4 t4 = ppos_[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
