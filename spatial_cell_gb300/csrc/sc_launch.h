@@ -117,6 +117,11 @@ struct ScLaunchCtx {
     ScBuffers *B;
     long long *launches;
     int gridCap;  // blocks of SC_THREADS resident on the whole device (grid-stride kernels)
+    // Two more streams for independent kernels of one phase: forked from st
+    // at `fork`, joined back into st through join[0..1] before the phase ends
+    // (null: everything runs on st).
+    cudaStream_t side[2];
+    cudaEvent_t fork, join[2];
 };
 void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic);
 void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac);

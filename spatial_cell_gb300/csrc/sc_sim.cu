@@ -186,6 +186,9 @@ struct sc_sim {
     ScBuffers B;
     cudaStream_t st = nullptr;
     cudaStream_t copySt = nullptr;          // frame copies to the host
+    cudaStream_t side[2] = {nullptr, nullptr};  // concurrent kernels of one phase (ScLaunchCtx)
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    bool forkClasses = false;               // run independent kernels of a phase on the side streams
     cudaEvent_t reduced[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
     int64_t frames = 0;                     // frames enqueued by sc_reduce_frame_async
     // One step as a CUDA graph, per host-side buffer state at the step's start
@@ -256,6 +259,11 @@ ScLaunchCtx ctx(sc_sim *s) {
     c.B = &s->B;
     c.launches = &s->launches;
     c.gridCap = s->gridCap;
+    c.side[0] = s->forkClasses ? s->side[0] : nullptr;
+    c.side[1] = s->forkClasses ? s->side[1] : nullptr;
+    c.fork = s->fork;
+    c.join[0] = s->join[0];
+    c.join[1] = s->join[1];
     return c;
 }
 
@@ -509,9 +517,12 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     {
         cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copySt, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
         for (int k = 0; k < 2 && e == cudaSuccess; k++) {
             e = cudaEventCreateWithFlags(&s->reduced[k], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copied[k], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join[k], cudaEventDisableTiming);
         }
         if (e != cudaSuccess) {
             sc_destroy(s);
@@ -537,6 +548,11 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.SP = P.S <= 4 ? 4 : P.S <= 8 ? 8 : 12;
     P.N = cfg->num_particles;
     P.Nm = cfg->num_metabolic_particles;
+    // Concurrent work classes pay off for a sim whose particles fill the
+    // device; smaller sims keep one stream, so many of them run side by side
+    // without the cross-stream joins (SC_FORK=0/1 overrides).
+    s->forkClasses = (int64_t)P.N >= (int64_t)s->gridCap * SC_THREADS;
+    if (const char *g = getenv("SC_FORK")) s->forkClasses = atoi(g) != 0;
     P.coordSteps = cfg->noise_coordination_steps;
     P.seed = cfg->seed;
     // SC_PAIR_LIST_LIMIT caps the pair lists (tests use it to run the
@@ -687,7 +703,10 @@ void sc_destroy(sc_sim *s) {
     for (int k = 0; k < 2; k++) {
         if (s->reduced[k]) cudaEventDestroy(s->reduced[k]);
         if (s->copied[k]) cudaEventDestroy(s->copied[k]);
+        if (s->side[k]) cudaStreamDestroy(s->side[k]);  // their work is joined into st
+        if (s->join[k]) cudaEventDestroy(s->join[k]);
     }
+    if (s->fork) cudaEventDestroy(s->fork);
     for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
     delete s;
 }

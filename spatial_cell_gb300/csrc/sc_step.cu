@@ -373,6 +373,7 @@ struct RelaxArgs {
 // kinds, 1 no bond partners, 2 collisions only (the class guarantees the
 // list holds no other kinds).  The bond loop reads the particle's bonds from
 // memory one at a time, so its body is emitted once.
+#define SC_PLAIN_GROUP 4
 template <bool SCAN, int MODE>
 __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4, float4 r4,
                                            float4 a4) {
@@ -506,6 +507,41 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
             uint32_t fl = pp_flags(P, IM, i, j, ppos, prad, phydro, B, A.pos, A.info);
             if (fl) body(j, fl);
         });
+    } else if (MODE == 2) {
+        // plain items list collisions only: the entries, then the
+        // neighbours' positions and velocities, of SC_PLAIN_GROUP pairs are
+        // loaded together, and the terms added in list order
+        const int c = A.L.cnt[i];
+        for (int k0 = 0; k0 < c; k0 += SC_PLAIN_GROUP) {
+            uint32_t e[SC_PLAIN_GROUP];
+            float4 t4[SC_PLAIN_GROUP], tv[SC_PLAIN_GROUP];
+#pragma unroll
+            for (int q = 0; q < SC_PLAIN_GROUP; q++)
+                e[q] = k0 + q < c ? A.L.list[sc_list_at(SC_LIST_PP, i, k0 + q)] : 0u;
+#pragma unroll
+            for (int q = 0; q < SC_PLAIN_GROUP; q++) {
+                t4[q] = make_float4(0, 0, 0, 0);
+                tv[q] = t4[q];
+                if (k0 + q < c) {
+                    const int j = (int)(e[q] & SC_PP_INDEX);
+                    t4[q] = A.pos[j];
+                    tv[q] = A.velIn[j];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < SC_PLAIN_GROUP; q++) {
+                if (k0 + q < c && (e[q] & SC_PP_COLLIDE)) {
+                    // dynamics.cuh:775-786
+                    const sc_f3 tpos = IM(sc_make_f3(t4[q].x, t4[q].y, t4[q].z));
+                    const float trad = t4[q].w;
+                    sc_f3 nd = normalize(tpos - ppos);
+                    float cd = prad + trad;
+                    sc_f3 tvel = sc_make_f3(tv[q].x, tv[q].y, tv[q].z);
+                    w += 1.0f;
+                    dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+                }
+            }
+        }
     } else {
         const int c = A.L.cnt[i];
         for (int k = 0; k < c; k++) {
@@ -904,12 +940,19 @@ __device__ __forceinline__ void metab_pair(const Imager &IM, sc_f3 pp, sc_f3 ppv
     dV += (tpos - nd * cd + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * k;
 }
 
-// Items whose list fits.  The next entry's neighbour data is loaded while the
-// current one is evaluated (the loop is bound by the latency of those loads).
+// One pair's neighbour velocity: a metabolic item's, or a lipid's.
+__device__ __forceinline__ float4 metab_pair_vel(const RelaxMArgs &A, uint32_t e) {
+    return ((e & SC_M_FROM_P) ? A.pvel : A.mvelIn)[e & SC_M_INDEX];
+}
+
 // Items whose list fits, in count order: each pair adds its precomputed
-// geometry and the neighbour's current velocity; the next pair's entry and
-// velocity are loaded while the current one is added.
-__global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, RelaxMArgs A) {
+// geometry and the neighbour's current velocity, in list order.  Pairs are
+// taken SC_METAB_GROUP at a time: the group's neighbour velocities and the
+// next group's entries are all in flight together, so a thread waits about
+// one memory latency per group instead of one per pair.  Entries are read
+// once per launch (evict-first); velocities are re-read by nearby items.
+#define SC_METAB_GROUP 4
+__global__ void __launch_bounds__(SC_THREADS, 3) k_relax_metab(ScParams P, RelaxMArgs A) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *A.nActivePtr) return;
     const int i = A.L.perm[g];
@@ -926,22 +969,30 @@ __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, Relax
     const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    const uint4 *__restrict__ pairs = A.pool + A.warpOff[g >> 5] + (g & 31);
-    uint4 E = c > 0 ? pairs[0] : make_uint4(0, 0, 0, 0);
-    float4 tv = c > 0 ? ((E.x & SC_M_FROM_P) ? A.pvel : A.mvelIn)[E.x & SC_M_INDEX] : make_float4(0, 0, 0, 0);
-    for (int k = 0; k < c; k++) {
-        uint4 En = E;
-        float4 tvn = tv;
-        if (k + 1 < c) {
-            En = pairs[(size_t)(k + 1) * 32];
-            tvn = ((En.x & SC_M_FROM_P) ? A.pvel : A.mvelIn)[En.x & SC_M_INDEX];
+    const uint4 *pairs = A.pool + A.warpOff[g >> 5] + (g & 31);
+    uint4 E[SC_METAB_GROUP];
+#pragma unroll
+    for (int q = 0; q < SC_METAB_GROUP; q++) E[q] = q < c ? __ldcs(pairs + (size_t)q * 32) : make_uint4(0, 0, 0, 0);
+    for (int k0 = 0; k0 < c; k0 += SC_METAB_GROUP) {
+        float4 tv[SC_METAB_GROUP];
+        uint4 En[SC_METAB_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) tv[q] = k0 + q < c ? metab_pair_vel(A, E[q].x) : make_float4(0, 0, 0, 0);
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) {
+            const int k = k0 + SC_METAB_GROUP + q;
+            En[q] = k < c ? __ldcs(pairs + (size_t)k * 32) : make_uint4(0, 0, 0, 0);
         }
-        const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
-        const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
-        w += kw;
-        dV += (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
-        E = En;
-        tv = tvn;
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) {
+            if (k0 + q < c) {
+                const float kw = (E[q].x & SC_M_FROM_P) ? 2.0f : 1.0f;
+                const sc_f3 a = sc_make_f3(__uint_as_float(E[q].y), __uint_as_float(E[q].z), __uint_as_float(E[q].w));
+                w += kw;
+                dV += (a + sc_make_f3(tv[q].x, tv[q].y, tv[q].z) - ppv) * 0.9f * kw;
+            }
+            E[q] = En[q];
+        }
     }
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
@@ -1967,11 +2018,26 @@ void sc_phase_relax(ScLaunchCtx &c) {
     PFields F = B.P(), X = B.Pnext();
     RelaxArgs A{B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds, pp_list(c),
                 F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg, B.classPP, B.ctr->ppClassCount};
-    // heaviest class first; each grid covers the class at most once
+    // The three classes write disjoint items and read only the input
+    // buffers: with side streams they run concurrently (bonded on st, the
+    // others on the side streams), so the classes fill each other's tails;
+    // each grid covers its class at most once.
     const int g = std::min(nblocks(c.P.N), c.gridCap);
+    const bool fork = c.side[0] != nullptr;
+    if (fork) {
+        cudaEventRecord(c.fork, c.st);
+        cudaStreamWaitEvent(c.side[0], c.fork, 0);
+        cudaStreamWaitEvent(c.side[1], c.fork, 0);
+    }
     k_relax<0><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
-    k_relax<1><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
-    k_relax<2><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
+    k_relax<2><<<g, SC_THREADS, 0, fork ? c.side[0] : c.st>>>(c.P, A);
+    k_relax<1><<<g, SC_THREADS, 0, fork ? c.side[1] : c.st>>>(c.P, A);
+    if (fork) {
+        cudaEventRecord(c.join[0], c.side[0]);
+        cudaEventRecord(c.join[1], c.side[1]);
+        cudaStreamWaitEvent(c.st, c.join[0], 0);
+        cudaStreamWaitEvent(c.st, c.join[1], 0);
+    }
     k_relax_overflow<<<std::min(nblocks(c.P.N), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfPP, &B.ctr->ovfPP);
     (*c.launches) += 3;
     B.cp[FP_VEL] ^= 1;

@@ -77,11 +77,14 @@ def test_whole_steps(product, species, periodic):
     assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
 
 
-@pytest.mark.parametrize("periodic,tiles", [(1, "1"), (0, "1"), (1, "0"), (0, "0")])
-def test_measured_workload_small(product, monkeypatch, periodic, tiles):
+@pytest.mark.parametrize("periodic,tiles,fork",
+                         [(1, "1", "0"), (0, "1", "0"), (1, "0", "0"), (0, "0", "0"), (1, "0", "1"), (0, "0", "1")])
+def test_measured_workload_small(product, monkeypatch, periodic, tiles, fork):
     """The measured workload's physics at a reduced size (same density), with
-    the metabolic sweeps on shared-memory tiles and on per-item lists."""
+    the metabolic sweeps on shared-memory tiles and on per-item lists, and
+    the particle work classes on one stream or forked onto three."""
     monkeypatch.setenv("SC_TILES", tiles)
+    monkeypatch.setenv("SC_FORK", fork)
     cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
                                  seed=3, periodic=periodic)
     rng = np.random.default_rng(3)
@@ -126,9 +129,12 @@ def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic, tiles):
     _same(cfg, gpu, cpu, f"2 steps with pair lists capped at {limit}")
 
 
-def test_step_graphs_equal_direct_launches(product, monkeypatch):
+@pytest.mark.parametrize("fork", ["0", "1"])
+def test_step_graphs_equal_direct_launches(product, monkeypatch, fork):
     """Steps replayed from captured CUDA graphs give the bytes of steps
-    launched phase by phase (several steps: both buffer parities replayed)."""
+    launched phase by phase (several steps: both buffer parities replayed),
+    with the particle work classes on one stream or forked onto three."""
+    monkeypatch.setenv("SC_FORK", fork)
     scene = scenes.test_scene(12, n=900, nm=1800, box=42.0, periodic=1)
     out = []
     for graphs in ("1", "0"):
