@@ -81,6 +81,7 @@ struct ScCounters {
     int ppClassCount[4];  // items per relax work class (k_build_pp)
     int ovfPP, ovfM;      // items whose particle / metabolic list overflowed (k_build_pp, k_build_m)
     int poolM;            // entries of the metabolic pair pool taken (k_build_m)
+    int poolLM;           // entries of the lipid-metabolic pair pool taken (k_build_lm)
 };
 
 // Relax work classes: items with bond partners in their list, items with

@@ -828,33 +828,33 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     });
 }
 
-// M pairs with their frozen geometry.  Positions do not change between the
-// sort and applyVelocities, so for every listed pair the part of the
-// reference's velocity term that depends on positions only,
-// A = tpos - normalize(tpos - pos) * collisionDistance (metabolites.cuh:
-// 196-203, 235-242), is the same in every relaxation sub-iteration.  It is
-// evaluated here, once per step, and each sub-iteration adds
-// ((A + tvel) - (pos + vel)) * 0.9 * weight: A is exactly the float3 the
-// reference's expression evaluates first, so sums and rounding are its own.
-// Layout: the pairs of a warp's 32 positions share one region of the pool,
-// entry k of lane l at warpOff[w] + 32 k + l, 16 bytes {neighbour | kind,
-// A.x, A.y, A.z}; a region is sized by the warp's longest list (its first
-// position: lists are count-ordered).  An overflowed item, or every item of
-// a block the pool has no room for, is listed in `ovf` for the scan.
-__device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int c, const uint32_t *scratch,
-                                             const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
-                                             uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
-                                             int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
-                                             int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
+// A pool position for the pairs of one count-ordered list position: the
+// block's items are ranked by count, each warp takes a region of
+// (its longest list) x 32 entries of the pool, and a list that does not fit
+// its capacity, or every list of a block the pool has no room for, is marked
+// overflowed (cnt = INT_MAX; listed in `ovf` when given).  Returns the item,
+// how many pairs to write and where its first one goes (entry k at
+// out[32 k]).
+struct PoolSlot {
+    int i, n;
+    uint4 *out;
+};
+template <int K>
+__device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int c, uint4 *__restrict__ pool,
+                                              int poolCap, int *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                              int *__restrict__ cnt, int *__restrict__ perm, int cap,
+                                              int *__restrict__ ovf, int *__restrict__ ovfCount) {
     __shared__ int s_n[SC_THREADS / 32];
     __shared__ int s_base;
     const int b0 = blockIdx.x * SC_THREADS, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     int src, cs;
-    count_rank<SC_LIST_M>(valid, c, &src, &cs);
-    const int limit = min(SC_LIST_M, P.listLimit);
+    count_rank<K>(valid, c, &src, &cs);
+    const int limit = min(K, P.listLimit);
     bool ovfl = cs > limit;
     int n = ovfl ? 0 : max(cs, 0);
-    if (lane == 0) s_n[warp] = n;  // the warp's longest stored list (descending order)
+    // the warp's longest stored list (overflowed lists rank first but store nothing)
+    const int wmax = __reduce_max_sync(0xffffffffu, n);
+    if (lane == 0) s_n[warp] = wmax;
     __syncthreads();
     if (t == 0) {
         int total = 0;
@@ -875,16 +875,42 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int 
         cnt[g] = ovfl ? INT_MAX : max(cs, 0);
         if (lane == 0) warpOff[g >> 5] = s_base < 0 ? 0 : off;
     }
-    if (ovfl) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
-    if (n == 0) return;
-    const int i = b0 + src;
+    if (ovfl && ovf) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
+    PoolSlot r;
+    r.i = b0 + src;
+    r.n = n;
+    r.out = pool + (n ? off : 0) + lane;
+    return r;
+}
+
+// M pairs with their frozen geometry.  Positions do not change between the
+// sort and applyVelocities, so for every listed pair the part of the
+// reference's velocity term that depends on positions only,
+// A = tpos - normalize(tpos - pos) * collisionDistance (metabolites.cuh:
+// 196-203, 235-242), is the same in every relaxation sub-iteration.  It is
+// evaluated here, once per step, and each sub-iteration adds
+// ((A + tvel) - (pos + vel)) * 0.9 * weight: A is exactly the float3 the
+// reference's expression evaluates first, so sums and rounding are its own.
+// Layout: the pairs of a warp's 32 positions share one region of the pool,
+// entry k of lane l at warpOff[w] + 32 k + l, 16 bytes {neighbour | kind,
+// A.x, A.y, A.z}; a region is sized by the warp's longest stored list.  An
+// overflowed item, or every item of a block the pool has no room for, is
+// listed in `ovf` for the scan.
+__device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int c, const uint32_t *scratch,
+                                             const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
+                                             uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
+                                             int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
+                                             int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
+    const PoolSlot S =
+        pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+    if (S.n == 0) return;
+    const int i = S.i;
     const float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w;
     CollisionDistCache cm, cp;
-    uint4 *__restrict__ out = pool + off + lane;
-    for (int k = 0; k < n; k++) {
+    for (int k = 0; k < S.n; k++) {
         const uint32_t e = scratch[sc_list_at(SC_LIST_M, i, k)];
         const int j = (int)(e & SC_M_INDEX);
         const bool fromP = (e & SC_M_FROM_P) != 0;
@@ -893,7 +919,7 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int 
         const sc_f3 nd = normalize(tpos - pp);
         const float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
         const sc_f3 a = tpos - nd * cd;
-        out[(size_t)k * 32] = make_uint4(e, __float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z));
+        S.out[(size_t)k * 32] = make_uint4(e, __float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z));
     }
 }
 
@@ -1317,12 +1343,20 @@ __device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t 
     });
 }
 
+// LM pairs with their frozen geometry, as the M pairs: per pair
+// A = tpos - normalize(tpos - pos) * collisionDistance
+// (metabolites.cuh:320-332), the first float3 the reference's velocity term
+// evaluates, in a pool region of the list position's warp (pool_take),
+// 16 bytes {neighbour, A.x, A.y, A.z} per entry.  An overflowed lipid
+// (cnt INT_MAX) is left to the scan of k_relax_partners.
 __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
                                                          const int *__restrict__ nActivePtr,
                                                          const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
                                                          const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-                                                         uint32_t *__restrict__ list, uint32_t *scratch,
-                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap) {
+                                                         uint4 *__restrict__ pool, int poolCap,
+                                                         int *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                                         uint32_t *scratch, int *__restrict__ cnt,
+                                                         int *__restrict__ perm, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
@@ -1331,14 +1365,33 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
         if ((in.z & SC_ACTIVE) && in.y == SC_PARTICLE_TYPE_LIPID)
             build_lm_item(P, cellStartM, i, ppos_, mpos, minfo, scratch, c);
     }
-    emit_count_ordered<SC_LIST_LM>(valid, c, P.listLimit, cap, scratch, list, cnt, perm);
+    const PoolSlot S =
+        pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr, nullptr);
+    if (S.n == 0) return;
+    const float4 p4 = ppos_[S.i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M);
+    const float prad = p4.w;
+    CollisionDistCache cc;
+    for (int k = 0; k < S.n; k++) {
+        const uint32_t j = scratch[sc_list_at(SC_LIST_LM, S.i, k)];
+        const float4 t4 = mpos[j];
+        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+        const sc_f3 nd = normalize(tpos - pp);
+        const sc_f3 a = tpos - nd * cc.get(prad, t4.w);
+        S.out[(size_t)k * 32] = make_uint4(j, __float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z));
+    }
 }
 
+// metabolites.cuh:267-340 for one lipid: each listed metabolic neighbour
+// adds its precomputed geometry and current velocity with weight 2, in list
+// order; the pairs are taken four at a time (entries, then velocities, all
+// in flight together).  An overflowed lipid scans its neighbourhood.
 __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     ScParams P, const uint32_t *__restrict__ cellStartM, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
-    PairList<SC_LIST_LM> L, const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-    const float4 *__restrict__ mvel) {
+    PairList<SC_LIST_LM> L, const uint4 *__restrict__ pool, const int *__restrict__ warpOff,
+    const float4 *__restrict__ mpos, const int4 *__restrict__ minfo, const float4 *__restrict__ mvel) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *nActivePtr) return;
     const int i = L.perm[g];
@@ -1347,45 +1400,46 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) return;
     float4 p4 = ppos_[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
-    const Imager IM(P, pp, SC_BINNED_M);
     const float prad = p4.w;
     float4 v4 = pvel_[i];
     const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
     sc_f3 dV = sc_zero3();
     float w = 0.0f;
-    CollisionDistCache cc;
-    auto body = [&](int j, float4 t4) {
-        sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
-        sc_f3 nd = normalize(tpos - pp);
-        float cd = cc.get(prad, t4.w);
-        w += 2.0f;
-        dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
-    };
     const int c = L.cnt[g];
     if (c <= min(SC_LIST_LM, P.listLimit)) {
-        // four entries per list load, their positions gathered together
-        const uint4 *__restrict__ chunks = sc_list4_chunks(L.list, SC_LIST_LM, g);
+        const uint4 *pairs = pool + warpOff[g >> 5] + (g & 31);
         for (int k0 = 0; k0 < c; k0 += 4) {
-            const uint4 E = chunks[(size_t)(k0 / 4) * 32];
-            const int e[4] = {(int)E.x, (int)E.y, (int)E.z, (int)E.w};
-            float4 t4[4];
+            uint4 E[4];
+            float4 tv[4];
 #pragma unroll
-            for (int kk = 0; kk < 4; kk++)
-                if (k0 + kk < c) t4[kk] = mpos[e[kk]];
+            for (int q = 0; q < 4; q++) E[q] = k0 + q < c ? __ldcs(pairs + (size_t)(k0 + q) * 32) : make_uint4(0, 0, 0, 0);
 #pragma unroll
-            for (int kk = 0; kk < 4; kk++) {
-                if (k0 + kk >= c) break;
-                body(e[kk], t4[kk]);
+            for (int q = 0; q < 4; q++) tv[q] = k0 + q < c ? mvel[E[q].x] : make_float4(0, 0, 0, 0);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (k0 + q < c) {
+                    const sc_f3 a = sc_make_f3(__uint_as_float(E[q].y), __uint_as_float(E[q].z), __uint_as_float(E[q].w));
+                    w += 2.0f;
+                    dV += (a + sc_make_f3(tv[q].x, tv[q].y, tv[q].z) - (pp + pv)) * 0.9f * 2.0f;
+                }
             }
         }
     } else {
+        const Imager IM(P, pp, SC_BINNED_M);
+        CollisionDistCache cc;
         const float lim = P.maxInt;
         scan27(P, cellStartM, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
             if (!active_m(P, minfo, j)) return;
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
-            if (sc_norm3(delta) <= cc.get(prad, t4.w)) body(j, t4);
+            const float cd = cc.get(prad, t4.w);
+            if (sc_norm3(delta) <= cd) {
+                sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+                sc_f3 nd = normalize(tpos - pp);
+                w += 2.0f;
+                dV += (tpos - nd * cd + ld3(mvel, j) - (pp + pv)) * 0.9f * 2.0f;
+            }
         });
     }
     st3(pvel_, i, pv + dV / fmaxf(w, 1.0f), v4.w);
@@ -2108,8 +2162,11 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     PFields F = B.P();
     if (!B.validLM) {
         if (B.scratchLM == B.listD) B.validD = false;
-        k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos,
-                                                             M.info, B.listLM, B.scratchLM, B.cntLM, B.permLM, c.P.N);
+        cudaMemsetAsync(&B.ctr->poolLM, 0, sizeof(int), c.st);
+        k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
+            c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos, M.info, reinterpret_cast<uint4 *>(B.listLM),
+            (int)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,
+            c.P.N);
         (*c.launches)++;
         B.validLM = true;
     }
@@ -2119,7 +2176,8 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     L.cap = c.P.N;
     L.perm = B.permLM;
     k_relax_partners<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
-                                                               F.vel, L, M.pos, M.info, M.vel);
+                                                               F.vel, L, reinterpret_cast<const uint4 *>(B.listLM),
+                                                               B.warpOffLM, M.pos, M.info, M.vel);
     (*c.launches)++;
 }
 
