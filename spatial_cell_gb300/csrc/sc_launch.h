@@ -42,6 +42,11 @@ struct ScBuffers {
     uint32_t *listPP, *listM, *listLM, *listD;
     int *cntPP, *cntM, *cntLM, *cntD;
     int *classPP;  // SC_RELAX_CLASSES segments of N item indices
+    // Bond matches of the particle list: per bonded item, up to
+    // SC_MAX_ACTIVE_INTERACTIONS entries (neighbour | bond slot << 29), in
+    // list order then bond-slot order, and their count (k_build_pp).
+    uint32_t *matchPP;
+    int *matchN;
     int *permM, *permLM, *permD;  // count-ordered list position -> item
     uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
     int *ovfPP, *ovfM;            // overflowed items

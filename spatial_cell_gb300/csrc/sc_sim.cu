@@ -663,6 +663,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.redP2, N)) || (rc = dalloc(s, &B.redM2, Nm)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
         (rc = dalloc(s, &B.cntPP, N)) ||
         (rc = dalloc(s, &B.classPP, (size_t)SC_RELAX_CLASSES * N)) ||
+        (rc = dalloc(s, &B.matchPP, (size_t)SC_MAX_ACTIVE_INTERACTIONS * N)) || (rc = dalloc(s, &B.matchN, N)) ||
         (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
         (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||

@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
                                                          const int *__restrict__ nb, const int *__restrict__ bonds,
                                                          uint32_t *__restrict__ list, int *__restrict__ cnt, int cap,
                                                          int *__restrict__ classIdx, int *__restrict__ classCount,
-                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
+                                                         int *__restrict__ ovf, int *__restrict__ ovfCount,
+                                                         uint32_t *__restrict__ match, int *__restrict__ matchN) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
     int4 in = info[i];
@@ -240,17 +241,26 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
         const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
         const Imager IM(P, ppos, SC_BINNED_P);
         const int phydro = (int)(int8_t)(in.w & 0xff);
-        int c = 0;
+        int c = 0, nm = 0;
         uint32_t any = 0;
+        uint32_t *__restrict__ myMatch = match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
         scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
             uint32_t f = pp_flags(P, IM, i, j, ppos, p4.w, phydro, B, pos, info);
             if (f) {
                 if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
                 c++;
                 any |= f;
+                if (f & SC_PP_PARTNER) {  // the bond slots naming this neighbour, in slot order
+                    const int tid_ = info[j].x;
+#pragma unroll
+                    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
+                        if (k < B.n && B.p[k] == tid_ && nm < SC_MAX_ACTIVE_INTERACTIONS)
+                            myMatch[nm++] = (uint32_t)j | ((uint32_t)k << 29);
+                }
             }
         });
         cnt[i] = c;
+        if (B.n >= 1) matchN[i] = nm;
         if (c > min(SC_LIST_PP, P.listLimit)) ovf[atomicAdd(ovfCount, 1)] = i;
         if (B.n >= 1) cls = 0;
         else if (c <= min(SC_LIST_PP, P.listLimit) && (any & SC_PP_POLAR)) cls = 1;
@@ -289,19 +299,21 @@ __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__rest
 }
 
 // ---- dynamics.cuh:288-402 coordinateNoise -----------------------------------
-// Only interaction partners change anything; they are the PARTNER entries of
-// the particle-particle list, in the reference's visiting order.
-// dynamics.cuh:288-402 for one particle.
+// Only interaction partners change anything: for a listed item they are its
+// bond matches (k_build_pp), in the reference's visiting order; an item
+// whose list overflowed scans its neighbourhood.
+// dynamics.cuh:288-402 for one particle; the new noise goes to pnOut / anOut.
 __device__ __forceinline__ void coordinate_noise_item(
     const ScParams &P, const uint32_t *__restrict__ cellStart, int i, const float4 *__restrict__ pos,
     const int4 *__restrict__ info, const int *__restrict__ nb, const int *__restrict__ bonds,
-    const PairList<SC_LIST_PP> &L, const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn,
-    float4 *__restrict__ pnOut, float4 *__restrict__ anOut, float frac) {
+    const PairList<SC_LIST_PP> &L, const uint32_t *__restrict__ match, const int *__restrict__ matchN,
+    const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn, float4 *__restrict__ pnOut,
+    float4 *__restrict__ anOut, float frac) {
     int4 in = info[i];
     float4 pn4 = pnIn[i], an4 = anIn[i];
     if (!(in.z & SC_ACTIVE) || nb[i] < 1) {
-        pnOut[i] = pn4;
-        anOut[i] = an4;
+        *pnOut = pn4;
+        *anOut = an4;
         return;
     }
     const int nbi = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
@@ -314,42 +326,70 @@ __device__ __forceinline__ void coordinate_noise_item(
     sc_f3 dPN = sc_zero3();
     sc_f4 dAN = sc_qid();
     float w = 0.0f;
-    for_pp(P, cellStart, L, i, ppos, prad, (int)(int8_t)(in.w & 0xff), nb, bonds, pos, info, [&](int j, uint32_t fl) {
-        if (!(fl & SC_PP_PARTNER)) return;
-        const int tid_ = info[j].x;
+    // one bond slot k naming neighbour j
+    auto term = [&](int j, int k) {
+        if (myBonds[3 * k] < 10 && frac > 0.25f) return;
         const float trad = pos[j].w;
-#pragma unroll 1
-        for (int k = 0; k < nbi; k++) {
-            if (myBonds[3 * k] < 10 && frac > 0.25f) continue;
-            if (myBonds[3 * k + 2] == tid_) {
-                sc_f3 tpn = ld3(pnIn, j);
-                sc_f4 tan_ = ld4(anIn, j);
-                float pMag = length(ppn);
-                dPN += (tpn - ppn) * 0.9f * trad / (prad + trad) * 1.0f;
-                dPN *= fmaxf(length(dPN), pMag) / length(dPN);
-                dAN = sc_slerp(dAN, sc_qmul(sc_qinv(pan), tan_), 0.9f * trad / (prad + trad) * 1.0f);
-                w += 1.0f;
-            }
+        sc_f3 tpn = ld3(pnIn, j);
+        sc_f4 tan_ = ld4(anIn, j);
+        float pMag = length(ppn);
+        dPN += (tpn - ppn) * 0.9f * trad / (prad + trad) * 1.0f;
+        dPN *= fmaxf(length(dPN), pMag) / length(dPN);
+        dAN = sc_slerp(dAN, sc_qmul(sc_qinv(pan), tan_), 0.9f * trad / (prad + trad) * 1.0f);
+        w += 1.0f;
+    };
+    if (L.cnt[i] <= min(SC_LIST_PP, P.listLimit)) {
+        const uint32_t *__restrict__ myMatch = match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
+        const int nm = matchN[i];
+        for (int m = 0; m < nm; m++) {
+            const uint32_t e = myMatch[m];
+            term((int)(e & SC_PP_INDEX), (int)(e >> 29));
         }
-    });
+    } else {
+        for_pp(P, cellStart, L, i, ppos, prad, (int)(int8_t)(in.w & 0xff), nb, bonds, pos, info,
+               [&](int j, uint32_t fl) {
+                   if (!(fl & SC_PP_PARTNER)) return;
+                   const int tid_ = info[j].x;
+#pragma unroll 1
+                   for (int k = 0; k < nbi; k++)
+                       if (myBonds[3 * k + 2] == tid_) term(j, k);
+               });
+    }
     ppn += dPN / fmaxf(w, 1.0f);
     pan = sc_qmul(sc_slerp(sc_qid(), dAN, 1.0f / fmaxf(w, 1.0f)), pan);
-    st3(pnOut, i, ppn, pn4.w);
-    st4(anOut, i, pan);
+    st3(pnOut, 0, ppn, pn4.w);
+    st4(anOut, 0, pan);
 }
 
 
-// Runs over the bonded work class (items with at least one bond); the
-// launcher copies every other item's noise to the output buffers first.
+// Runs over the bonded work class (items with at least one bond), the new
+// noise of class position t going to pnTmp[t] / anTmp[t]; every other
+// item's noise is unchanged.
 __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ classIdx,
     const int *__restrict__ classCount, const float4 *__restrict__ pos, const int4 *__restrict__ info,
     const int *__restrict__ nb, const int *__restrict__ bonds, PairList<SC_LIST_PP> L,
-    const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn, float4 *__restrict__ pnOut,
-    float4 *__restrict__ anOut, float frac) {
+    const uint32_t *__restrict__ match, const int *__restrict__ matchN, const float4 *__restrict__ pnIn,
+    const float4 *__restrict__ anIn, float4 *__restrict__ pnTmp, float4 *__restrict__ anTmp, float frac) {
     const int n0 = classCount[0];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n0; t += gridDim.x * blockDim.x)
-        coordinate_noise_item(P, cellStart, classIdx[t], pos, info, nb, bonds, L, pnIn, anIn, pnOut, anOut, frac);
+        coordinate_noise_item(P, cellStart, classIdx[t], pos, info, nb, bonds, L, match, matchN, pnIn, anIn,
+                              pnTmp + t, anTmp + t, frac);
+}
+
+// The bonded class's new noise written back in place (after every read of
+// the old values).
+__global__ void __launch_bounds__(SC_THREADS) k_noise_writeback(const int *__restrict__ classIdx,
+                                                                const int *__restrict__ classCount,
+                                                                const float4 *__restrict__ pnTmp,
+                                                                const float4 *__restrict__ anTmp,
+                                                                float4 *__restrict__ pn, float4 *__restrict__ an) {
+    const int n0 = classCount[0];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n0; t += gridDim.x * blockDim.x) {
+        const int i = classIdx[t];
+        pn[i] = pnTmp[t];
+        an[i] = anTmp[t];
+    }
 }
 
 // ---- dynamics.cuh:405-822 relax ------------------------------------------------
@@ -365,6 +405,8 @@ struct RelaxArgs {
     float4 *__restrict__ velOut, *__restrict__ rotOut, *__restrict__ avOut, *__restrict__ dbg;
     const int *__restrict__ classIdx;    // items by work class (k_build_pp)
     const int *__restrict__ classCount;
+    const uint32_t *__restrict__ match;  // bond matches of the list (k_build_pp)
+    const int *__restrict__ matchN;
 };
 
 // One particle's relaxation.  SCAN = false reads the particle's pair list;
@@ -563,12 +605,12 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
 
 // A bonded particle's relaxation (work class 0, list path).  The pose terms
 // of its rule and chain bonds do not depend on the running sums, so they are
-// evaluated first, bond by bond in the order the reference meets them, with
-// every lane of a warp on its own first bond, then its second ...; the list
-// is then walked once more to add every term in the reference's order (the
-// slerps of dAV and the float sums are order-dependent).  A test bond rotates
-// the particle itself, which later terms read: such particles take the
-// in-order path.
+// evaluated first, from its bond matches (k_build_pp records them in the
+// order the reference meets them), with every lane of a warp on its own
+// first bond, then its second ...; the list is then walked once more to add
+// every term in the reference's order (the slerps of dAV and the float sums
+// are order-dependent).  A test bond rotates the particle itself, which
+// later terms read: such particles take the in-order path.
 struct BondTerm {
     sc_f3 dv;   // velocity term
     sc_f4 q;    // dAV slerp target
@@ -597,18 +639,16 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
     const sc_f3 nextUp = sc_rotate(up, pav);
     const float flex = SC_PI_REF / 8;
     const int c = A.L.cnt[i];
-    // 1. the partner entries of the list
-    int pj[SC_MAX_ACTIVE_INTERACTIONS];
-    int np = 0;
-    for (int k = 0; k < c; k++) {
-        const uint32_t e = A.L.list[sc_list_at(SC_LIST_PP, i, k)];
-        if ((e & SC_PP_PARTNER) && np < SC_MAX_ACTIVE_INTERACTIONS) pj[np++] = (int)(e & SC_PP_INDEX);
-    }
-    // 2. their bonds' terms, in list order, then bond-slot order
+    // 1. the terms of its bond matches (list order, then bond-slot order)
+    const uint32_t *__restrict__ myMatch = A.match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
+    const int nm = min(A.matchN[i], SC_MAX_ACTIVE_INTERACTIONS);
     BondTerm T[SC_MAX_ACTIVE_INTERACTIONS];
     int nt = 0;
-    for (int q = 0; q < np; q++) {
-        const int j = pj[q];
+    for (int m = 0; m < nm; m++) {
+        const uint32_t me = myMatch[m];
+        const int j = (int)(me & SC_PP_INDEX), k = (int)(me >> 29);
+        const int it = myBonds[3 * k];
+        if (!(it >= 10 || it == SC_INTERACTION_TYPE_CHAIN) || nt >= SC_MAX_ACTIVE_INTERACTIONS) continue;
         const int4 tin = A.info[j];
         const int tid_ = tin.x, ttype = tin.y;
         const float4 t4 = A.pos[j];
@@ -616,57 +656,50 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
         const float trad = t4.w, idist = prad + trad;
         const sc_f4 trot = ld4(A.rotIn, j), tav = ld4(A.avIn, j);
         const sc_f3 tvel = ld3(A.velIn, j);
-#pragma unroll 1
-        for (int k = 0; k < nbi; k++) {
-            if (myBonds[3 * k + 2] != tid_) continue;
-            const int it = myBonds[3 * k];
-            if (it >= 10 && nt < SC_MAX_ACTIVE_INTERACTIONS) {
-                // dynamics.cuh:591-655
-                const sc_rule &pii = rule_at(P, it);
-                sc_f4 ro = rule_ori(pii);
-                sc_f3 rp = rule_pos(pii);
-                bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
-                sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
-                sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
-                sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
-                sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
-                BondTerm &b = T[nt++];
-                b.q = sc_qmul(sc_slerp(rro, orro, 0.5f), rro);
-                b.t = 0.9f * trad / (prad + trad);
-                sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot)))
-                               : sc_rotate(rp, sc_qmul(tav, trot));
-                rrp += tpos;
-                sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot)))
-                                : sc_rotate(rp, sc_qmul(pav, prot));
-                orrp += ppos;
-                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
-                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
-                b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
-            } else if (it == SC_INTERACTION_TYPE_CHAIN && nt < SC_MAX_ACTIVE_INTERACTIONS) {
-                // dynamics.cuh:692-769
-                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), trot), pav);
-                sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
-                bool fwd = myBonds[3 * k + 1] == SC_INTERACTION_GROUP_FORWARD;
-                BondTerm &b = T[nt++];
-                b.q = sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd);
-                b.t = 0.9f * trad / (prad + trad);
-                sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
-                sc_f3 axis = sc_safe_cross(relUp, -nnd);
-                float ang = sc_angle3(relUp, -nnd);
-                sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
-                rrp *= idist;
-                rrp += tpos;
-                sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
-                sc_f3 oaxis = sc_safe_cross(oUp, nnd);
-                float oang = sc_angle3(oUp, nnd);
-                sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
-                orrp *= idist;
-                orrp += ppos;
-                sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
-                sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
-                b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
-                b.dbg = rrp - ppos;
-            }
+        if (it >= 10) {
+            // dynamics.cuh:591-655
+            const sc_rule &pii = rule_at(P, it);
+            sc_f4 ro = rule_ori(pii);
+            sc_f3 rp = rule_pos(pii);
+            bool o1 = p_order(ptype, pid, ttype, tid_), o2 = p_order(ttype, tid_, ptype, pid);
+            sc_f4 tro_p = o1 ? sc_qmul(trot, sc_qinv(ro)) : sc_qmul(trot, ro);
+            sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
+            sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
+            sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
+            BondTerm &b = T[nt++];
+            b.q = sc_qmul(sc_slerp(rro, orro, 0.5f), rro);
+            b.t = 0.9f * trad / (prad + trad);
+            sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot))) : sc_rotate(rp, sc_qmul(tav, trot));
+            rrp += tpos;
+            sc_f3 orrp = o2 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(pav, prot))) : sc_rotate(rp, sc_qmul(pav, prot));
+            orrp += ppos;
+            sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+            sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+            b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+        } else {
+            // dynamics.cuh:692-769
+            sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), trot), pav);
+            sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
+            bool fwd = myBonds[3 * k + 1] == SC_INTERACTION_GROUP_FORWARD;
+            BondTerm &b = T[nt++];
+            b.q = sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd);
+            b.t = 0.9f * trad / (prad + trad);
+            sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
+            sc_f3 axis = sc_safe_cross(relUp, -nnd);
+            float ang = sc_angle3(relUp, -nnd);
+            sc_f3 rrp = sc_rotate(relUp, sc_quat(axis, fminf(fmaxf(ang, -flex), flex)));
+            rrp *= idist;
+            rrp += tpos;
+            sc_f3 oUp = (fwd ? -1.0f : 1.0f) * nextUp;
+            sc_f3 oaxis = sc_safe_cross(oUp, nnd);
+            float oang = sc_angle3(oUp, nnd);
+            sc_f3 orrp = sc_rotate(oUp, sc_quat(oaxis, fminf(fmaxf(oang, -flex), flex)));
+            orrp *= idist;
+            orrp += ppos;
+            sc_f3 pDV = (rrp + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+            sc_f3 tpDV = (orrp + pvel - (tpos + tvel)) * 0.9f * prad / (prad + trad) * 1.0f;
+            b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
+            b.dbg = rrp - ppos;
         }
     }
     // 3. every term in the reference's order
@@ -677,7 +710,7 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
     sc_f3 phobPos = sc_zero3();
     float phobSum = 0.0f;
     float w = 0.0f;
-    int ut = 0;
+    int ut = 0, mi = 0;
     for (int kk = 0; kk < c; kk++) {
         const uint32_t fl = A.L.list[sc_list_at(SC_LIST_PP, i, kk)];
         const int j = (int)(fl & SC_PP_INDEX);
@@ -698,10 +731,9 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
             phobPos += tpPV * pap;
         }
         if (fl & SC_PP_PARTNER) {
-            const int tid_ = A.info[j].x;
-#pragma unroll 1
-            for (int k = 0; k < nbi; k++) {
-                if (myBonds[3 * k + 2] != tid_) continue;
+            // this neighbour's bond matches are the next ones in order
+            for (; mi < nm && (int)(myMatch[mi] & SC_PP_INDEX) == j; mi++) {
+                const int k = (int)(myMatch[mi] >> 29);
                 const int it = myBonds[3 * k];
                 if ((it >= 10 || it == SC_INTERACTION_TYPE_CHAIN) && ut < nt) {
                     const BondTerm &b = T[ut++];
@@ -2020,7 +2052,8 @@ static void ensure_pp(ScLaunchCtx &c) {
     cudaMemsetAsync(&B.ctr->ovfPP, 0, sizeof(int), c.st);
     k_build_pp<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
                                                          F.bonds, B.listPP, B.cntPP, c.P.N, B.classPP,
-                                                         B.ctr->ppClassCount, B.ovfPP, &B.ctr->ovfPP);
+                                                         B.ctr->ppClassCount, B.ovfPP, &B.ctr->ovfPP, B.matchPP,
+                                                         B.matchN);
     (*c.launches)++;
     B.validPP = true;
 }
@@ -2038,15 +2071,16 @@ void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     ensure_pp(c);
+    // the other buffers of the two noise fields hold the bonded class's new
+    // values by class position until they are written back in place
     PFields F = B.P(), X = B.Pnext();
-    cudaMemcpyAsync(X.posnoise, F.posnoise, (size_t)c.P.N * sizeof(float4), cudaMemcpyDeviceToDevice, c.st);
-    cudaMemcpyAsync(X.angnoise, F.angnoise, (size_t)c.P.N * sizeof(float4), cudaMemcpyDeviceToDevice, c.st);
-    k_coordinate_noise<<<std::min(nblocks(c.P.N), c.gridCap), SC_THREADS, 0, c.st>>>(
-        c.P, B.cellStartP, B.classPP, B.ctr->ppClassCount, F.pos, F.info, F.nb, F.bonds, pp_list(c), F.posnoise,
-        F.angnoise, X.posnoise, X.angnoise, frac);
-    B.cp[FP_POSNOISE] ^= 1;
-    B.cp[FP_ANGNOISE] ^= 1;
-    (*c.launches)++;
+    const int g = std::min(nblocks(c.P.N), c.gridCap);
+    k_coordinate_noise<<<g, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.classPP, B.ctr->ppClassCount, F.pos, F.info,
+                                                    F.nb, F.bonds, pp_list(c), B.matchPP, B.matchN, F.posnoise,
+                                                    F.angnoise, X.posnoise, X.angnoise, frac);
+    k_noise_writeback<<<g, SC_THREADS, 0, c.st>>>(B.classPP, B.ctr->ppClassCount, X.posnoise, X.angnoise,
+                                                   F.posnoise, F.angnoise);
+    (*c.launches) += 2;
 }
 
 void sc_phase_apply_noise(ScLaunchCtx &c) {
@@ -2071,7 +2105,8 @@ void sc_phase_relax(ScLaunchCtx &c) {
     ensure_pp(c);
     PFields F = B.P(), X = B.Pnext();
     RelaxArgs A{B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb, F.bonds, pp_list(c),
-                F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg, B.classPP, B.ctr->ppClassCount};
+                F.vel, F.rot, F.angvel, X.vel, X.rot, X.angvel, F.dbg, B.classPP, B.ctr->ppClassCount,
+                B.matchPP, B.matchN};
     // The three classes write disjoint items and read only the input
     // buffers: with side streams they run concurrently (bonded on st, the
     // others on the side streams), so the classes fill each other's tails;
