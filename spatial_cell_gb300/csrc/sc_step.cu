@@ -1010,13 +1010,15 @@ __device__ __forceinline__ float4 metab_pair_vel(const RelaxMArgs &A, uint32_t e
 // one memory latency per group instead of one per pair.  Entries are read
 // once per launch (evict-first); velocities are re-read by nearby items.
 #define SC_METAB_GROUP 4
-__global__ void __launch_bounds__(SC_THREADS, 3) k_relax_metab(ScParams P, RelaxMArgs A) {
+__global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, RelaxMArgs A) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *A.nActivePtr) return;
     const int i = A.L.perm[g];
     if (i < 0) return;
     const float4 v4 = A.mvelIn[i];
-    if (!(A.minfo[i].z & SC_ACTIVE)) {
+    // after the sort the active items are exactly the binned ones
+    const bool act = P.mAllActive ? i < (int)A.cellStartM[P.cells] : (A.minfo[i].z & SC_ACTIVE) != 0;
+    if (!act) {
         A.mvelOut[i] = v4;
         return;
     }
@@ -1881,7 +1883,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
         float4 v = metIn[(size_t)i * Q + q];
         pm[4 * q] = v.x; pm[4 * q + 1] = v.y; pm[4 * q + 2] = v.z; pm[4 * q + 3] = v.w;
     }
-    if (!(info[i].z & SC_ACTIVE)) {
+    // after the sort the active items are exactly the binned ones
+    const bool act = P.mAllActive ? i < (int)cellStart[P.cells] : (info[i].z & SC_ACTIVE) != 0;
+    if (!act) {
 #pragma unroll
         for (int q = 0; q < Q; q++) metOut[(size_t)i * Q + q] = metIn[(size_t)i * Q + q];
         return;
