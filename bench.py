@@ -316,6 +316,59 @@ def serving_sample(args, capacity):
                       "(scaled down from 10,000 requests of up to 1M particles and 5,000 steps)"}
 
 
+def vesicle_sample(args, native, torch):
+    """The crowded vesicle case (walled 900 nm box: 2 M lipids on a 400 nm
+    bilayer shell, 6 M interior particles, 50 k 20-particle lattice complexes,
+    32 M metabolic items; counts scaled by --vesicle-scale), generated on the
+    device: particle-steps/s over --vesicle-steps steps after a warm-up step,
+    and the same with 4 replicas stepping together when the device has room
+    for them.  Wall clock with the device synchronised on both sides."""
+    cfg, groups, nm = scenes.vesicle_workload(args.vesicle_scale)
+    items = cfg.num_particles + nm
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+
+    def make(seed):
+        s = native.Simulation(cfg, types, rules)
+        s.generate_scene(groups, nm, seed)
+        s.prepare()
+        s.step(1)  # warm-up: captures the step graphs
+        s.sync()
+        return s
+
+    sims = [make(cfg.seed)]
+    free1, _ = torch.cuda.mem_get_info()
+    per_sim = free0 - free1
+    k = args.vesicle_steps
+    t0 = time.perf_counter()
+    sims[0].step(k)
+    sims[0].sync()
+    one = items * k / (time.perf_counter() - t0)
+    out = {"scale": args.vesicle_scale, "particles": cfg.num_particles, "metabolic_particles": nm,
+           "box_nm": cfg.sim_size, "walls": True, "steps": k, "value": one, "unit": UNIT,
+           "device_bytes_per_sim": per_sim,
+           "scene": "2 leaflets r=400/396 nm (lipids uniform on each sphere), dummy/A/B 70/15/15 in the ball "
+                    "r<390 nm, 20-site lattice complexes (3 nm, tree of chain bonds) in r<384 nm, metabolic "
+                    "uniform in the box; generated on the device (sc_generate_scene), seed 5",
+           "timing": "wall clock, device synchronised before and after"}
+    if 3 * per_sim < 0.9 * free1:
+        sims += [make(cfg.seed + r) for r in range(1, 4)]
+        t0 = time.perf_counter()
+        for _ in range(k):
+            for s in sims:
+                s.step(1)
+        for s in sims:
+            s.sync()
+        out["replicas4"] = {"value": 4 * items * k / (time.perf_counter() - t0), "unit": UNIT}
+    else:
+        out["replicas4"] = {"not_run": f"4 replicas need {4 * per_sim / 1e9:.0f} GB of device memory, "
+                                       f"{free0 / 1e9:.0f} GB were free"}
+    for s in sims:
+        s.close()
+    return out
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
@@ -441,6 +494,7 @@ def run_ours(args):
     batched = batched_sample(args, native, torch) if args.batch_replicas > 0 and world == 1 else None
     served = (serving_sample(args, batched["value"] if batched else value)
               if args.serve_requests > 0 and world == 1 else None)
+    vesicle = vesicle_sample(args, native, torch) if args.vesicle_scale > 0 and world == 1 else None
 
     line = None
     if rank == 0:
@@ -475,6 +529,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "batched": batched,
             "serving": served,
+            "vesicle": vesicle,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -495,6 +550,9 @@ def main():
                     help="replica cells in the batched sample (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=4)
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving sample (0: skip it)")
+    ap.add_argument("--vesicle-scale", type=float, default=1.0,
+                    help="count scale of the vesicle sample (0: skip it)")
+    ap.add_argument("--vesicle-steps", type=int, default=3)
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()

@@ -268,6 +268,10 @@ int sc_sync(sc_sim *sim);
  * metabolic relaxation, out[2] lipid-metabolic, out[3] diffusion; -1 for a
  * list not built since its inputs last changed.  Waits for the sim. */
 int sc_pair_counts(sc_sim *sim, int64_t out[4]);
+/* Items whose pair list overflowed its capacity (they take the scan paths),
+ * per list in the order of sc_pair_counts; -1 for a list not built since its
+ * inputs last changed.  Waits for the sim. */
+int sc_list_overflows(sc_sim *sim, int64_t out[4]);
 /* 1 when all work enqueued on the sim has finished, 0 while some is still
  * running (does not wait; for loops that drive many sims at once). */
 int sc_idle(sc_sim *sim);
@@ -338,6 +342,61 @@ int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info
  * Counters as sc_load_state with step 0 and next particle id n. */
 int sc_generate_uniform(sc_sim *sim, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
                         int32_t nkinds, uint64_t seed);
+
+/* Structured scenes: the particles are a list of groups, generated on the
+ * device one after another (group g's particles follow group g-1's; ids are
+ * indices), the metabolic particles as in sc_generate_uniform.  Group kinds
+ * restate the reference's host setup helpers (setup/particle_setup.cuh,
+ * setup/interaction_setup.cuh) with counter-based draws in place of its
+ * std::mt19937 stream:
+ *   UNIFORM_BOX      count particles uniform in the box (fillParticlesUniform)
+ *   UNIFORM_BALL     count particles uniform in the ball (center, radius)
+ *   SPHERE_SHELL     count particles uniform on the sphere (center, radius),
+ *                    oriented quaternionFromTo(up, radial) * rot as
+ *                    fillParticlesSphere orients them
+ *   FIBONACCI_SHELL  fillParticlesSphere: count points of the Fibonacci
+ *                    spiral on the sphere; radius <= 0 takes the
+ *                    reference's count-based radius
+ *   COMPLEXES        count complexes of unit particles on a random patch of
+ *                    the cubic lattice of the given spacing (grown site by
+ *                    site from a neighbour of an earlier site), one random
+ *                    orientation per complex, centre uniform in the ball;
+ *                    each site bonded to the site it grew from
+ *   WRAPPED_CHAINS   count chains of unit particles (fillParticlesWrappedChain,
+ *                    each member's step -(radius of type id t-1 + radius of
+ *                    t) along its up vector, its orientation slerped 0.3 of
+ *                    the way to a random one), start uniform in the ball,
+ *                    linked serially (linkParticlesSerially)
+ * Member types are drawn from the group's mix (kinds / fractions), except
+ * chains, whose member k has kind k % nkinds.  Bonds use interaction type
+ * link_type with group FORWARD on the earlier particle and BACKWARD on the
+ * later one.  Positions are clamped into [0, sim_size] as the reference's
+ * helpers clamp them. */
+#define SC_SCENE_UNIFORM_BOX 0
+#define SC_SCENE_UNIFORM_BALL 1
+#define SC_SCENE_SPHERE_SHELL 2
+#define SC_SCENE_FIBONACCI_SHELL 3
+#define SC_SCENE_COMPLEXES 4
+#define SC_SCENE_WRAPPED_CHAINS 5
+#define SC_SCENE_MAX_UNIT 64
+
+typedef struct sc_scene_group {
+    int32_t kind;          /* SC_SCENE_* */
+    int32_t count;         /* particles, or complexes / chains */
+    int32_t unit;          /* particles per complex / chain (<= SC_SCENE_MAX_UNIT) */
+    int32_t nkinds;        /* 1 .. 4 */
+    int32_t kinds[4];      /* type ids */
+    float fractions[4];    /* relative weights */
+    float center[3];
+    float radius;          /* ball / sphere radius */
+    float spacing;         /* complex lattice spacing */
+    float rot[4];          /* shells: base orientation (x, y, z, w) */
+    int32_t link_type;     /* interaction type of complex / chain bonds */
+} sc_scene_group;
+
+/* Fills the sim with the groups' particles (their total must fit its
+ * capacity) and nm metabolic particles; counters as sc_generate_uniform. */
+int sc_generate_scene(sc_sim *sim, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed);
 
 /* ---- checkpoint / resume (no counterpart in the reference) ----
  * A checkpoint holds the whole state -- the active particle and metabolic

@@ -162,3 +162,22 @@ def generate_uniform(n, nm, kinds, fractions, types, box, species, seed):
     if rc != 0:
         raise ValueError("bad mix")
     return p[:n], m[:nm]
+
+
+def generate_scene(groups, nm, types, box, species, seed):
+    """The structured scene generator's records built by the CPU oracle
+    (spatial_cell_gb300/csrc/sc_gen.h): (particles, metabolic) arrays."""
+    lib = ctypes.CDLL(build.build_port())
+    f = lib.scp_generate_scene
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_float,
+                  ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    g = np.ascontiguousarray(np.concatenate([np.atleast_1d(x) for x in groups]), abi.SCENE_GROUP_DTYPE)
+    t = np.ascontiguousarray(types, abi.TYPE_INFO_DTYPE)
+    n = f(g.ctypes.data, len(g), nm, t.ctypes.data, len(t), box, species, seed, None, None)
+    if n < 0:
+        raise ValueError("invalid scene groups")
+    p = np.zeros(max(n, 1), abi.PARTICLE_DTYPE)
+    m = np.zeros(max(nm, 1), abi.METABOLIC_DTYPE)
+    f(g.ctypes.data, len(g), nm, t.ctypes.data, len(t), box, species, seed, p.ctypes.data, m.ctypes.data)
+    return p[:n], m[:nm]

@@ -858,6 +858,27 @@ int scp_generate_uniform(int32_t n, int32_t nm, const int32_t *kinds, const floa
     return 0;
 }
 
+// The structured scene generator's records (sc_gen.h) built on the host:
+// returns the particle count, or -1 for an invalid group list.
+int64_t scp_generate_scene(const sc_scene_group *groups, int32_t ng, int32_t nm, const sc_type_info *types,
+                           int32_t ntypes, float box, int32_t species, uint64_t seed, sc_particle *p,
+                           sc_metabolic_particle *m) {
+    std::vector<sc_gen_group> gg((size_t)(ng > 0 ? ng : 1));
+    const char *why = "";
+    const int64_t n = sc_gen_prepare(groups, ng, types, ntypes, gg.data(), &why);
+    if (n < 0) return -1;
+    if (!p) return n;  // size query
+    for (int32_t g = 0; g < ng; g++) {
+        const sc_gen_group &G = gg[(size_t)g];
+        const int per = (G.kind == SC_SCENE_COMPLEXES || G.kind == SC_SCENE_WRAPPED_CHAINS) ? G.unit : 1;
+        for (int32_t u = 0; u < G.count; u++) sc_gen_unit(&p[G.first + (int64_t)u * per], &G, u, box, seed);
+    }
+    for (int32_t j = 0; j < nm; j++)
+        sc_gen_metabolic(&m[j], j, box, species, types[SC_PARTICLE_TYPE_METABOLIC].radius,
+                         types[SC_PARTICLE_TYPE_METABOLIC].hydrophobic, seed);
+    return n;
+}
+
 void scp_f2h(const float *x, uint16_t *out, int n) {
     for (int i = 0; i < n; i++) out[i] = sc_f2h(x[i]);
 }

@@ -53,6 +53,50 @@ RULE_DTYPE = np.dtype({
     "offsets": [0, 4, 8, 12, 16, 20, 21, 22, 23, 24, 25, 28, 32, 36, 48, 64, 68, 80],
     "itemsize": 96})
 
+# sc_scene_group (include/spatialcell.h)
+SCENE_UNIFORM_BOX = 0
+SCENE_UNIFORM_BALL = 1
+SCENE_SPHERE_SHELL = 2
+SCENE_FIBONACCI_SHELL = 3
+SCENE_COMPLEXES = 4
+SCENE_WRAPPED_CHAINS = 5
+SCENE_MAX_UNIT = 64
+SCENE_GROUP_DTYPE = np.dtype({
+    "names": ["kind", "count", "unit", "nkinds", "kinds", "fractions", "center", "radius", "spacing", "rot",
+              "link_type"],
+    "formats": ["<i4", "<i4", "<i4", "<i4", ("<i4", 4), ("<f4", 4), ("<f4", 3), "<f4", "<f4", ("<f4", 4), "<i4"],
+    "offsets": [0, 4, 8, 12, 16, 32, 48, 60, 64, 68, 84],
+    "itemsize": 88})
+
+
+def scene_group(kind, count, kinds, fractions=None, center=(0.0, 0.0, 0.0), radius=0.0, unit=1, spacing=0.0,
+                rot=(0.0, 0.0, 0.0, 1.0), link_type=1):
+    """One sc_scene_group record."""
+    g = np.zeros(1, SCENE_GROUP_DTYPE)
+    kinds = list(kinds)
+    fractions = [1.0] * len(kinds) if fractions is None else list(fractions)
+    g["kind"] = kind
+    g["count"] = count
+    g["unit"] = unit
+    g["nkinds"] = len(kinds)
+    g["kinds"][0, :len(kinds)] = kinds
+    g["fractions"][0, :len(fractions)] = fractions
+    g["center"] = center
+    g["radius"] = radius
+    g["spacing"] = spacing
+    g["rot"] = rot
+    g["link_type"] = link_type
+    return g
+
+
+def scene_particles(groups):
+    """Particles a list of scene groups generates."""
+    compound = (SCENE_COMPLEXES, SCENE_WRAPPED_CHAINS)
+    g = np.concatenate([np.atleast_1d(x) for x in groups]) if len(groups) else np.zeros(0, SCENE_GROUP_DTYPE)
+    per = np.where(np.isin(g["kind"], compound), g["unit"], 1).astype(np.int64)
+    return int((g["count"].astype(np.int64) * per).sum())
+
+
 # sc_phase (include/spatialcell.h)
 PHASE_SORT_PARTICLES = 0
 PHASE_SORT_METABOLIC = 1

@@ -49,10 +49,14 @@
 // (one page, where a k-major layout would put each k of an item in a different
 // page).  An item with more pairs than the list holds is marked by a count
 // above the capacity and its kernels scan its neighbourhood instead.
-#define SC_LIST_PP 32   // particle-particle: rule/chain/test bonds, polar pairs, collisions
-#define SC_LIST_M 96    // metabolic: colliding metabolic particles and lipids
+#define SC_LIST_PP 128  // particle-particle: rule/chain/test bonds, polar pairs, collisions (dense
+                        // lipid membranes list ~100)
+#define SC_LIST_M 160   // metabolic: colliding metabolic particles and lipids (beside a dense
+                        // membrane ~110)
 #define SC_LIST_LM 48   // lipid <- metabolic collisions
 #define SC_LIST_D 96    // metabolic diffusion partners
+// The diffusion list's buffer is also the metabolic list's build scratch.
+#define SC_LIST_DBUF (SC_LIST_M > SC_LIST_D ? SC_LIST_M : SC_LIST_D)
 #define SC_PP_POLAR 0x80000000u
 #define SC_PP_PARTNER 0x40000000u
 #define SC_PP_COLLIDE 0x20000000u

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <cmath>
@@ -41,9 +42,27 @@ __global__ void k_sum_counts(const int *__restrict__ cnt, const int *__restrict_
     if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)out, (unsigned long long)acc);
 }
 
+// Items of a list whose count is above `limit` (overflowed).
+__global__ void k_count_over(const int *__restrict__ cnt, const int *__restrict__ nActivePtr, int limit,
+                             long long *out) {
+    const int n = *nActivePtr;
+    long long acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += cnt[i] > limit;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)out, (unsigned long long)acc);
+}
+
 __global__ void k_gen_particles(uint8_t *aos, int n, float box, sc_gen_mix mix, uint64_t seed) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) sc_gen_particle(reinterpret_cast<sc_particle *>(aos + (size_t)i * sizeof(sc_particle)), i, box, &mix, seed);
+}
+// Work unit u of a scene group: its first record is at particle first + u * per.
+__global__ void k_gen_scene(uint8_t *aos, sc_gen_group G, int per, float box, uint64_t seed) {
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < G.count)
+        sc_gen_unit(reinterpret_cast<sc_particle *>(aos + (size_t)(G.first + (int64_t)u * per) * sizeof(sc_particle)), &G,
+                    u, box, seed);
 }
 __global__ void k_gen_metabolic(uint8_t *aos, int nm, float box, int species, float radius, int8_t hydrophobic,
                                 uint64_t seed) {
@@ -666,14 +685,14 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.matchPP, (size_t)SC_MAX_ACTIVE_INTERACTIONS * N)) || (rc = dalloc(s, &B.matchN, N)) ||
         (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
         (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
-        (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_D, (int)Nm))) ||
+        (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_DBUF, (int)Nm))) ||
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
         (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)) ||
         (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)) || (rc = dalloc(s, &B.warpOffLM, (size_t)N / 32 + 1)) ||
         (rc = dalloc(s, &B.lipidP, N)))
         return bail(rc);
     // The LM list is built in the diffusion list's buffer when it fits.
-    if (sc_list_words(SC_LIST_LM, (int)N) <= sc_list_words(SC_LIST_D, (int)Nm)) {
+    if (sc_list_words(SC_LIST_LM, (int)N) <= sc_list_words(SC_LIST_DBUF, (int)Nm)) {
         B.scratchLM = B.listD;
     } else if ((rc = dalloc(s, &B.scratchLM, sc_list_words(SC_LIST_LM, (int)N)))) {
         return bail(rc);
@@ -823,6 +842,32 @@ int sc_pair_counts(sc_sim *s, int64_t out[4]) {
     return check_launch(s);
 }
 
+int sc_list_overflows(sc_sim *s, int64_t out[4]) {
+    if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
+    cudaSetDevice(s->device);
+    const ScBuffers &B = s->B;
+    const int *cnt[4] = {B.cntPP, B.cntM, B.cntLM, B.cntD};
+    const bool valid[4] = {B.validPP, B.validM, B.validLM, B.validD};
+    const int cap[4] = {s->P.N, s->P.Nm, s->P.N, s->P.Nm};
+    const int lim = s->P.listLimit;
+    const int limit[4] = {std::min(SC_LIST_PP, lim), std::min(SC_LIST_M, lim), std::min(SC_LIST_LM, lim),
+                          std::min(SC_LIST_D, lim)};
+    const int *nact[4] = {&B.ctr->nActive, &B.ctr->nActiveM, &B.ctr->nActive, &B.ctr->nActiveM};
+    long long *d = nullptr;
+    SC_CK(s, cudaMallocAsync((void **)&d, 4 * sizeof(long long), s->st));
+    SC_CK(s, cudaMemsetAsync(d, 0, 4 * sizeof(long long), s->st));
+    for (int k = 0; k < 4; k++)
+        if (valid[k] && cap[k] > 0)
+            k_count_over<<<std::max(1, std::min(nb_of(cap[k]), 1024)), SC_THREADS, 0, s->st>>>(cnt[k], nact[k],
+                                                                                            limit[k], d + k);
+    long long h[4] = {0, 0, 0, 0};
+    SC_CK(s, cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, s->st));
+    SC_CK(s, cudaFreeAsync(d, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    for (int k = 0; k < 4; k++) out[k] = valid[k] ? (int64_t)h[k] : -1;
+    return check_launch(s);
+}
+
 int sc_idle(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);
@@ -916,18 +961,13 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
     return SC_OK;
 }
 
-int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
-                        int32_t nkinds, uint64_t seed) {
-    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+// The common part of the scene generators: resets the host-side state,
+// runs `particles` (which writes the n particle records into the staging
+// buffer on the sim's stream), unpacks them, generates and unpacks nm
+// metabolic particles and sets the counters.
+static int generate_into(sc_sim *s, int n, int nm, uint64_t seed, const std::function<void(float)> &particles) {
     const int N = s->P.N, Nm = s->P.Nm;
-    if (n < 0 || nm < 0 || n > N || nm > Nm) return set_err(s, SC_E_INVALID, "scene larger than the capacity");
-    const int ntypes = (int)s->types.size();
-    sc_gen_mix mix;
-    memset(&mix, 0, sizeof mix);
-    if (n > 0 && (!kinds || !fractions || sc_gen_make_mix(&mix, kinds, fractions, nkinds, s->types.data(), ntypes)))
-        return set_err(s, SC_E_INVALID, "the particle mix needs 1 to 4 kinds of the type table, weights >= 0");
-    if (nm > 0 && ntypes <= SC_PARTICLE_TYPE_METABOLIC)
+    if (nm > 0 && (int)s->types.size() <= SC_PARTICLE_TYPE_METABOLIC)
         return set_err(s, SC_E_INVALID, "the type table has no metabolic particle type (1000)");
     size_t bytes = std::max((size_t)n * sizeof(sc_particle), (size_t)nm * sizeof(sc_metabolic_particle));
     int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
@@ -941,7 +981,7 @@ int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, 
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
     const float box = s->cfg.sim_size;
     if (N > 0) {
-        if (n) k_gen_particles<<<nb_of(n), SC_THREADS, 0, s->st>>>(s->staging, n, box, mix, seed);
+        if (n) particles(box);
         k_unpack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, n, N, B.p[0]);
     }
     if (Nm > 0) {
@@ -965,6 +1005,42 @@ int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, 
     if (rc) return rc;
     s->loaded = true;
     return SC_OK;
+}
+
+int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
+                        int32_t nkinds, uint64_t seed) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    if (n < 0 || nm < 0 || n > s->P.N || nm > s->P.Nm) return set_err(s, SC_E_INVALID, "scene larger than the capacity");
+    sc_gen_mix mix;
+    memset(&mix, 0, sizeof mix);
+    if (n > 0 && (!kinds || !fractions ||
+                  sc_gen_make_mix(&mix, kinds, fractions, nkinds, s->types.data(), (int)s->types.size())))
+        return set_err(s, SC_E_INVALID, "the particle mix needs 1 to 4 kinds of the type table, weights >= 0");
+    return generate_into(s, n, nm, seed, [&](float box) {
+        k_gen_particles<<<nb_of(n), SC_THREADS, 0, s->st>>>(s->staging, n, box, mix, seed);
+    });
+}
+
+int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    cudaSetDevice(s->device);
+    if (n_groups < 0 || (n_groups > 0 && !groups) || nm < 0 || nm > s->P.Nm)
+        return set_err(s, SC_E_INVALID, "bad group list or metabolic count");
+    std::vector<sc_gen_group> gg((size_t)std::max(n_groups, 1));
+    const char *why = "";
+    const int64_t total = sc_gen_prepare(groups, n_groups, s->types.data(), (int32_t)s->types.size(), gg.data(), &why);
+    if (total < 0) return set_err(s, SC_E_INVALID, why);
+    const int n = (int)total;
+    if (n > s->P.N) return set_err(s, SC_E_INVALID, "scene larger than the capacity");
+    return generate_into(s, n, nm, seed, [&](float box) {
+        for (int32_t g = 0; g < n_groups; g++) {
+            const sc_gen_group &G = gg[(size_t)g];
+            const int per = (G.kind == SC_SCENE_COMPLEXES || G.kind == SC_SCENE_WRAPPED_CHAINS) ? G.unit : 1;
+            if (G.count > 0)
+                k_gen_scene<<<nb_of(G.count), SC_THREADS, 0, s->st>>>(s->staging, G, per, box, seed);
+        }
+    });
 }
 
 int sc_checkpoint_write(sc_sim *s, void *file) {

@@ -34,6 +34,7 @@ _SIGS = {
     "sc_sync": (ctypes.c_int, [_P]),
     "sc_idle": (ctypes.c_int, [_P]),
     "sc_pair_counts": (ctypes.c_int, [_P, _P]),
+    "sc_list_overflows": (ctypes.c_int, [_P, _P]),
     "sc_export_state": (ctypes.c_int, [_P, _P, _P]),
     "sc_export_grid": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "sc_get_counters": (ctypes.c_int, [_P, ctypes.POINTER(abi.Counters)]),
@@ -43,6 +44,7 @@ _SIGS = {
     "sc_get_stream": (ctypes.c_void_p, [_P]),
     "sc_generate_uniform": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P, ctypes.c_int32,
                                            ctypes.c_uint64]),
+    "sc_generate_scene": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64]),
     "sc_checkpoint_write": (ctypes.c_int, [_P, _P]),
     "sc_checkpoint_read": (ctypes.c_int, [_P, _P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
@@ -174,6 +176,15 @@ class Simulation:
         _check(self.L.sc_generate_uniform(self.h, n, nm, abi.ptr(k), abi.ptr(f), len(k), seed), self.h,
                "sc_generate_uniform")
 
+    def generate_scene(self, groups, nm, seed):
+        """Fills the sim on the device (sc_generate_scene): the particles of
+        the scene groups (abi.SCENE_GROUP_DTYPE records), one group after
+        another, and nm metabolic particles uniform in the box."""
+        g = np.ascontiguousarray(np.concatenate([np.atleast_1d(x) for x in groups]) if len(groups) else
+                                 np.zeros(0, abi.SCENE_GROUP_DTYPE), abi.SCENE_GROUP_DTYPE)
+        _check(self.L.sc_generate_scene(self.h, abi.ptr(g) if len(g) else None, len(g), nm, seed), self.h,
+               "sc_generate_scene")
+
     def prepare(self):
         _check(self.L.sc_prepare(self.h), self.h, "sc_prepare")
 
@@ -184,6 +195,12 @@ class Simulation:
         """Pairs in the current lists: (particle, metabolic, lipid-metabolic, diffusion), -1 if not built."""
         out = np.zeros(4, np.int64)
         _check(self.L.sc_pair_counts(self.h, abi.ptr(out)), self.h, "sc_pair_counts")
+        return tuple(int(x) for x in out)
+
+    def list_overflows(self):
+        """Items whose list overflowed, per list as pair_counts; -1 if not built."""
+        out = np.zeros(4, np.int64)
+        _check(self.L.sc_list_overflows(self.h, abi.ptr(out)), self.h, "sc_list_overflows")
         return tuple(int(x) for x in out)
 
     def idle(self):

@@ -150,6 +150,48 @@ def batch_replicas(count, seed=3, n_lo=2048, n_hi=262144):
     return out
 
 
+def vesicle_groups(box, shell_r=400.0, lipids=2_000_000, interior=6_000_000, complexes=50_000, complex_size=20,
+                   spacing=3.0, leaflet_gap=4.0):
+    """Scene groups of the crowded vesicle case: a lipid bilayer shell
+    (two leaflets leaflet_gap apart, lipids uniform on each sphere and split
+    by area, heads out on the outer leaflet and in on the inner one, as the
+    reference's two fillParticlesSphere leaflets are oriented), interior
+    particles dummy / A / B 70 / 15 / 15 uniform in the ball inside, and
+    rigid-lattice complexes of dummies (complex_size sites on the cubic
+    lattice of the given spacing, bonded along the growth tree with chain
+    bonds) in the same ball."""
+    c = (box / 2.0, box / 2.0, box / 2.0)
+    ri = shell_r - leaflet_gap
+    n_out = int(round(lipids * shell_r ** 2 / (shell_r ** 2 + ri ** 2)))
+    inner = ri - 6.0
+    return [
+        abi.scene_group(abi.SCENE_SPHERE_SHELL, n_out, [LIPID], center=c, radius=shell_r),
+        abi.scene_group(abi.SCENE_SPHERE_SHELL, lipids - n_out, [LIPID], center=c, radius=ri,
+                        rot=(1.0, 0.0, 0.0, 0.0)),
+        abi.scene_group(abi.SCENE_UNIFORM_BALL, interior, [DUMMY, TYPE_A, TYPE_B], [0.70, 0.15, 0.15], center=c,
+                        radius=inner),
+        abi.scene_group(abi.SCENE_COMPLEXES, complexes, [DUMMY], center=c, radius=inner - 2.0 * spacing,
+                        unit=complex_size, spacing=spacing, link_type=abi.INTERACTION_TYPE_CHAIN),
+    ]
+
+
+def vesicle_workload(scale=1.0):
+    """The crowded vesicle stress case (900 nm walled box, 2 M lipids on a
+    400 nm bilayer shell, 6 M interior particles, 50 k 20-particle complexes,
+    32 M metabolic items, seed 5), every count scaled by `scale` and every
+    length by its cube root.  Returns (config, groups, metabolic count)."""
+    s = scale ** (1.0 / 3.0)
+    box = 900.0 * s
+    groups = vesicle_groups(box, shell_r=400.0 * s, lipids=int(2_000_000 * scale), interior=int(6_000_000 * scale),
+                            complexes=int(50_000 * scale))
+    n = abi.scene_particles(groups)
+    nm = int(32_000_000 * scale)
+    cfg = abi.make_config(num_particles=n, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
+                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5,
+                          steps=1000, periodic=0)
+    return cfg, groups, nm
+
+
 def build_workload(name, **overrides):
     """Config, tables and initial state of a measured workload."""
     cfg = workload_config(name, **overrides)

@@ -22,8 +22,8 @@ from . import abi, native, scenes
 # Device bytes per item of a simulation: state (two buffers of every field)
 # and pair lists, from the allocation in sc_create; an upper bound used for
 # admission.
-BYTES_PER_PARTICLE = 1400
-BYTES_PER_METABOLIC = 1700
+BYTES_PER_PARTICLE = 1800
+BYTES_PER_METABOLIC = 2200
 
 
 @dataclasses.dataclass
