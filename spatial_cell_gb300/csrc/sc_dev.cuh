@@ -88,10 +88,14 @@ struct ScCounters {
     int poolLM;           // entries of the lipid-metabolic pair pool taken (k_build_lm)
 };
 
-// Relax work classes: items with bond partners in their list, items with
-// polar (lipid) pairs and no partners, and the rest.  k_relax runs the
-// classes one after another so a warp's items take the same branches.
+// Relax work classes: 0 bonded items, 1 items with polar (lipid) pairs and no
+// bonds, 2 the rest.  Each class has its own kernel, so a warp's items take
+// the same branches.
 #define SC_RELAX_CLASSES 3
+// Bond match count of a bonded item (low bits) and its in-order flag (a
+// test bond: relaxed by the in-order scan).
+#define SC_MATCH_COUNT 0xff
+#define SC_MATCH_INORDER 0x100
 
 struct ScParams {
     float simSize, maxInt, maxDiff, cell;

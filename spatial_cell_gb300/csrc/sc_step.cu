@@ -260,8 +260,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
             }
         });
         cnt[i] = c;
-        if (B.n >= 1) matchN[i] = nm;
-        if (c > min(SC_LIST_PP, P.listLimit)) ovf[atomicAdd(ovfCount, 1)] = i;
+        // A test bond rotates the particle itself, which its later terms
+        // read: its relaxation takes the in-order scan with the overflowed
+        // items (its noise stays with the bonded class).
+        bool testBond = false;
+#pragma unroll
+        for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) testBond |= k < B.n && B.t[k] == 0;
+        if (B.n >= 1) matchN[i] = nm | (testBond ? SC_MATCH_INORDER : 0);
+        if (c > min(SC_LIST_PP, P.listLimit) || testBond) ovf[atomicAdd(ovfCount, 1)] = i;
         if (B.n >= 1) cls = 0;
         else if (c <= min(SC_LIST_PP, P.listLimit) && (any & SC_PP_POLAR)) cls = 1;
     }
@@ -340,7 +346,7 @@ __device__ __forceinline__ void coordinate_noise_item(
     };
     if (L.cnt[i] <= min(SC_LIST_PP, P.listLimit)) {
         const uint32_t *__restrict__ myMatch = match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
-        const int nm = matchN[i];
+        const int nm = matchN[i] & SC_MATCH_COUNT;
         for (int m = 0; m < nm; m++) {
             const uint32_t e = myMatch[m];
             term((int)(e & SC_PP_INDEX), (int)(e >> 29));
@@ -610,7 +616,8 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
 // first bond, then its second ...; the list is then walked once more to add
 // every term in the reference's order (the slerps of dAV and the float sums
 // are order-dependent).  A test bond rotates the particle itself, which
-// later terms read: such particles take the in-order path.
+// later terms read: such particles (SC_MATCH_INORDER) take the in-order
+// scan of k_relax_overflow.
 struct BondTerm {
     sc_f3 dv;   // velocity term
     sc_f4 q;    // dAV slerp target
@@ -620,13 +627,7 @@ struct BondTerm {
 
 __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4,
                                                   float4 r4, float4 a4) {
-    const int nbi = min(max(A.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
     const int *__restrict__ myBonds = A.bonds + (size_t)i * 24;
-    for (int k = 0; k < nbi; k++)
-        if (myBonds[3 * k] == 0) {
-            relax_item<false, 0>(P, A, i, in, v4, r4, a4);
-            return;
-        }
     float4 p4 = A.pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, ppos, SC_BINNED_P);
@@ -641,7 +642,7 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
     const int c = A.L.cnt[i];
     // 1. the terms of its bond matches (list order, then bond-slot order)
     const uint32_t *__restrict__ myMatch = A.match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
-    const int nm = min(A.matchN[i], SC_MAX_ACTIVE_INTERACTIONS);
+    const int nm = min(A.matchN[i] & SC_MATCH_COUNT, SC_MAX_ACTIVE_INTERACTIONS);
     BondTerm T[SC_MAX_ACTIVE_INTERACTIONS];
     int nt = 0;
     for (int m = 0; m < nm; m++) {
@@ -772,27 +773,48 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
     if (dbgTouched) st4(A.dbg, i, pdbg);
 }
 
-// The items of one work class whose list fits (the others are left to
-// k_relax_overflow), grid-stride over the class's index segment.
+// One item of a work class (the items whose list overflowed, and bonded
+// items with a test bond, are left to k_relax_overflow).
+template <int MODE>
+__device__ __forceinline__ void relax_class_item(const ScParams &P, const RelaxArgs &A, int i) {
+    int4 in = A.info[i];
+    float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
+    if (!(in.z & SC_ACTIVE)) {
+        A.velOut[i] = v4;
+        A.rotOut[i] = r4;
+        A.avOut[i] = a4;
+        return;
+    }
+    if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) return;
+    if (MODE == 0) {
+        if (!(A.matchN[i] & SC_MATCH_INORDER)) relax_bonded_item(P, A, i, in, v4, r4, a4);
+    } else {
+        relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
+    }
+}
+
+// The items of one work class, grid-stride over the class's index segment.
+// The bonded class goes block by block, its items ranked by bond-match
+// count inside the block, so a warp's lanes walk about as many bond terms
+// (items with more bonds would otherwise hold back the rest of their warp).
 template <int MODE>
 __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
     const int n = A.classCount[MODE];
     const int *__restrict__ idx = A.classIdx + (size_t)MODE * A.L.cap;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int i = idx[t];
-        int4 in = A.info[i];
-        float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
-        if (!(in.z & SC_ACTIVE)) {
-            A.velOut[i] = v4;
-            A.rotOut[i] = r4;
-            A.avOut[i] = a4;
-            continue;
+    if (MODE == 0) {
+        __shared__ int s_item[SC_THREADS];
+        for (int base = blockIdx.x * SC_THREADS; base < n; base += gridDim.x * SC_THREADS) {
+            const int t = base + threadIdx.x;
+            const int i = t < n ? idx[t] : -1;
+            s_item[threadIdx.x] = i;
+            int src, cs;
+            count_rank<SC_MAX_ACTIVE_INTERACTIONS>(i >= 0, i >= 0 ? (A.matchN[i] & SC_MATCH_COUNT) : 0, &src, &cs);
+            if (cs >= 0) relax_class_item<MODE>(P, A, s_item[src]);
+            __syncthreads();  // the ranking's shared arrays are reused by the next round
         }
-        if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) continue;
-        if (MODE == 0)
-            relax_bonded_item(P, A, i, in, v4, r4, a4);
-        else
-            relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
+    } else {
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+            relax_class_item<MODE>(P, A, idx[t]);
     }
 }
 
