@@ -84,8 +84,9 @@ struct ScCounters {
     int tileCounter[4];
     int ppClassCount[4];  // items per relax work class (k_build_pp)
     int ovfPP, ovfM;      // items whose particle / metabolic list overflowed (k_build_pp, k_build_m)
-    int poolM;            // entries of the metabolic pair pool taken (k_build_m)
-    int poolLM;           // entries of the lipid-metabolic pair pool taken (k_build_lm)
+    int _pad;
+    unsigned long long poolM;   // entries the metabolic list blocks asked of their pool (k_build_m)
+    unsigned long long poolLM;  // the same for the lipid-metabolic lists (k_build_lm)
 };
 
 // Relax work classes: 0 bonded items, 1 items with polar (lipid) pairs and no

@@ -698,6 +698,10 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         return bail(rc);
     }
     B.invalidateLists();
+    B.poolCapM = std::min<size_t>(sc_list_words(SC_LIST_M, (int)Nm) / 4, (size_t)INT_MAX - 1024);
+    // SC_POOL_M_PER_ITEM=n starts the metabolic pair pool at n entries per item
+    if (const char *pp = getenv("SC_POOL_M_PER_ITEM"))
+        B.poolCapM = std::min(B.poolCapM, (size_t)std::max(0, atoi(pp)) * (size_t)std::max<int64_t>(Nm, 1));
     B.polyCap = 4096;
     P.lipidP = B.lipidP;
     cudaMemsetAsync(B.ctr, 0, sizeof(ScCounters), s->st);
@@ -809,6 +813,36 @@ int sc_step(sc_sim *s, int32_t n_steps) {
 }
 
 
+// The metabolic pair pool is sized for the lists the sim needs: its last
+// build's demand (what every block asked for, granted or not) is read at
+// each synchronisation and, when it exceeded the pool, the pool grows to
+// 1.25x the demand.  Lists of blocks the pool had no room for were scanned
+// instead, so results never depend on the pool's size; step graphs, which
+// hold the old buffer, are dropped.  Called with the sim's streams idle.
+static int grow_pools(sc_sim *s) {
+    ScBuffers &B = s->B;
+    unsigned long long need = 0;
+    SC_CK(s, cudaMemcpy(&need, &B.ctr->poolM, sizeof need, cudaMemcpyDeviceToHost));
+    const size_t most = (size_t)INT_MAX - 1024;  // pool offsets are 32-bit
+    if (need <= B.poolCapM || B.poolCapM >= most) return SC_OK;
+    const size_t cap = std::min<size_t>((size_t)need + (size_t)need / 4 + 1024, most);
+    uint32_t *grown = nullptr;
+    int rc = dalloc(s, &grown, cap * 4);
+    if (rc) {  // no room: keep the pool (the overflowing blocks keep scanning)
+        cudaGetLastError();
+        s->err.clear();
+        return SC_OK;
+    }
+    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)B.listM));
+    SC_CK(s, cudaFreeAsync(B.listM, s->st));
+    B.listM = grown;
+    B.poolCapM = cap;
+    B.validM = false;
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
+    s->graphs.clear();
+    return SC_OK;
+}
+
 int sc_sync(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);
@@ -817,7 +851,7 @@ int sc_sync(sc_sim *s) {
     int derr = 0;
     SC_CK(s, cudaMemcpy(&derr, &s->B.ctr->error, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr) return set_err(s, SC_E_DEVICE, "device-side error code " + std::to_string(derr));
-    return SC_OK;
+    return s->loaded ? grow_pools(s) : SC_OK;
 }
 
 int sc_pair_counts(sc_sim *s, int64_t out[4]) {

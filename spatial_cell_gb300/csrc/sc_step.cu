@@ -895,7 +895,7 @@ struct PoolSlot {
 };
 template <int K>
 __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int c, uint4 *__restrict__ pool,
-                                              int poolCap, int *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                              int poolCap, unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
                                               int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                               int *__restrict__ ovf, int *__restrict__ ovfCount) {
     __shared__ int s_n[SC_THREADS / 32];
@@ -913,8 +913,9 @@ __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int
     if (t == 0) {
         int total = 0;
         for (int w = 0; w < SC_THREADS / 32; w++) total += s_n[w] * 32;
-        const int base = total ? atomicAdd(poolUsed, total) : 0;
-        s_base = base + total <= poolCap ? base : -1;
+        // 64-bit demand: it keeps counting what blocks ask for past the pool
+        const unsigned long long base = total ? atomicAdd(poolUsed, (unsigned long long)total) : 0ull;
+        s_base = base + (unsigned long long)total <= (unsigned long long)poolCap ? (int)base : -1;
     }
     __syncthreads();
     if (s_base < 0 && cs > 0) {
@@ -952,7 +953,7 @@ __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int
 // listed in `ovf` for the scan.
 __device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int c, const uint32_t *scratch,
                                              const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
-                                             uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
+                                             uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
                                              int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
                                              int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const PoolSlot S =
@@ -982,7 +983,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                        uint4 *__restrict__ pool, int poolCap, int *__restrict__ poolUsed,
+                                                        uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
                                                         int *__restrict__ warpOff, uint32_t *scratch,
                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
@@ -1410,7 +1411,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
                                                          const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
                                                          const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                          uint4 *__restrict__ pool, int poolCap,
-                                                         int *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                                         unsigned long long *__restrict__ poolUsed,
+                                                         int *__restrict__ warpOff,
                                                          uint32_t *scratch, int *__restrict__ cnt,
                                                          int *__restrict__ perm, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2184,10 +2186,10 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
                 c.P, B.cellStartM, B.cellStartP, M.pos, M.info, F.pos, F.info, reinterpret_cast<uint16_t *>(B.listM),
                 B.cntM, B.ovfM, &B.ctr->ovfM);
         } else {
-            cudaMemsetAsync(&B.ctr->poolM, 0, sizeof(int), c.st);
+            cudaMemsetAsync(&B.ctr->poolM, 0, sizeof(B.ctr->poolM), c.st);
             k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
                 c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info,
-                reinterpret_cast<uint4 *>(B.listM), (int)(sc_list_words(SC_LIST_M, c.P.Nm) / 4), &B.ctr->poolM,
+                reinterpret_cast<uint4 *>(B.listM), (int)B.poolCapM, &B.ctr->poolM,
                 B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
         }
         (*c.launches)++;
@@ -2223,7 +2225,7 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     PFields F = B.P();
     if (!B.validLM) {
         if (B.scratchLM == B.listD) B.validD = false;
-        cudaMemsetAsync(&B.ctr->poolLM, 0, sizeof(int), c.st);
+        cudaMemsetAsync(&B.ctr->poolLM, 0, sizeof(B.ctr->poolLM), c.st);
         k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
             c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos, M.info, reinterpret_cast<uint4 *>(B.listLM),
             (int)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,

@@ -194,3 +194,24 @@ def test_capacity_exactly_full(product):
         e.prepare()
         e.step(2)
     _same(cfg, gpu, cpu, "2 steps at full capacity")
+
+
+def test_metabolic_pool_grows_and_results_do_not_change(product, monkeypatch):
+    """A metabolic pair pool too small for the lists: the blocks it has no
+    room for scan their neighbourhoods, the pool grows at the next
+    synchronisation, and every step matches the oracle bit for bit."""
+    monkeypatch.setenv("SC_POOL_M_PER_ITEM", "2")
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(15, n=900, nm=1800, box=42.0, periodic=1))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(1)
+    _same(cfg, gpu, cpu, "1 step on a short pool")
+    gpu.sync()  # grows the pool
+    for ph, a in [(abi.PHASE_SORT_PARTICLES, 0), (abi.PHASE_SORT_METABOLIC, 0), (abi.PHASE_RELAX_METAB, 0)]:
+        for e in (gpu, cpu):
+            e.run_phase(ph, a)
+    assert gpu.list_overflows()[1] == 0, "the grown pool still overflows"
+    _same(cfg, gpu, cpu, "after the pool grew")
+    for e in (gpu, cpu):
+        e.step(2)
+    _same(cfg, gpu, cpu, "2 more steps")
