@@ -1538,7 +1538,15 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
         cs = P.pidx[2 * in.y];
         ce = P.pidx[2 * in.y + 1];
     }
-    if (cs >= ce) {
+    // No rule of its type can add a bond when each is transition-only or
+    // its group is already active on the item (bonds are only added below,
+    // so a blocked rule stays blocked): the scan would change nothing.
+    bool open = false;
+    for (int k = cs; k < ce && !open && pnb < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+        const sc_rule &pii = P.prules[k];
+        open = !pii.only_via_transition && !(pii.group >= 0 && group_active_in(bonds + (size_t)i * 24, pnb, pii.group));
+    }
+    if (!open) {
         nbOut[i] = pnb;
         return;
     }
@@ -1603,7 +1611,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
     int b[SC_MAX_ACTIVE_INTERACTIONS * 3];
 #pragma unroll
     for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS * 3; k++) b[k] = k < 3 * pnb ? bondsIn[(size_t)i * 24 + k] : 0;
-    if ((in.z & SC_ACTIVE) && pnb >= 1) {
+    // Only bonds whose rule transitions or breaks after a transition act in
+    // the scan: without one the scan would change nothing.
+    bool acts = false;
+#pragma unroll
+    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
+        if (k < pnb && b[3 * k] >= 10) {
+            const sc_rule &pii = rule_at(P, b[3 * k]);
+            acts |= pii.transition_to >= 0 || pii.break_after_transition;
+        }
+    if ((in.z & SC_ACTIVE) && acts) {
         float4 p4 = pos[i];
         const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
         const Imager IM(P, ppos, SC_BINNED_P);
