@@ -398,6 +398,31 @@ typedef struct sc_scene_group {
  * capacity) and nm metabolic particles; counters as sc_generate_uniform. */
 int sc_generate_scene(sc_sim *sim, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed);
 
+/* ---- observables (no counterpart in the reference) ----
+ * Ensemble quantities reduced on the device in double precision, in a fixed
+ * order (the same bytes on every run).  Index 0 is the particles, 1 the
+ * metabolic particles; only active items count. */
+typedef struct sc_observables {
+    double msd[2];            /* mean squared displacement since sc_mark_positions (nm^2), items
+                                 matched by id; minimum image in a periodic box */
+    int64_t msd_items[2];     /* items in the mean (active, with a mark) */
+    double mean_v2[2];        /* mean |velocity|^2 */
+    int64_t active[2];        /* active items */
+    int64_t bond_slots;       /* sum of n_active_interactions over active particles */
+    double metabolites[SC_AOS_NUM_METABOLITES]; /* total amount of each simulated species */
+} sc_observables;
+/* Records every active item's position, by id, as the origin of the MSD. */
+int sc_mark_positions(sc_sim *sim);
+int sc_observe(sc_sim *sim, sc_observables *out);
+/* Histogram of the distances of ordered particle pairs (i, j), i != j, i of
+ * type type_a and j of type type_b (-1: any type), active, closer than r_max
+ * (at most the grid cell size): counts[b] for distance in
+ * [b, b + 1) * r_max / n_bins.  Distances in double precision from the float
+ * positions (minimum image in a periodic box).  Sorts the particles into
+ * their cells first when they have moved since the last sort (the next
+ * step's sort then leaves them in place, so the trajectory is unchanged). */
+int sc_pair_histogram(sc_sim *sim, int32_t type_a, int32_t type_b, float r_max, int32_t n_bins, uint64_t *counts);
+
 /* ---- checkpoint / resume (no counterpart in the reference) ----
  * A checkpoint holds the whole state -- the active particle and metabolic
  * records in the reference's layouts, the step counter and the next particle

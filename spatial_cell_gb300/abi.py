@@ -157,6 +157,17 @@ class Counters(ctypes.Structure):
     ]
 
 
+class Observables(ctypes.Structure):
+    _fields_ = [
+        ("msd", ctypes.c_double * 2),
+        ("msd_items", ctypes.c_int64 * 2),
+        ("mean_v2", ctypes.c_double * 2),
+        ("active", ctypes.c_int64 * 2),
+        ("bond_slots", ctypes.c_int64),
+        ("metabolites", ctypes.c_double * AOS_NUM_METABOLITES),
+    ]
+
+
 assert ctypes.sizeof(Config) == 88
 assert ctypes.sizeof(Counters) == 32
 

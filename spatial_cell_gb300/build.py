@@ -20,7 +20,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libspatialcell.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["sc_grid.cu", "sc_step.cu", "sc_sim.cu", "sc_noalloc.cu"]
+CU_SOURCES = ["sc_grid.cu", "sc_step.cu", "sc_sim.cu", "sc_noalloc.cu", "sc_observe.cu"]
 CPP_SOURCES = ["sc_host.cpp"]
 HEADERS = ["scmath.h", "sc_dev.cuh", "sc_launch.h", "sc_json.hpp"]
 

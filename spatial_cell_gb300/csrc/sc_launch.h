@@ -117,6 +117,21 @@ void sc_launch_gather_particles(cudaStream_t st, const uint32_t *perm, int n, co
 void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, const MFields &src,
                                 const MFields &dst, long long *launches);
 
+// sc_observe.cu: FP64 observables.  The observe launcher reduces one item set
+// into out[sc_observe_cols()] through a partials table of
+// sc_observe_rows() x sc_observe_cols() doubles (columns: MSD sum, MSD
+// items, |v|^2 sum, active items, bond slots, then one per species).
+int sc_observe_cols();
+int sc_observe_rows();
+void sc_launch_mark(cudaStream_t st, const int *nActive, const float4 *pos, const int4 *info, float4 *mark,
+                    int markCap);
+void sc_launch_observe(cudaStream_t st, const int *nActive, const float4 *pos, const float4 *vel, const int4 *info,
+                       const int *nb, const float *met, int sp, int S, const float4 *mark, int markCap, double box,
+                       int periodic, double *partials, double *out);
+void sc_launch_pair_histogram(cudaStream_t st, const ScParams &P, const uint32_t *cellStart, const int *nActive,
+                              const float4 *pos, const int4 *info, int typeA, int typeB, double rMax, int nBins,
+                              unsigned long long *counts, int gridCap);
+
 // sc_step.cu: one launcher per reference phase (include/spatialcell.h, sc_phase)
 struct ScLaunchCtx {
     cudaStream_t st;

@@ -229,6 +229,10 @@ struct sc_sim {
     uint8_t *staging = nullptr;
     size_t stagingBytes = 0;
     bool loaded = false;
+    // observables: MSD origins by id, the partials table and the results
+    float4 *markP = nullptr, *markM = nullptr;
+    int markCapP = 0, markCapM = 0;
+    double *obs = nullptr;  // partials table, then 2 result rows
 };
 
 namespace {
@@ -1075,6 +1079,102 @@ int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups,
                 k_gen_scene<<<nb_of(G.count), SC_THREADS, 0, s->st>>>(s->staging, G, per, box, seed);
         }
     });
+}
+
+int sc_mark_positions(sc_sim *s) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    cudaSetDevice(s->device);
+    ScCounters c;
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    SC_CK(s, cudaMemcpy(&c, s->B.ctr, sizeof c, cudaMemcpyDeviceToHost));
+    const int capP = std::max(std::max(s->P.N, c.nextId), 1), capM = std::max(s->P.Nm, 1);
+    if (capP > s->markCapP) {
+        if (s->markP) {
+            s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->markP));
+            cudaFreeAsync(s->markP, s->st);
+            s->markP = nullptr;
+        }
+        int rc = dalloc(s, &s->markP, (size_t)capP);
+        if (rc) return rc;
+        s->markCapP = capP;
+    }
+    if (!s->markM) {
+        int rc = dalloc(s, &s->markM, (size_t)capM);
+        if (rc) return rc;
+        s->markCapM = capM;
+    }
+    ScBuffers &B = s->B;
+    SC_CK(s, cudaMemsetAsync(s->markP, 0, (size_t)s->markCapP * sizeof(float4), s->st));
+    SC_CK(s, cudaMemsetAsync(s->markM, 0, (size_t)s->markCapM * sizeof(float4), s->st));
+    if (s->P.N > 0) sc_launch_mark(s->st, &B.ctr->nActive, B.P().pos, B.P().info, s->markP, s->markCapP);
+    if (s->P.Nm > 0) sc_launch_mark(s->st, &B.ctr->nActiveM, B.M().pos, B.M().info, s->markM, s->markCapM);
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    return check_launch(s);
+}
+
+int sc_observe(sc_sim *s, sc_observables *out) {
+    if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    cudaSetDevice(s->device);
+    const int cols = sc_observe_cols(), rows = sc_observe_rows();
+    if (!s->obs) {
+        int rc = dalloc(s, &s->obs, (size_t)(rows + 2) * cols);
+        if (rc) return rc;
+    }
+    ScBuffers &B = s->B;
+    double *res = s->obs + (size_t)rows * cols;
+    SC_CK(s, cudaMemsetAsync(res, 0, 2 * (size_t)cols * sizeof(double), s->st));
+    const double box = s->cfg.sim_size;
+    if (s->P.N > 0) {
+        PFields F = B.P();
+        sc_launch_observe(s->st, &B.ctr->nActive, F.pos, F.vel, F.info, F.nb, nullptr, 0, 0, s->markP, s->markCapP,
+                          box, s->P.periodic, s->obs, res);
+    }
+    if (s->P.Nm > 0) {
+        MFields M = B.M();
+        sc_launch_observe(s->st, &B.ctr->nActiveM, M.pos, M.vel, M.info, nullptr,
+                          reinterpret_cast<const float *>(M.met), s->P.SP, s->P.S, s->markM, s->markCapM, box,
+                          s->P.periodic, s->obs, res + cols);
+    }
+    std::vector<double> h((size_t)2 * cols);
+    SC_CK(s, cudaMemcpyAsync(h.data(), res, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    memset(out, 0, sizeof *out);
+    for (int k = 0; k < 2; k++) {
+        const double *r = &h[(size_t)k * cols];
+        out->msd_items[k] = (int64_t)r[1];
+        out->msd[k] = r[1] > 0 ? r[0] / r[1] : 0.0;
+        out->active[k] = (int64_t)r[3];
+        out->mean_v2[k] = r[3] > 0 ? r[2] / r[3] : 0.0;
+    }
+    out->bond_slots = (int64_t)h[4];
+    for (int m = 0; m < SC_AOS_NUM_METABOLITES; m++) out->metabolites[m] = h[(size_t)cols + 5 + m];
+    return check_launch(s);
+}
+
+int sc_pair_histogram(sc_sim *s, int32_t type_a, int32_t type_b, float r_max, int32_t n_bins, uint64_t *counts) {
+    if (!s || !counts) return set_err(s, SC_E_INVALID, "null argument");
+    if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
+    if (n_bins < 1 || n_bins > 4096) return set_err(s, SC_E_INVALID, "n_bins must be in 1..4096");
+    if (!(r_max > 0.0f) || r_max > s->cfg.grid_cell_size)
+        return set_err(s, SC_E_INVALID, "r_max must be in (0, grid cell size]");
+    cudaSetDevice(s->device);
+    int rc;
+    if (!(s->P.binned & SC_BINNED_P) && (rc = run_phase(s, SC_PHASE_SORT_PARTICLES, 0))) return rc;
+    ScBuffers &B = s->B;
+    unsigned long long *d = nullptr;
+    SC_CK(s, cudaMallocAsync((void **)&d, (size_t)n_bins * sizeof(unsigned long long), s->st));
+    SC_CK(s, cudaMemsetAsync(d, 0, (size_t)n_bins * sizeof(unsigned long long), s->st));
+    if (s->P.N > 0) {
+        PFields F = B.P();
+        sc_launch_pair_histogram(s->st, s->P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, type_a, type_b,
+                                 (double)r_max, n_bins, d, s->gridCap);
+    }
+    SC_CK(s, cudaMemcpyAsync(counts, d, (size_t)n_bins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
+    SC_CK(s, cudaFreeAsync(d, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    return check_launch(s);
 }
 
 int sc_checkpoint_write(sc_sim *s, void *file) {

@@ -45,6 +45,9 @@ _SIGS = {
     "sc_generate_uniform": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P, ctypes.c_int32,
                                            ctypes.c_uint64]),
     "sc_generate_scene": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64]),
+    "sc_mark_positions": (ctypes.c_int, [_P]),
+    "sc_observe": (ctypes.c_int, [_P, ctypes.POINTER(abi.Observables)]),
+    "sc_pair_histogram": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_int32, _P]),
     "sc_checkpoint_write": (ctypes.c_int, [_P, _P]),
     "sc_checkpoint_read": (ctypes.c_int, [_P, _P]),
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
@@ -196,6 +199,26 @@ class Simulation:
         out = np.zeros(4, np.int64)
         _check(self.L.sc_pair_counts(self.h, abi.ptr(out)), self.h, "sc_pair_counts")
         return tuple(int(x) for x in out)
+
+    def mark_positions(self):
+        """Records the current positions as the origin of the MSD (sc_mark_positions)."""
+        _check(self.L.sc_mark_positions(self.h), self.h, "sc_mark_positions")
+
+    def observe(self):
+        """FP64 observables (sc_observe) as a dict: msd, msd_items, mean_v2, active
+        (each a (particles, metabolic) pair), bond_slots, metabolites."""
+        o = abi.Observables()
+        _check(self.L.sc_observe(self.h, ctypes.byref(o)), self.h, "sc_observe")
+        return {"msd": tuple(o.msd), "msd_items": tuple(o.msd_items), "mean_v2": tuple(o.mean_v2),
+                "active": tuple(o.active), "bond_slots": int(o.bond_slots),
+                "metabolites": tuple(o.metabolites)}
+
+    def pair_histogram(self, type_a, type_b, r_max, n_bins):
+        """Distance histogram of ordered particle pairs (sc_pair_histogram)."""
+        out = np.zeros(n_bins, np.uint64)
+        _check(self.L.sc_pair_histogram(self.h, type_a, type_b, r_max, n_bins, abi.ptr(out)), self.h,
+               "sc_pair_histogram")
+        return out
 
     def list_overflows(self):
         """Items whose list overflowed, per list as pair_counts; -1 if not built."""
