@@ -258,10 +258,17 @@ def batched_sample(args, native, torch):
     stream as a captured graph, all in flight together, against the same
     replicas stepped one at a time.  Wall-clock with the device synchronised
     on both sides; particle-steps/s of all replicas."""
+    from spatial_cell_gb300 import autotune
     reps = scenes.batch_replicas(args.batch_replicas)
+    # the tuner picks cell size and tile use on a median-size cell; work
+    # classes stay on one stream per cell (many cells fill the device)
+    mid = sorted(reps, key=lambda r: r[0].num_particles)[len(reps) // 2][0]
+    best, times = autotune.tune(mid, fork=(0,))
     sims = []
     for cfg, types, rules, p, m in reps:
-        s = native.Simulation(cfg, types, rules)
+        cfg, env = autotune.apply(cfg, best)
+        with autotune._env(**env):
+            s = native.Simulation(cfg, types, rules)
         s.load_state(p, m)
         s.prepare()
         s.step(1)  # warm-up: captures the step graphs
@@ -290,7 +297,10 @@ def batched_sample(args, native, torch):
     return {"replicas": len(reps), "particles_and_metabolic": items, "steps": args.batch_steps,
             "value": batched, "unit": UNIT, "one_at_a_time": alone, "speedup": batched / alone,
             "sizes": "particles log-uniform in [2048, 262144] (seed 3), metabolic x2, cubes at 65,536 per "
-                     "(200 nm)^3, mix Dirichlet(2,2,1,1), periodic, 6 nm cells",
+                     "(200 nm)^3, mix Dirichlet(2,2,1,1), periodic",
+            "autotuned": {"cell_nm": best[0], "tiles": best[2], "tuned_on_particles": mid.num_particles,
+                          "candidates_ms_per_step": {f"cell {c:g} tiles {t}": round(v * 1e3, 3)
+                                                     for (c, f, t), v in sorted(times.items())}},
             "timing": "wall clock, device synchronised before and after"}
 
 

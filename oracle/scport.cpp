@@ -117,6 +117,7 @@ struct scp_sim {
     int nActive = 0, lastActive = -1, nextId = 0, nActiveM = 0, step = 0;
     bool periodic = false;   // periodic box extension (cfg.periodic)
     int nUsed = 2;           // cells per axis that hold positions, ceil(simSize / cell)
+    float cellSize = 1.0f;   // cell width: the configured size, in a periodic box simSize / nUsed
 
     const sc_rule &rule(int id) const {
         static const sc_rule z = zero_rule();
@@ -129,7 +130,7 @@ struct scp_sim {
     // config.cuh:65-74, or in a periodic box the cells the box spans
     int idx_limit() const { return periodic ? nUsed : ngrid; }
     uint32_t key_of(sc_f3 pos) const {
-        float c = cfg.grid_cell_size;
+        float c = cellSize;
         int n = idx_limit();
         return cell_key(sc_grid_idx(pos.x, c, n), sc_grid_idx(pos.y, c, n), sc_grid_idx(pos.z, c, n));
     }
@@ -139,7 +140,7 @@ struct scp_sim {
     // order; per cell calls f(key).
     template <class F>
     void cells27(sc_f3 pos, F &&f) const {
-        float c = cfg.grid_cell_size;
+        float c = cellSize;
         int n = idx_limit();
         int cx = (int)sc_grid_idx(pos.x, c, n), cy = (int)sc_grid_idx(pos.y, c, n), cz = (int)sc_grid_idx(pos.z, c, n);
         if (periodic) {
@@ -945,7 +946,9 @@ scp_sim *scp_create(const sc_config *cfg, const sc_type_info *types, int n_types
     s->nbits = bits;
     s->periodic = cfg->periodic != 0;
     s->nUsed = ng;
-    if (s->periodic && ng < 3) { delete s; return nullptr; }
+    s->cellSize = cfg->grid_cell_size;
+    if (s->periodic) s->nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &s->cellSize);
+    if (s->periodic && s->nUsed < 3) { delete s; return nullptr; }
     s->cells = (size_t)p2 * p2 * p2;
     s->N = cfg->num_particles;
     s->Nm = cfg->num_metabolic_particles;

@@ -87,6 +87,8 @@ extern "C" int sc_sort_cells_static(const sc_config *cfg, const void *pos, const
     P.cells = (uint32_t)ngrid * (uint32_t)ngrid * (uint32_t)ngrid;
     P.periodic = cfg->periodic != 0;
     P.nUsed = (int)ceilf(cfg->grid_cell_size > 0.0f ? cfg->sim_size / cfg->grid_cell_size : 0.0f);
+    if (cfg->periodic && cfg->grid_cell_size > 0.0f)
+        P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
     long long launches = 0;
     if (cudaMemsetAsync(ctr, 0, sizeof(ScCounters), st) != cudaSuccess) return SC_E_CUDA;
     int cur = sc_launch_sort(st, (const float4 *)pos, (const int4 *)info, n, P, keys, vals, hist, lookback, ctr,

@@ -525,7 +525,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         return set_err(nullptr, SC_E_INVALID, "negative sub-iteration count");
     // The periodic extension wraps neighbourhoods over the cells the box
     // spans; with fewer than three a cell would be visited twice.
-    if (cfg->periodic && ceilf(cfg->sim_size / cfg->grid_cell_size) < 3.0f)
+    if (cfg->periodic && floorf(cfg->sim_size / cfg->grid_cell_size) < 3.0f)
         return set_err(nullptr, SC_E_INVALID, "a periodic box needs at least 3 grid cells per axis");
 
     sc_sim *s = new sc_sim();
@@ -583,6 +583,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.listLimit = 1 << 30;
     P.periodic = cfg->periodic != 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
+    if (cfg->periodic) P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
     if (const char *lim = getenv("SC_PAIR_LIST_LIMIT")) P.listLimit = std::max(0, atoi(lim));
     // Tile capacities of the metabolic sweeps from the mean occupancy of the
     // cells a tile spans, with room for fluctuations.  The tiled sweep is

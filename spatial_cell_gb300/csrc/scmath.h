@@ -606,6 +606,16 @@ SC_HD sc_f3 sc_wrap3(sc_f3 v, float L) { return sc_make_f3(sc_wrap1(v.x, L), sc_
 // The reference's cell index (grid.cuh:13-17): min((uint)(c / cell), n - 1).
 // The float -> unsigned conversion saturates as the GPU's cvt.rzi.u32.f32
 // does (negative and NaN -> 0), which keeps the host build defined too.
+// Cells per axis of a periodic box and their width: the box split into
+// floor(L / cell) equal cells, each at least `cell` wide, so the 27 cells
+// around an item hold every item within `cell` of it, across the faces too.
+SC_HD int sc_periodic_cells(float L, float cell, float *width) {
+    const float q = floorf(L / cell);
+    const int n = q >= 1.0f ? (int)q : 1;
+    *width = L / (float)n;
+    return n;
+}
+
 SC_HD uint32_t sc_grid_idx(float c, float cell, int n) {
     float q = c / cell;
     uint32_t g = !(q > 0.0f) ? 0u : (q >= 4294967296.0f ? 0xffffffffu : (uint32_t)q);

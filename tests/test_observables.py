@@ -108,3 +108,40 @@ def test_pair_histogram_refuses_radius_beyond_a_cell(product):
     cfg, gpu, _ = _engines(product)
     with pytest.raises(ScError):
         gpu.pair_histogram(-1, -1, cfg.grid_cell_size * 1.5, 8)
+
+
+@pytest.mark.gpu
+def test_ensemble_msd_and_rdf_after_1000_steps(product):
+    """The small workload's physics (1,024 particles, 2,048 metabolic items,
+    periodic 50 nm cube) for 1000 steps on the device and on the CPU oracle:
+    the device's FP64 MSD and pair-distance histogram stay within 1 % of the
+    host oracle's (they agree to rounding, the trajectories being identical)."""
+    from oracle.engine import OracleEngine
+    n, nm = 1024, 2048
+    cfg = scenes.workload_config("plain_small", num_particles=n, num_metabolic_particles=nm,
+                                 sim_size=200.0 * (n / 65536.0) ** (1.0 / 3.0), seed=3)
+    rng = np.random.default_rng(3)
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    p = scenes.uniform_particles(rng, n, cfg.sim_size, types)
+    m = scenes.uniform_metabolic(rng, nm, cfg.sim_size, types, cfg.num_metabolites)
+    gpu = product.Simulation(cfg, types, rules)
+    cpu = OracleEngine("port", cfg, types, rules)
+    for e in (gpu, cpu):
+        e.load_state(p, m, step=0, next_particle_id=n)
+        e.prepare()
+    gpu.mark_positions()
+    pc, mc = cpu.export_state()
+    origins = (obs.mark(pc), obs.mark(mc))
+    for e in (gpu, cpu):
+        e.step(1000)
+    got = gpu.observe()
+    pc, mc = cpu.export_state()
+    for k, recs in enumerate((pc, mc)):
+        ref = obs.observe(recs, origins[k], cfg.sim_size, True)
+        assert abs(got["msd"][k] - ref["msd"]) <= 0.01 * ref["msd"]
+        assert got["msd"][k] == pytest.approx(ref["msd"], rel=1e-12)
+    h = gpu.pair_histogram(-1, -1, 6.0, 24).astype(np.float64)
+    ref_h = obs.pair_histogram(pc, -1, -1, 6.0, 24, cfg.sim_size, True).astype(np.float64)
+    big = ref_h >= 100
+    assert (np.abs(h[big] - ref_h[big]) <= 0.01 * ref_h[big]).all()
+    assert h.tolist() == ref_h.tolist()

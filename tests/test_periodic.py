@@ -100,6 +100,31 @@ def test_pair_across_the_face_interacts_through_the_image():
     assert moved[1] > 0.0
 
 
+def test_pair_across_the_face_of_a_box_not_a_multiple_of_the_cell():
+    """A 50 nm box with 6 nm cells is split into 8 equal cells of 6.25 nm (not
+    8 of 6 and a 2 nm sliver), so a pair 4 nm apart across the face, one of
+    them 3 nm inside it, is in neighbouring cells and collides (radii 2.5)."""
+    box = 50.0
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    p = scenes.blank_particles(2)
+    p["id"] = [0, 1]
+    p["type"] = scenes.TYPE_A
+    p["radius"] = types["radius"][scenes.TYPE_A]
+    p["pos"] = [[1.0, 20.0, 20.0], [box - 3.0, 20.0, 20.0]]
+    p["rot"] = [[0, 0, 0, 1]] * 2
+    p["angular_velocity"] = [[0, 0, 0, 1]] * 2
+    m = scenes.uniform_metabolic(np.random.default_rng(0), 4, 8.0, types, 10)
+    m["pos"] += np.float32(10.0)
+    cfg = scenes.workload_config("plain_small", num_particles=8, num_metabolic_particles=8, sim_size=box,
+                                 num_metabolites=10, seed=2, periodic=1, movement_noise_scale=0.0,
+                                 rotation_noise_scale=0.0, relaxation_steps=4)
+    e = _engine(cfg, types, rules, p, m)
+    e.run_phase(abi.PHASE_SORT_PARTICLES)
+    e.run_phase(abi.PHASE_RELAX, 0)
+    gp, _ = e.export_state()
+    assert np.abs(gp["velocity"]).max() > 0.0  # 4 nm < 2.5 + 2.5: they overlap and push apart
+
+
 def test_oracle_rejects_a_box_of_fewer_than_three_cells():
     from oracle.engine import OracleEngine
     cfg = abi.make_config(num_particles=8, num_metabolic_particles=8, sim_size=12.0, grid_cell_size=6.0,
