@@ -497,6 +497,18 @@ int ensure_staging(sc_sim *s, size_t bytes) {
     return SC_OK;
 }
 
+// The AoS staging buffer is only needed while records cross the boundary:
+// it goes back to the device's pool (stream-ordered, no synchronisation)
+// after each load, generation and export, which leaves a resident sim
+// 304 bytes per metabolic particle lighter.
+void release_staging(sc_sim *s) {
+    if (!s->staging) return;
+    cudaFreeAsync(s->staging, s->st);
+    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->staging));
+    s->staging = nullptr;
+    s->stagingBytes = 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -783,6 +795,7 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     SC_CK(s, cudaStreamSynchronize(s->st));
     rc = check_launch(s);
     if (rc) return rc;
+    release_staging(s);
     s->loaded = true;
     return SC_OK;
 }
@@ -956,6 +969,7 @@ int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *me
                                  cudaMemcpyDeviceToHost, s->st));
     }
     SC_CK(s, cudaStreamSynchronize(s->st));
+    release_staging(s);
     return check_launch(s);
 }
 
@@ -1042,6 +1056,7 @@ static int generate_into(sc_sim *s, int n, int nm, uint64_t seed, const std::fun
     SC_CK(s, cudaStreamSynchronize(s->st));
     rc = check_launch(s);
     if (rc) return rc;
+    release_staging(s);
     s->loaded = true;
     return SC_OK;
 }
