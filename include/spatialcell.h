@@ -181,6 +181,9 @@ typedef struct sc_config {
                                  [0, simSize]); 1: periodic box (minimum-image
                                  pairs, wrapped cells and positions; needs at
                                  least 3 cells per axis) */
+    int32_t walls;            /* walled box (periodic = 0): 0 the reference's clamp of
+                                 positions to [0, simSize]; 1 reflecting walls (a step
+                                 past a wall is mirrored back into the box) */
     uint64_t seed;            /* Philox key of the Brownian noise */
 } sc_config;
 

@@ -262,7 +262,9 @@ void apply_velocities(const scp_sim &s, std::vector<T> &items, int n, float f) {
     for (int i = 0; i < n; i++) {
         T &p = items[i];
         if (!(p.flags & kActive)) continue;
-        p.pos = s.periodic ? sc_wrap3(p.pos + p.vel * f, s.cfg.sim_size) : clamp(p.pos + p.vel * f, 0.0f, s.cfg.sim_size);
+        p.pos = s.periodic ? sc_wrap3(p.pos + p.vel * f, s.cfg.sim_size)
+                           : (s.cfg.walls ? sc_reflect3(p.pos + p.vel * f, s.cfg.sim_size)
+                                          : clamp(p.pos + p.vel * f, 0.0f, s.cfg.sim_size));
         p.vel *= s.cfg.velocity_decay;
         p.rot = sc_qmul(sc_slerp(sc_qid(), p.angVel, f), p.rot);
         p.rot /= length(p.rot);

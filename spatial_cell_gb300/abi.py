@@ -138,6 +138,7 @@ class Config(ctypes.Structure):
         ("report_every_nth_frame", ctypes.c_int32),
         ("num_metabolites", ctypes.c_int32),
         ("periodic", ctypes.c_int32),
+        ("walls", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
     ]
 
@@ -177,7 +178,7 @@ DEFAULT_CONFIG = dict(num_particles=65536, num_metabolic_particles=65536, steps=
                       movement_noise_scale=0.7, rotation_noise_scale=0.05, metabolite_movement_noise_scale=1.5,
                       velocity_decay=0.7, angular_velocity_decay=0.7, noise_coordination_steps=16,
                       relaxation_steps=32, metabolite_diffusion_steps=8, persist_every_nth_frame=1,
-                      report_every_nth_frame=10, num_metabolites=10, periodic=0, seed=42)
+                      report_every_nth_frame=10, num_metabolites=10, periodic=0, walls=0, seed=42)
 
 
 def make_config(**kw):

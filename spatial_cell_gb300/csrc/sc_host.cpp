@@ -132,6 +132,7 @@ extern "C" int sc_config_load_json(const char *path, sc_config *c) {
     I("reportEveryNthFrame", &c->report_every_nth_frame);
     I("numMetabolites", &c->num_metabolites);
     I("periodic", &c->periodic);
+    I("walls", &c->walls);
     if (const scjson::Value *m = v.find("seed")) c->seed = (uint64_t)(m->type == scjson::Value::Int ? m->i : (long long)m->as_double());
     return SC_OK;
 }

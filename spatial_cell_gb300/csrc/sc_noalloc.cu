@@ -86,6 +86,7 @@ extern "C" int sc_sort_cells_static(const sc_config *cfg, const void *pos, const
     P.bits = bits;
     P.cells = (uint32_t)ngrid * (uint32_t)ngrid * (uint32_t)ngrid;
     P.periodic = cfg->periodic != 0;
+    P.walls = cfg->walls != 0;
     P.nUsed = (int)ceilf(cfg->grid_cell_size > 0.0f ? cfg->sim_size / cfg->grid_cell_size : 0.0f);
     if (cfg->periodic && cfg->grid_cell_size > 0.0f)
         P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);

@@ -594,6 +594,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     // neighbourhood-scan path of every kernel); unset means full capacity.
     P.listLimit = 1 << 30;
     P.periodic = cfg->periodic != 0;
+    P.walls = cfg->walls != 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
     if (cfg->periodic) P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
     if (const char *lim = getenv("SC_PAIR_LIST_LIMIT")) P.listLimit = std::max(0, atoi(lim));

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_apply_velocities(const int *__re
     float4 p4 = pos[i];
     sc_f3 p = sc_make_f3(p4.x, p4.y, p4.z);
     sc_f3 v = ld3(vel, i);
-    p = P.periodic ? sc_wrap3(p + v * f, P.simSize) : clamp(p + v * f, 0.0f, P.simSize);
+    p = P.periodic ? sc_wrap3(p + v * f, P.simSize)
+                   : (P.walls ? sc_reflect3(p + v * f, P.simSize) : clamp(p + v * f, 0.0f, P.simSize));
     v *= P.velDecay;
     sc_f4 av = ld4(angvel, i);
     sc_f4 r = sc_qmul(sc_slerp(sc_qid(), av, f), ld4(rot, i));
@@ -795,8 +796,9 @@ __device__ __forceinline__ void relax_class_item(const ScParams &P, const RelaxA
 
 // The items of one work class, grid-stride over the class's index segment.
 // The bonded class goes block by block, its items ranked by bond-match
-// count inside the block, so a warp's lanes walk about as many bond terms
-// (items with more bonds would otherwise hold back the rest of their warp).
+// count (chain-bonded apart from rule-bonded) inside the block, so a warp's
+// lanes walk about as many bond terms of the same kind (items with more
+// bonds would otherwise hold back the rest of their warp).
 template <int MODE>
 __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
     const int n = A.classCount[MODE];
@@ -807,8 +809,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
             const int t = base + threadIdx.x;
             const int i = t < n ? idx[t] : -1;
             s_item[threadIdx.x] = i;
+            // rank key: bond-match count, chain-bonded items apart from rule-bonded ones (their
+            // pose terms are different code)
+            int key = 0;
+            if (i >= 0)
+                key = (A.matchN[i] & SC_MATCH_COUNT) +
+                      (A.bonds[(size_t)i * 24] == SC_INTERACTION_TYPE_CHAIN ? SC_MAX_ACTIVE_INTERACTIONS + 1 : 0);
             int src, cs;
-            count_rank<SC_MAX_ACTIVE_INTERACTIONS>(i >= 0, i >= 0 ? (A.matchN[i] & SC_MATCH_COUNT) : 0, &src, &cs);
+            count_rank<2 * SC_MAX_ACTIVE_INTERACTIONS + 1>(i >= 0, key, &src, &cs);
             if (cs >= 0) relax_class_item<MODE>(P, A, s_item[src]);
             __syncthreads();  // the ranking's shared arrays are reused by the next round
         }

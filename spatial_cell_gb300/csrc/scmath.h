@@ -606,6 +606,14 @@ SC_HD sc_f3 sc_wrap3(sc_f3 v, float L) { return sc_make_f3(sc_wrap1(v.x, L), sc_
 // The reference's cell index (grid.cuh:13-17): min((uint)(c / cell), n - 1).
 // The float -> unsigned conversion saturates as the GPU's cvt.rzi.u32.f32
 // does (negative and NaN -> 0), which keeps the host build defined too.
+// A position mirrored back into [0, L] at reflecting walls (an excursion
+// longer than the box is clamped after the mirror).
+SC_HD float sc_reflect1(float x, float L) {
+    const float r = x < 0.0f ? -x : (x > L ? L - (x - L) : x);
+    return fminf(fmaxf(r, 0.0f), L);
+}
+SC_HD sc_f3 sc_reflect3(sc_f3 v, float L) { return sc_make_f3(sc_reflect1(v.x, L), sc_reflect1(v.y, L), sc_reflect1(v.z, L)); }
+
 // Cells per axis of a periodic box and their width: the box split into
 // floor(L / cell) equal cells, each at least `cell` wide, so the 27 cells
 // around an item hold every item within `cell` of it, across the faces too.

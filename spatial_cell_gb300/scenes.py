@@ -176,8 +176,8 @@ def vesicle_groups(box, shell_r=400.0, lipids=2_000_000, interior=6_000_000, com
 
 
 def vesicle_workload(scale=1.0):
-    """The crowded vesicle stress case (900 nm walled box, 2 M lipids on a
-    400 nm bilayer shell, 6 M interior particles, 50 k 20-particle complexes,
+    """The crowded vesicle stress case (900 nm box with reflecting walls, 2 M
+    lipids on a 400 nm bilayer shell, 6 M interior particles, 50 k 20-particle complexes,
     32 M metabolic items, seed 5), every count scaled by `scale` and every
     length by its cube root.  Returns (config, groups, metabolic count)."""
     s = scale ** (1.0 / 3.0)
@@ -188,7 +188,7 @@ def vesicle_workload(scale=1.0):
     nm = int(32_000_000 * scale)
     cfg = abi.make_config(num_particles=n, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
                           max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5,
-                          steps=1000, periodic=0)
+                          steps=1000, periodic=0, walls=1)
     return cfg, groups, nm
 
 
@@ -266,7 +266,7 @@ def _link_serially(p, start, end, itype=abi.INTERACTION_TYPE_CHAIN):
         b["n_active_interactions"] = k + 1
 
 
-def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, periodic=0):
+def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, periodic=0, walls=0):
     """A dense small box with uniform particles of all kinds, a few wrapped
     chains, pre-bonded rule pairs, a test bond, and metabolites.  Returns
     (config, types, rules, particles, metabolic, next_particle_id)."""
@@ -330,5 +330,6 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, p
     cfg = abi.make_config(num_particles=n + capacity_slack, num_metabolic_particles=nm + 16, sim_size=box,
                           grid_cell_size=6.0, max_interaction_distance=5.5, max_diffusion_distance=6.0,
                           num_metabolites=species, seed=1000 + seed, noise_coordination_steps=4,
-                          relaxation_steps=6, metabolite_diffusion_steps=3, steps=10, periodic=periodic)
+                          relaxation_steps=6, metabolite_diffusion_steps=3, steps=10, periodic=periodic,
+                          walls=walls)
     return cfg, types, rules, p, m, n

@@ -31,11 +31,12 @@ def _same(cfg, gpu, cpu, what):
     assert_same_counters(gpu.counters(), cpu.counters(), what=what)
 
 
-@pytest.mark.parametrize("seed,periodic", [(0, 0), (1, 0), (2, 1), (3, 1)])
-def test_lockstep_every_phase(product, seed, periodic):
+@pytest.mark.parametrize("seed,periodic,walls", [(0, 0, 0), (1, 0, 0), (2, 1, 0), (3, 1, 0), (4, 0, 1)])
+def test_lockstep_every_phase(product, seed, periodic, walls):
     """Prepare + two steps, comparing the whole state after every kernel
     (reference walls, and the periodic box extension)."""
-    cfg, gpu, cpu = _engines(product, scenes.test_scene(seed, n=900, nm=1800, box=42.0, periodic=periodic))
+    cfg, gpu, cpu = _engines(product, scenes.test_scene(seed, n=900, nm=1800, box=42.0, periodic=periodic,
+                                                        walls=walls))
     prep = [(abi.PHASE_SORT_PARTICLES, 0), (abi.PHASE_SORT_METABOLIC, 0), (abi.PHASE_REMOVE_INTERFERING, 0),
             (abi.PHASE_COMPLEXIFY, -1)]
     seq = prep + step_phases(cfg) * 2

@@ -125,6 +125,35 @@ def test_pair_across_the_face_of_a_box_not_a_multiple_of_the_cell():
     assert np.abs(gp["velocity"]).max() > 0.0  # 4 nm < 2.5 + 2.5: they overlap and push apart
 
 
+def test_reflecting_walls_mirror_a_step_past_the_wall():
+    """With walls = 1 a step that leaves the box is mirrored back into it
+    (the reference clamps it onto the wall instead)."""
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    box = 30.0
+    p = scenes.blank_particles(2)
+    p["id"] = [0, 1]
+    p["type"] = scenes.DUMMY
+    p["radius"] = types["radius"][scenes.DUMMY]
+    p["pos"] = [[0.5, 15.0, 15.0], [29.0, 15.0, 15.0]]
+    p["velocity"] = [[-2.0, 0.0, 0.0], [4.0, 0.0, 0.0]]
+    p["rot"] = [[0, 0, 0, 1]] * 2
+    p["angular_velocity"] = [[0, 0, 0, 1]] * 2
+    m = scenes.uniform_metabolic(np.random.default_rng(0), 4, 8.0, types, 10)
+    m["pos"] += np.float32(10.0)
+    got = {}
+    for walls in (0, 1):
+        cfg = scenes.workload_config("plain_small", num_particles=8, num_metabolic_particles=8, sim_size=box,
+                                     num_metabolites=10, seed=2, periodic=0, walls=walls)
+        e = _engine(cfg, types, rules, p, m)
+        e.run_phase(abi.PHASE_APPLY_VELOCITIES)
+        gp, _ = e.export_state()
+        gp = gp[(gp["flags"] & abi.PARTICLE_FLAG_ACTIVE) != 0]
+        got[walls] = gp["pos"][np.argsort(gp["id"])][:, 0]
+    # x + 0.45 v: 0.5 - 0.9 = -0.4 and 29 + 1.8 = 30.8
+    assert got[0].tolist() == [0.0, 30.0]
+    assert np.allclose(got[1], [0.4, 29.2], atol=1e-5)
+
+
 def test_oracle_rejects_a_box_of_fewer_than_three_cells():
     from oracle.engine import OracleEngine
     cfg = abi.make_config(num_particles=8, num_metabolic_particles=8, sim_size=12.0, grid_cell_size=6.0,

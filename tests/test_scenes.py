@@ -165,7 +165,7 @@ def test_device_vesicle_equals_oracle_and_steps_bit_exact(product):
     n, nm, seed = abi.scene_particles(groups), 9000, 17
     cfg = abi.make_config(num_particles=n + 64, num_metabolic_particles=nm + 64, sim_size=box, grid_cell_size=6.0,
                           max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5,
-                          steps=10, periodic=0)
+                          steps=10, periodic=0, walls=1)
     types, rules = _types(), scenes.baseline_rules()
     p, m = _gen(groups, nm=nm, box=box, species=cfg.num_metabolites, seed=seed, types=types)
     g = product.Simulation(cfg, types, rules)
