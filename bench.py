@@ -327,7 +327,7 @@ def serving_sample(args, capacity):
 
 
 def vesicle_sample(args, native, torch):
-    """The crowded vesicle case (walled 900 nm box: 2 M lipids on a 400 nm
+    """The crowded vesicle case (900 nm box with reflecting walls: 2 M lipids on a 400 nm
     bilayer shell, 6 M interior particles, 50 k 20-particle lattice complexes,
     32 M metabolic items; counts scaled by --vesicle-scale), generated on the
     device: particle-steps/s over --vesicle-steps steps after a warm-up step,
@@ -353,7 +353,7 @@ def vesicle_sample(args, native, torch):
     sims[0].sync()
     one = items * k / (time.perf_counter() - t0)
     out = {"scale": args.vesicle_scale, "particles": cfg.num_particles, "metabolic_particles": nm,
-           "box_nm": cfg.sim_size, "walls": True, "steps": k, "value": one, "unit": UNIT,
+           "box_nm": cfg.sim_size, "walls": "reflecting", "steps": k, "value": one, "unit": UNIT,
            "scene": "2 leaflets r=400/396 nm (lipids uniform on each sphere), dummy/A/B 70/15/15 in the ball "
                     "r<390 nm, 20-site lattice complexes (3 nm, tree of chain bonds) in r<384 nm, metabolic "
                     "uniform in the box; generated on the device (sc_generate_scene), seed 5",
