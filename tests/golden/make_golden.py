@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle import build as obuild  # noqa: E402
 from oracle.engine import OracleEngine  # noqa: E402
 from spatial_cell_gb300 import abi, scenes  # noqa: E402
 
@@ -39,7 +40,36 @@ def scene_workload():
     return cfg, types, rules, p, m, n
 
 
-SCENES = {"golden_mixed": scene_mixed, "golden_workload": scene_workload}
+def scene_tables():
+    """The shipped tables (universe-config/gen/large-molecules.json, 179 types;
+    complexification.json, 648 rules with 396 transitions and 64
+    polymerisations) on a dense walled box of lipids and the partner types
+    of the rules that complexify forms directly."""
+    from spatial_cell_gb300 import native
+    gen = os.path.join(os.path.dirname(os.path.dirname(obuild.REFERENCE_SRC)), "universe-config", "gen")
+    types = native.load_types_json(os.path.join(gen, "large-molecules.json"))
+    rules = native.load_rules_json(os.path.join(gen, "complexification.json"))
+    direct = rules[rules["only_via_transition"] == 0]
+    kinds = sorted({int(t) for t in np.concatenate([direct["first_partner_type"], direct["second_partner_type"]])
+                    if t >= 0 and types["radius"][t] > 0})
+    n, nm, box = 1600, 1200, 44.0
+    rng = np.random.default_rng(91)
+    ty = np.where(rng.random(n) < 0.2, 0, rng.choice(kinds, n)).astype(np.int32)
+    p = scenes.blank_particles(n)
+    p["id"] = np.arange(n, dtype=np.int32)
+    p["type"] = ty
+    p["radius"] = types["radius"][ty]
+    p["hydrophobic"] = types["hydrophobic"][ty]
+    p["pos"] = (rng.random((n, 3)) * box).astype(np.float32)
+    p["rot"] = scenes.random_quaternions(rng, n)
+    m = scenes.uniform_metabolic(rng, nm, box, types, 10)
+    cfg = abi.make_config(num_particles=n + 256, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
+                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=10, seed=91,
+                          steps=10, relaxation_steps=6, metabolite_diffusion_steps=3, periodic=0)
+    return cfg, types, rules, p, m, n
+
+
+SCENES = {"golden_mixed": scene_mixed, "golden_workload": scene_workload, "golden_tables": scene_tables}
 
 
 def generate(name):
@@ -67,5 +97,5 @@ def generate(name):
 
 
 if __name__ == "__main__":
-    for n in SCENES:
+    for n in (sys.argv[1:] or SCENES):
         print(generate(n), os.path.getsize(os.path.join(HERE, n + ".npz")))

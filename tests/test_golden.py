@@ -13,7 +13,7 @@ from spatial_cell_gb300 import abi
 from tests.helpers import assert_same_state, diff_fields
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ["golden_mixed", "golden_workload"]
+NAMES = ["golden_mixed", "golden_workload", "golden_tables"]
 
 
 def _load(name):
