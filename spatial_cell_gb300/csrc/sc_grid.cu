@@ -188,23 +188,29 @@ __global__ void k_cell_start(const uint32_t *__restrict__ keys, int n, uint32_t 
     cellStart[c] = (uint32_t)lo;
 }
 
+// The gathers load every field of the source slot before storing any: the
+// destination arrays are other buffers, but the compiler cannot know that,
+// and interleaved loads and stores would keep one load in flight per thread.
 __global__ void __launch_bounds__(SC_THREADS) k_gather_particles(const uint32_t *__restrict__ perm, int n, PFields src,
                                                                  PFields dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = (int)perm[i];
-    dst.pos[i] = src.pos[s];
-    dst.vel[i] = src.vel[s];
-    dst.rot[i] = src.rot[s];
-    dst.angvel[i] = src.angvel[s];
-    dst.posnoise[i] = src.posnoise[s];
-    dst.angnoise[i] = src.angnoise[s];
-    dst.dbg[i] = src.dbg[s];
-    dst.info[i] = src.info[s];
-    dst.state[i] = src.state[s];
-    dst.lscs[i] = src.lscs[s];
-    dst.spoly[i] = src.spoly[s];
-    int nb = src.nb[s];
+    const float4 pos = src.pos[s], vel = src.vel[s], rot = src.rot[s], angvel = src.angvel[s];
+    const float4 posnoise = src.posnoise[s], angnoise = src.angnoise[s], dbg = src.dbg[s];
+    const int4 info = src.info[s];
+    const int state = src.state[s], lscs = src.lscs[s], spoly = src.spoly[s], nb = src.nb[s];
+    dst.pos[i] = pos;
+    dst.vel[i] = vel;
+    dst.rot[i] = rot;
+    dst.angvel[i] = angvel;
+    dst.posnoise[i] = posnoise;
+    dst.angnoise[i] = angnoise;
+    dst.dbg[i] = dbg;
+    dst.info[i] = info;
+    dst.state[i] = state;
+    dst.lscs[i] = lscs;
+    dst.spoly[i] = spoly;
     dst.nb[i] = nb;
     int nw = min(max(nb, 0), SC_MAX_ACTIVE_INTERACTIONS) * 3;
     const int *b = src.bonds + (size_t)s * 24;
@@ -217,17 +223,27 @@ __global__ void __launch_bounds__(SC_THREADS) k_gather_metabolic(const uint32_t 
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = (int)perm[i];
-    dst.pos[i] = src.pos[s];
-    dst.vel[i] = src.vel[s];
-    dst.rot[i] = src.rot[s];
-    dst.angvel[i] = src.angvel[s];
-    dst.posnoise[i] = src.posnoise[s];
-    dst.angnoise[i] = src.angnoise[s];
-    dst.dbg[i] = src.dbg[s];
-    dst.info[i] = src.info[s];
-    dst.state[i] = src.state[s];
-    dst.orig[i] = src.orig[s];
-    for (int k = 0; k < sp4; k++) dst.met[(size_t)i * sp4 + k] = src.met[(size_t)s * sp4 + k];
+    const float4 pos = src.pos[s], vel = src.vel[s], rot = src.rot[s], angvel = src.angvel[s];
+    const float4 posnoise = src.posnoise[s], angnoise = src.angnoise[s], dbg = src.dbg[s];
+    const int4 info = src.info[s];
+    const int state = src.state[s], orig = src.orig[s];
+    float4 met[3];  // up to 12 species
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (k < sp4) met[k] = src.met[(size_t)s * sp4 + k];
+    dst.pos[i] = pos;
+    dst.vel[i] = vel;
+    dst.rot[i] = rot;
+    dst.angvel[i] = angvel;
+    dst.posnoise[i] = posnoise;
+    dst.angnoise[i] = angnoise;
+    dst.dbg[i] = dbg;
+    dst.info[i] = info;
+    dst.state[i] = state;
+    dst.orig[i] = orig;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (k < sp4) dst.met[(size_t)i * sp4 + k] = met[k];
 }
 
 // ---- host-side launchers -----------------------------------------------------
