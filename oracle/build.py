@@ -63,7 +63,7 @@ def reference_available():
 
 def build_ref(force=False):
     """Compiles the reference's kernels for the host; None if the reference
-    tree is absent (as on the GPU machine)."""
+    tree is absent."""
     if not reference_available():
         return None
     out = ref_path()

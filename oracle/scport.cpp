@@ -1,6 +1,6 @@
 // scport.cpp -- CPU restatement of spatial_cell_sim's step.
 //
-// TEST INFRASTRUCTURE ONLY: the checker of the sm_103a step (tests/,
+// TEST INFRASTRUCTURE ONLY: what the sm_103a step is checked against (tests/,
 // __graft_entry__.smoke()) and the timed CPU baseline of bench.py.  Nothing
 // in the product links or calls it.
 //
