@@ -51,6 +51,7 @@ struct ScBuffers {
     uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
     int *ovfPP, *ovfM;            // overflowed items
     int *warpOffM;                // metabolic pair pool: first entry of every warp's region
+    int *workP;                   // particle work list (the items complexify scans)
     size_t poolCapM;              // entries (16 bytes) the metabolic pair pool (listM) holds
     int *warpOffLM;               // lipid-metabolic pair pool: the same
     uint8_t *lipidP;              // per sorted particle slot: active lipid (after each particle sort)

@@ -1533,31 +1533,54 @@ __device__ __forceinline__ bool group_active_in(const int *__restrict__ b, int n
 // ---- interactions.cuh:216-346 complexify --------------------------------------
 // New interactions are appended at slots [nb, nb') of the item's own list,
 // which no neighbour reads (they read [0, nb)); nb' goes to the next buffer.
+// The items complexify can act on, collected before the scan so the scan's
+// warps hold only such items (they are a small, scattered part of the
+// particles: left in place, almost every warp would carry one or two
+// scanning lanes).  No rule of an item's type can add a bond when each is
+// transition-only or its group is already active on the item (bonds are
+// only added by the scan, so a blocked rule stays blocked); such an item's
+// bond count is passed through here.
+__global__ void __launch_bounds__(SC_THREADS) k_complexify_select(ScParams P, const int *__restrict__ nActivePtr,
+                                                                  const int4 *__restrict__ info,
+                                                                  const int *__restrict__ nbIn,
+                                                                  int *__restrict__ nbOut,
+                                                                  const int *__restrict__ bonds,
+                                                                  int *__restrict__ work, int *__restrict__ workCount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool open = false;
+    if (i < *nActivePtr) {
+        const int4 in = info[i];
+        const int pnb = nbIn[i];
+        int cs = 0, ce = 0;
+        if ((in.z & SC_ACTIVE) && in.y >= 0 && 2 * in.y + 1 < P.nPidx) {
+            cs = P.pidx[2 * in.y];
+            ce = P.pidx[2 * in.y + 1];
+        }
+        for (int k = cs; k < ce && !open && pnb < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+            const sc_rule &pii = P.prules[k];
+            open = !pii.only_via_transition &&
+                   !(pii.group >= 0 && group_active_in(bonds + (size_t)i * 24, pnb, pii.group));
+        }
+        if (!open) nbOut[i] = pnb;
+    }
+    // warp-aggregated append (order within the list is free: items do not read what others add)
+    const unsigned m = __ballot_sync(0xffffffffu, open);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(workCount, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (open) work[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_complexify(
-    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
     const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
     const int *__restrict__ state, const int *__restrict__ nbIn, int *__restrict__ nbOut, int *bonds) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
+    const int i = work[t];
     int4 in = info[i];
     int pnb = nbIn[i];
-    int cs = 0, ce = 0;
-    if ((in.z & SC_ACTIVE) && in.y >= 0 && 2 * in.y + 1 < P.nPidx) {
-        cs = P.pidx[2 * in.y];
-        ce = P.pidx[2 * in.y + 1];
-    }
-    // No rule of its type can add a bond when each is transition-only or
-    // its group is already active on the item (bonds are only added below,
-    // so a blocked rule stays blocked): the scan would change nothing.
-    bool open = false;
-    for (int k = cs; k < ce && !open && pnb < SC_MAX_ACTIVE_INTERACTIONS; k++) {
-        const sc_rule &pii = P.prules[k];
-        open = !pii.only_via_transition && !(pii.group >= 0 && group_active_in(bonds + (size_t)i * 24, pnb, pii.group));
-    }
-    if (!open) {
-        nbOut[i] = pnb;
-        return;
-    }
+    const int cs = P.pidx[2 * in.y], ce = P.pidx[2 * in.y + 1];
     float4 p4 = pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, ppos, SC_BINNED_P);
@@ -1602,6 +1625,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     });
     (void)nb0;
     nbOut[i] = pnb;
+  }
 }
 
 // ---- interactions.cuh:349-555 transitionInteractions -------------------------
@@ -2289,10 +2313,13 @@ void sc_phase_complexify(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     PFields F = B.P(), X = B.Pnext();
-    k_complexify<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.rot, F.info,
-                                                           F.state, F.nb, X.nb, F.bonds);
+    cudaMemsetAsync(&B.ctr->workCount, 0, sizeof(int), c.st);
+    k_complexify_select<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, &B.ctr->nActive, F.info, F.nb, X.nb, F.bonds,
+                                                                  B.workP, &B.ctr->workCount);
+    k_complexify<<<std::min(nblocks(c.P.N), c.gridCap), SC_THREADS, 0, c.st>>>(
+        c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot, F.info, F.state, F.nb, X.nb, F.bonds);
     B.cp[FP_NB] ^= 1;
-    (*c.launches)++;
+    (*c.launches) += 2;
 }
 
 void sc_phase_transition(ScLaunchCtx &c) {
