@@ -896,7 +896,8 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
 // its capacity, or every list of a block the pool has no room for, is marked
 // overflowed (cnt = INT_MAX; listed in `ovf` when given).  Returns the item,
 // how many pairs to write and where its first one goes (entry k at
-// out[32 k]).
+// out[32 k]).  With `items`, thread t of the block stands for item
+// items[b0 + t] (a compacted list) and perm holds those items.
 struct PoolSlot {
     int i, n;
     uint4 *out;
@@ -905,7 +906,8 @@ template <int K>
 __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int c, uint4 *__restrict__ pool,
                                               int poolCap, unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
                                               int *__restrict__ cnt, int *__restrict__ perm, int cap,
-                                              int *__restrict__ ovf, int *__restrict__ ovfCount) {
+                                              int *__restrict__ ovf, int *__restrict__ ovfCount,
+                                              const int *__restrict__ items = nullptr) {
     __shared__ int s_n[SC_THREADS / 32];
     __shared__ int s_base;
     const int b0 = blockIdx.x * SC_THREADS, t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -934,13 +936,13 @@ __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int
     for (int w = 0; w < warp; w++) off += s_n[w] * 32;
     const int g = b0 + t;
     if (g < cap) {
-        perm[g] = cs >= 0 ? b0 + src : -1;
+        perm[g] = cs >= 0 ? (items ? items[b0 + src] : b0 + src) : -1;
         cnt[g] = ovfl ? INT_MAX : max(cs, 0);
         if (lane == 0) warpOff[g >> 5] = s_base < 0 ? 0 : off;
     }
     if (ovfl && ovf) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
     PoolSlot r;
-    r.i = b0 + src;
+    r.i = cs >= 0 && items ? items[b0 + src] : b0 + src;
     r.n = n;
     r.out = pool + (n ? off : 0) + lane;
     return r;
@@ -1414,25 +1416,42 @@ __device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t 
 // evaluates, in a pool region of the list position's warp (pool_take),
 // 16 bytes {neighbour, A.x, A.y, A.z} per entry.  An overflowed lipid
 // (cnt INT_MAX) is left to the scan of k_relax_partners.
+// The active lipids, compacted (warp-aggregated appends: the order of the
+// lists does not matter, each lipid's own list keeps the scan's order), so
+// the LM build's warps hold only lipids.
+__global__ void __launch_bounds__(SC_THREADS) k_lipid_select(const int *__restrict__ nActivePtr,
+                                                             const int4 *__restrict__ pinfo, int *__restrict__ work,
+                                                             int *__restrict__ workCount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool lip = false;
+    if (i < *nActivePtr) {
+        const int4 in = pinfo[i];
+        lip = (in.z & SC_ACTIVE) && in.y == SC_PARTICLE_TYPE_LIPID;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, lip);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(workCount, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (lip) work[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
-                                                         const int *__restrict__ nActivePtr,
-                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                                         const int *__restrict__ lipids,
+                                                         const int *__restrict__ lipidCount,
+                                                         const float4 *__restrict__ ppos_,
                                                          const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                          uint4 *__restrict__ pool, int poolCap,
                                                          unsigned long long *__restrict__ poolUsed,
                                                          int *__restrict__ warpOff,
                                                          uint32_t *scratch, int *__restrict__ cnt,
                                                          int *__restrict__ perm, int cap) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < *nActivePtr;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < *lipidCount;
     int c = 0;
-    if (valid) {
-        int4 in = pinfo[i];
-        if ((in.z & SC_ACTIVE) && in.y == SC_PARTICLE_TYPE_LIPID)
-            build_lm_item(P, cellStartM, i, ppos_, mpos, minfo, scratch, c);
-    }
-    const PoolSlot S =
-        pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr, nullptr);
+    if (valid) build_lm_item(P, cellStartM, lipids[t], ppos_, mpos, minfo, scratch, c);
+    const PoolSlot S = pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr,
+                                             nullptr, lipids);
     if (S.n == 0) return;
     const float4 p4 = ppos_[S.i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -2275,10 +2294,13 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     if (!B.validLM) {
         if (B.scratchLM == B.listD) B.validD = false;
         cudaMemsetAsync(&B.ctr->poolLM, 0, sizeof(B.ctr->poolLM), c.st);
+        cudaMemsetAsync(&B.ctr->workCount, 0, sizeof(int), c.st);
+        k_lipid_select<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, B.workP, &B.ctr->workCount);
         k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
-            c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info, M.pos, M.info, reinterpret_cast<uint4 *>(B.listLM),
+            c.P, B.cellStartM, B.workP, &B.ctr->workCount, F.pos, M.pos, M.info, reinterpret_cast<uint4 *>(B.listLM),
             (int)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,
             c.P.N);
+        (*c.launches)++;
         (*c.launches)++;
         B.validLM = true;
     }
