@@ -202,11 +202,12 @@ __device__ __forceinline__ uint32_t pp_flags(const ScParams &P, const Imager &IM
                                              const BondRegs &B, const float4 *__restrict__ pos,
                                              const int4 *__restrict__ info) {
     if (j == i) return 0;
-    int4 tin = info[j];
-    if (!(tin.z & SC_ACTIVE)) return 0;
+    // the cube test first: most candidates fail it, and then need no record
     float4 t4 = pos[j];
     sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
     if (outside_cube(delta, P.maxInt)) return 0;
+    int4 tin = info[j];
+    if (!(tin.z & SC_ACTIVE)) return 0;
     float dist = sc_norm3(delta);
     float s = prad + t4.w;
     int thydro = (int)(int8_t)(tin.w & 0xff);
@@ -1611,11 +1612,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     const float lim = P.maxInt;
     scan27(P, cellStart, ppos, reach(P, ppos, lim, SC_BINNED_P), [&](int j) {
         if (j == i) return;
-        int4 tin = info[j];
-        if (!(tin.z & SC_ACTIVE)) return;
         float4 t4 = pos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
         if (outside_cube(delta, lim)) return;
+        int4 tin = info[j];
+        if (!(tin.z & SC_ACTIVE)) return;
         sc_f4 trot = ld4(rot, j);
         sc_f3 tup = sc_rotate(sc_up(), trot);
         const int ttype = tin.y;
@@ -1683,11 +1684,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
         const float lim = P.maxInt;
         scan27(P, cellStart, ppos, reach(P, ppos, lim, SC_BINNED_P), [&](int j) {
             if (j == i) return;
-            int4 tin = info[j];
-            if (!(tin.z & SC_ACTIVE)) return;
             float4 t4 = pos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
             if (outside_cube(delta, lim)) return;
+            int4 tin = info[j];
+            if (!(tin.z & SC_ACTIVE)) return;
             bool loaded = false;
             sc_f4 trot;
             sc_f3 tup;
