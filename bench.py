@@ -561,7 +561,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving sample (0: skip it)")
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
-    ap.add_argument("--vesicle-steps", type=int, default=3)
+    ap.add_argument("--vesicle-steps", type=int, default=6)
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()
