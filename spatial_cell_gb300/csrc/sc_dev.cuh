@@ -244,6 +244,12 @@ __device__ __forceinline__ Reach reach(const ScParams &P, sc_f3 pos, float lim, 
     return r;
 }
 
+// A neighbour cell index c + o (c in [0, n), o in -1..1) taken around the
+// periodic box: ((c + o + n) mod n) without the integer division.
+__device__ __forceinline__ uint32_t wrap_cell(int v, int n) {
+    return (uint32_t)(v < 0 ? v + n : (v >= n ? v - n : v));
+}
+
 template <class F>
 __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__restrict__ cellStart, sc_f3 pos,
                                        const Reach &R, F &&f) {
@@ -254,7 +260,7 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
         // the z run of a column is one slot range unless it wraps
         for (int ox = R.xl; ox <= R.xh; ox++) {
             for (int oy = R.yl; oy <= R.yh; oy++) {
-                uint32_t base = cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n), 0);
+                uint32_t base = cell_key(P, wrap_cell(cx + ox, n), wrap_cell(cy + oy, n), 0);
                 if (cz + R.zl >= 0 && cz + R.zh <= n - 1) {
                     for (uint32_t j = cellStart[base | (uint32_t)(cz + R.zl)],
                                   e = cellStart[(base | (uint32_t)(cz + R.zh)) + 1];
@@ -262,7 +268,7 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
                         f((int)j);
                 } else {
                     for (int oz = R.zl; oz <= R.zh; oz++) {
-                        uint32_t key = base | (uint32_t)((cz + oz + n) % n);
+                        uint32_t key = base | wrap_cell(cz + oz, n);
                         for (uint32_t j = cellStart[key], e = cellStart[key + 1]; j < e; j++) f((int)j);
                     }
                 }
@@ -297,8 +303,8 @@ __device__ __forceinline__ void cells27(const ScParams &P, sc_f3 pos, const Reac
         for (int ox = R.xl; ox <= R.xh; ox++)
             for (int oy = R.yl; oy <= R.yh; oy++)
                 for (int oz = R.zl; oz <= R.zh; oz++)
-                    f(cell_key(P, (uint32_t)((cx + ox + n) % n), (uint32_t)((cy + oy + n) % n),
-                               (uint32_t)((cz + oz + n) % n)));
+                    f(cell_key(P, wrap_cell(cx + ox, n), wrap_cell(cy + oy, n),
+                               wrap_cell(cz + oz, n)));
         return;
     }
     for (int gx = max(cx + R.xl, 0); gx <= min(cx + R.xh, n - 1); gx++)

@@ -842,14 +842,22 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, Relax
 // recomputed only when the partner radius changes.
 struct CollisionDistCache {
     float rt = 0.0f, cd = 0.0f;
+    sc_sqrt_le le;
     bool valid = false;
     __device__ __forceinline__ float get(float rp, float r) {
         if (!valid || !(r == rt)) {
             rt = r;
             valid = true;
             cd = sc_coll_dist(rp, r);
+            le = sc_sqrt_le_make(cd);
         }
         return cd;
+    }
+    // sc_norm3(delta) <= the collision distance of (rp, r), the reference's
+    // test (metabolites.cuh:193-203), mostly without the square root
+    __device__ __forceinline__ bool collides(float rp, float r, sc_f3 delta) {
+        get(rp, r);
+        return sc_sqrt_le_test(le, sc_normsq3(delta));
     }
 };
 
@@ -873,7 +881,7 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cm.get(prad, t4.w)) {
+            if (cm.collides(prad, t4.w, delta)) {
                 if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j;
                 c++;
             }
@@ -883,7 +891,7 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
             float4 t4 = ppos_[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cp.get(prad, t4.w)) {
+            if (cp.collides(prad, t4.w, delta)) {
                 if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j | SC_M_FROM_P;
                 c++;
             }
@@ -1112,7 +1120,7 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
             float4 t4 = A.mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cm.get(prad, t4.w))
+            if (cm.collides(prad, t4.w, delta))
                 metab_pair(IM, pp, ppv, t4, A.mvelIn[j], cm.get(prad, t4.w), false, dV, w);
         }
         for (uint32_t j = A.cellStartP[key], e = A.cellStartP[key + 1]; j < e; j++) {
@@ -1120,7 +1128,7 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
             float4 t4 = A.ppos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) continue;
-            if (sc_norm3(delta) <= cp.get(prad, t4.w))
+            if (cp.collides(prad, t4.w, delta))
                 metab_pair(IM, pp, ppv, t4, A.pvel[j], cp.get(prad, t4.w), true, dV, w);
         }
     });
@@ -1259,7 +1267,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m_tile(ScParams P, const u
                 float4 t4 = spos[o];
                 sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
                 if (outside_cube(delta, lim)) continue;
-                if (sc_norm3(delta) <= cm.get(prad, t4.w)) {
+                if (cm.collides(prad, t4.w, delta)) {
                     if (c < climit) list[sc_list16_at(SC_LIST_M, i, c)] = (uint16_t)o;
                     c++;
                 }
@@ -1270,7 +1278,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m_tile(ScParams P, const u
                 float4 t4 = spos[o];
                 sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
                 if (outside_cube(delta, lim)) continue;
-                if (sc_norm3(delta) <= cp.get(prad, t4.w)) {
+                if (cp.collides(prad, t4.w, delta)) {
                     if (c < climit) list[sc_list16_at(SC_LIST_M, i, c)] = (uint16_t)o;
                     c++;
                 }
@@ -1404,7 +1412,7 @@ __device__ __forceinline__ void build_lm_item(const ScParams &P, const uint32_t 
         float4 t4 = mpos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
-        if (sc_norm3(delta) <= cc.get(prad, t4.w)) {
+        if (cc.collides(prad, t4.w, delta)) {
             if (c < min(SC_LIST_LM, P.listLimit)) list[sc_list_at(SC_LIST_LM, i, c)] = (uint32_t)j;
             c++;
         }
@@ -1519,8 +1527,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
             float4 t4 = mpos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
-            const float cd = cc.get(prad, t4.w);
-            if (sc_norm3(delta) <= cd) {
+            if (cc.collides(prad, t4.w, delta)) {
+                const float cd = cc.cd;
                 sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
                 sc_f3 nd = normalize(tpos - pp);
                 w += 2.0f;
@@ -1935,12 +1943,13 @@ __device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
+    const sc_sqrt_le within = sc_sqrt_le_make(lim);
     scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
         if (j == i || !active_m(P, info, j)) return;
         float4 t4 = pos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
         if (outside_cube(delta, lim)) return;
-        if (sc_norm3(delta) <= lim) {
+        if (sc_sqrt_le_test(within, sc_normsq3(delta))) {
             if (c < min(SC_LIST_D, P.listLimit)) list[sc_list_at(SC_LIST_D, i, c)] = (uint32_t)j;
             c++;
         }
@@ -2035,13 +2044,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
         const Imager IM(P, pp, SC_BINNED_M);
         const float lim = P.maxDiff;
+        const sc_sqrt_le within = sc_sqrt_le_make(lim);
         scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
             if (j == i) return;
             if (!active_m(P, info, j)) return;
             float4 t4 = pos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
-            if (sc_norm3(delta) <= lim) body(j);
+            if (sc_sqrt_le_test(within, sc_normsq3(delta))) body(j);
         });
     }
 #pragma unroll

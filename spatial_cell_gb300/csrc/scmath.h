@@ -388,6 +388,36 @@ SC_HD float sc_normsq3(sc_f3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
 SC_HD float sc_normsq4(sc_f4 a) { return a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w; }
 SC_HD float sc_norm3(sc_f3 a) { return sqrtf(sc_normsq3(a)); }
 
+// sqrtf(x) <= d, deciding without the square root wherever the answer is
+// certain.  sqrtf rounds to nearest and rounding is monotone, so for a
+// normal d > 0: with lo = fl(fl(d*d) * (1 - 2^-20)) <= d^2 (1 - 2^-21),
+// x <= lo gives sqrt(x) < d, hence sqrtf(x) <= d; with
+// hi = fl(fl(d*d) * (1 + 2^-20)) >= d^2 (1 + 2^-21), x > hi gives
+// sqrt(x) > d (1 + 2^-22 - 2^-45), beyond the midpoint d (1 + 2^-24) between
+// d and the next float, hence sqrtf(x) > d.  Only x in (lo, hi] (and NaN)
+// takes sqrtf; for d outside [1e-10, 1e10] (or NaN) every x does.
+typedef struct {
+    float d, lo, hi;
+} sc_sqrt_le;
+SC_HD sc_sqrt_le sc_sqrt_le_make(float d) {
+    sc_sqrt_le s;
+    s.d = d;
+    if (d >= 1e-10f && d <= 1e10f) {
+        const float d2 = d * d;
+        s.lo = d2 * (1.0f - 0x1p-20f);
+        s.hi = d2 * (1.0f + 0x1p-20f);
+    } else {
+        s.lo = NAN;  // no comparison with NaN holds: every x takes sqrtf
+        s.hi = NAN;
+    }
+    return s;
+}
+SC_HD bool sc_sqrt_le_test(sc_sqrt_le s, float x) {
+    if (x <= s.lo) return true;
+    if (x > s.hi) return false;
+    return sqrtf(x) <= s.d;
+}
+
 // math.cuh:90-96
 SC_HD sc_f3 sc_safe_cross(sc_f3 a, sc_f3 b) {
     sc_f3 c = cross(a, b);
