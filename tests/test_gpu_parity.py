@@ -117,7 +117,8 @@ def test_deterministic(product):
 
 
 @pytest.mark.parametrize("limit,periodic,tiles",
-                         [("0", 0, "1"), ("2", 0, "1"), ("2", 1, "1"), ("2", 1, "0"), ("3", 0, "0"), ("5", 1, "0")])
+                         [("0", 0, "1"), ("2", 0, "1"), ("2", 1, "1"), ("2", 1, "0"), ("3", 0, "0"), ("5", 1, "0"),
+                          ("9", 1, "0"), ("12", 0, "0")])
 def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic, tiles):
     """Items whose pair list overflows are handled by scanning their
     neighbourhood; with the list capacity capped, both paths run side by side
