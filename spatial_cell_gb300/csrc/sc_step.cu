@@ -645,7 +645,9 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
     // 1. the terms of its bond matches (list order, then bond-slot order)
     const uint32_t *__restrict__ myMatch = A.match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
     const int nm = min(A.matchN[i] & SC_MATCH_COUNT, SC_MAX_ACTIVE_INTERACTIONS);
-    BondTerm T[SC_MAX_ACTIVE_INTERACTIONS];
+    // the first term stays in registers (most bonded items have one); the
+    // rest go to a per-thread array
+    BondTerm T0, T[SC_MAX_ACTIVE_INTERACTIONS - 1];
     int nt = 0;
     for (int m = 0; m < nm; m++) {
         const uint32_t me = myMatch[m];
@@ -659,6 +661,7 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
         const float trad = t4.w, idist = prad + trad;
         const sc_f4 trot = ld4(A.rotIn, j), tav = ld4(A.avIn, j);
         const sc_f3 tvel = ld3(A.velIn, j);
+        BondTerm b;
         if (it >= 10) {
             // dynamics.cuh:591-655
             const sc_rule &pii = rule_at(P, it);
@@ -669,7 +672,6 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
             sc_f4 tro_t = o2 ? sc_qmul(prot, sc_qinv(ro)) : sc_qmul(prot, ro);
             sc_f4 rro = sc_qmul(sc_qinv(sc_qmul(pav, prot)), sc_qmul(tav, tro_p));
             sc_f4 orro = sc_qmul(sc_qinv(sc_qmul(tav, trot)), sc_qmul(pav, tro_t));
-            BondTerm &b = T[nt++];
             b.q = sc_qmul(sc_slerp(rro, orro, 0.5f), rro);
             b.t = 0.9f * trad / (prad + trad);
             sc_f3 rrp = o1 ? sc_rotate(-rp, sc_qmul(sc_qinv(ro), sc_qmul(tav, trot))) : sc_rotate(rp, sc_qmul(tav, trot));
@@ -684,7 +686,6 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
             sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), trot), pav);
             sc_f3 nnd = normalize(tpos + tvel - (ppos + pvel));
             bool fwd = myBonds[3 * k + 1] == SC_INTERACTION_GROUP_FORWARD;
-            BondTerm &b = T[nt++];
             b.q = sc_quat_from_to(nextUp, (fwd ? -1.0f : 1.0f) * nnd);
             b.t = 0.9f * trad / (prad + trad);
             sc_f3 relUp = (fwd ? 1.0f : -1.0f) * nextTup;
@@ -704,6 +705,11 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
             b.dv = (pDV - (pDV + tpDV) / 2.0f) * 0.9f * prad / (prad + trad) * 1.0f;
             b.dbg = rrp - ppos;
         }
+        if (nt == 0)
+            T0 = b;
+        else
+            T[nt - 1] = b;
+        nt++;
     }
     // 3. every term in the reference's order
     sc_f4 pdbg = sc_make_f4(0, 0, 0, 0);
@@ -739,7 +745,8 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
                 const int k = (int)(myMatch[mi] >> 29);
                 const int it = myBonds[3 * k];
                 if ((it >= 10 || it == SC_INTERACTION_TYPE_CHAIN) && ut < nt) {
-                    const BondTerm &b = T[ut++];
+                    const BondTerm b = ut == 0 ? T0 : T[ut - 1];
+                    ut++;
                     if (it == SC_INTERACTION_TYPE_CHAIN && !dbgTouched) {
                         pdbg = ld4(A.dbg, i);
                         dbgTouched = true;
