@@ -171,21 +171,27 @@ __device__ __forceinline__ void emit_count_ordered(bool valid, int c, int limit,
     if (ovf && cs > min(K, limit)) ovf[atomicAdd(ovfCount, 1)] = g;
 }
 
-// Bonds of one particle held in registers.
+// Bonds of one particle held in registers, with a one-word filter of the
+// partner ids (bit id mod 32 set for each bond) that rules most candidates
+// out before the slot-by-slot comparison.
 struct BondRegs {
     int n;
+    uint32_t filter;
     int t[SC_MAX_ACTIVE_INTERACTIONS], g[SC_MAX_ACTIVE_INTERACTIONS], p[SC_MAX_ACTIVE_INTERACTIONS];
     __device__ __forceinline__ void load(const int *__restrict__ nb, const int *__restrict__ bonds, int i) {
         n = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+        filter = 0u;
 #pragma unroll
         for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
             const int *b = bonds + (size_t)i * 24 + 3 * k;
             t[k] = k < n ? b[0] : 0;
             g[k] = k < n ? b[1] : 0;
             p[k] = k < n ? b[2] : 0;
+            if (k < n) filter |= 1u << (p[k] & 31);
         }
     }
     __device__ __forceinline__ bool has_partner(int id) const {
+        if (!((filter >> (id & 31)) & 1u)) return false;
         bool r = false;
 #pragma unroll
         for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
@@ -193,6 +199,24 @@ struct BondRegs {
         return r;
     }
 };
+
+// The tests of a candidate inside the interaction cube: returns the entry
+// flags, 0 if the pair contributes nothing.
+__device__ __forceinline__ uint32_t pp_flags_in_cube(sc_f3 delta, float trad, int j, float prad, int phydro,
+                                                     const BondRegs &B, const int4 *__restrict__ info) {
+    int4 tin = info[j];
+    if (!(tin.z & SC_ACTIVE)) return 0;
+    float dist = sc_norm3(delta);
+    float s = prad + trad;
+    int thydro = (int)(int8_t)(tin.w & 0xff);
+    uint32_t f = 0;
+    if ((phydro > 0 || thydro > 0) && sc_within_lipid_range(dist, s) && phydro == SC_POLAR && thydro == SC_POLAR)
+        f |= SC_PP_POLAR;
+    bool partner = B.has_partner(tin.x);
+    if (partner) f |= SC_PP_PARTNER;
+    if (!partner && dist < s) f |= SC_PP_COLLIDE;
+    return f;
+}
 
 // The position-only tests of relax for candidate j of particle i
 // (dynamics.cuh:452-478, 584-589, 775-777): returns the entry flags, 0 if
@@ -206,18 +230,7 @@ __device__ __forceinline__ uint32_t pp_flags(const ScParams &P, const Imager &IM
     float4 t4 = pos[j];
     sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
     if (outside_cube(delta, P.maxInt)) return 0;
-    int4 tin = info[j];
-    if (!(tin.z & SC_ACTIVE)) return 0;
-    float dist = sc_norm3(delta);
-    float s = prad + t4.w;
-    int thydro = (int)(int8_t)(tin.w & 0xff);
-    uint32_t f = 0;
-    if ((phydro > 0 || thydro > 0) && sc_within_lipid_range(dist, s) && phydro == SC_POLAR && thydro == SC_POLAR)
-        f |= SC_PP_POLAR;
-    bool partner = B.has_partner(tin.x);
-    if (partner) f |= SC_PP_PARTNER;
-    if (!partner && dist < s) f |= SC_PP_COLLIDE;
-    return f;
+    return pp_flags_in_cube(delta, t4.w, j, prad, phydro, B, info);
 }
 
 // Particle-particle list, built once after the sort; read by coordinateNoise
@@ -246,21 +259,45 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
         int c = 0, nm = 0;
         uint32_t any = 0;
         uint32_t *__restrict__ myMatch = match + (size_t)i * SC_MAX_ACTIVE_INTERACTIONS;
-        scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
-            uint32_t f = pp_flags(P, IM, i, j, ppos, p4.w, phydro, B, pos, info);
-            if (f) {
-                if (c < min(SC_LIST_PP, P.listLimit)) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
-                c++;
-                any |= f;
-                if (f & SC_PP_PARTNER) {  // the bond slots naming this neighbour, in slot order
-                    const int tid_ = info[j].x;
+        const int K = min(SC_LIST_PP, P.listLimit);
+        auto add = [&](int j, uint32_t f) {
+            if (c < K) list[sc_list_at(SC_LIST_PP, i, c)] = (uint32_t)j | f;
+            c++;
+            any |= f;
+            if (f & SC_PP_PARTNER) {  // the bond slots naming this neighbour, in slot order
+                const int tid_ = info[j].x;
 #pragma unroll
-                    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
-                        if (k < B.n && B.p[k] == tid_ && nm < SC_MAX_ACTIVE_INTERACTIONS)
-                            myMatch[nm++] = (uint32_t)j | ((uint32_t)k << 29);
-                }
+                for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++)
+                    if (k < B.n && B.p[k] == tid_ && nm < SC_MAX_ACTIVE_INTERACTIONS)
+                        myMatch[nm++] = (uint32_t)j | ((uint32_t)k << 29);
             }
+        };
+        // 1. the candidates inside the interaction cube, in visiting order, held in the list's
+        // slots (a cheap loop: most candidates leave at the cube test)
+        int pc = 0;
+        scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
+            if (j == i) return;
+            const float4 t4 = pos[j];
+            if (outside_cube(IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos, P.maxInt)) return;
+            if (pc < K) list[sc_list_at(SC_LIST_PP, i, pc)] = (uint32_t)j;
+            pc++;
         });
+        if (pc <= K) {
+            // 2. their remaining tests in order, the list compacted in place (entry c <= k)
+            for (int k = 0; k < pc; k++) {
+                const int j = (int)list[sc_list_at(SC_LIST_PP, i, k)];
+                const float4 t4 = pos[j];
+                const sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - ppos;
+                const uint32_t f = pp_flags_in_cube(delta, t4.w, j, p4.w, phydro, B, info);
+                if (f) add(j, f);
+            }
+        } else {
+            // more in-cube candidates than the list holds: every test in one scan
+            scan27(P, cellStart, ppos, reach(P, ppos, P.maxInt, SC_BINNED_P), [&](int j) {
+                const uint32_t f = pp_flags(P, IM, i, j, ppos, p4.w, phydro, B, pos, info);
+                if (f) add(j, f);
+            });
+        }
         cnt[i] = c;
         // A test bond rotates the particle itself, which its later terms
         // read: its relaxation takes the in-order scan with the overflowed
