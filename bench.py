@@ -98,10 +98,16 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed region starts once the sampler is producing (nvidia-smi takes a moment to
+            # start); what it saw before the region is dropped
+            t0 = time.perf_counter()
+            while not self.samples and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
+            self.samples.clear()
         except Exception:
             self.proc = None
         return self
