@@ -184,3 +184,32 @@ def test_config_loader_matches_reference(product, tmp_path):
         c2 = abi.make_config()
         assert f["load_config"](str(p).encode(), ctypes.byref(c2), ctypes.byref(ng), ctypes.byref(nb)) == 0
         assert product.grid(c1) == (ng.value, nb.value), (size, cell)
+
+
+@pytest.mark.parametrize("case", ["no_metabolic", "no_particles", "inactive_gaps", "tiny"])
+def test_edge_states_byte_identical(case):
+    """The port against the reference's own kernels on the states the GPU
+    edge-case tests use: without metabolic items, without particles, with
+    inactive items among active ones (the reference's gaps after removals),
+    and a scene of a few items."""
+    scene = list(scenes.test_scene(14, n=900, nm=1800, box=42.0))
+    p, m = scene[3].copy(), scene[4].copy()
+    if case == "no_metabolic":
+        m = m[:0]
+    elif case == "no_particles":
+        p = p[:0]
+        scene[5] = 0
+    elif case == "inactive_gaps":
+        p["flags"][::7] &= ~abi.PARTICLE_FLAG_ACTIVE
+        m["flags"][::5] &= ~abi.PARTICLE_FLAG_ACTIVE
+    else:
+        p, m = p[:9], m[:17]
+    scene[3], scene[4] = p, m
+    cfg, port, ref = _pair(tuple(scene))
+    port.prepare()
+    ref.prepare()
+    _bytes_equal(port, ref, f"{case}: after prepare")
+    for k in range(2):
+        port.step(1)
+        ref.step(1)
+        _bytes_equal(port, ref, f"{case}: after step {k + 1}")
