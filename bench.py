@@ -235,6 +235,12 @@ def cpu_sample(args, reps=1, warmup=0):
     """Times the CPU oracle on a same-density sub-box of the workload:
     `warmup` untimed steps, then `reps` timed steps."""
     from oracle import engine as oengine
+    # every host thread this process may run on (a launcher's OMP_NUM_THREADS=1 does not apply: rank 0
+    # runs the CPU leg alone)
+    try:
+        oengine.set_threads(len(os.sched_getaffinity(0)))
+    except (AttributeError, OSError):
+        oengine.set_threads(os.cpu_count() or 1)
     frac = args.cpu_fraction
     cfg = scenes.workload_config(args.workload, **sub_box(args.workload, frac))
     n, nm, box = cfg.num_particles, cfg.num_metabolic_particles, cfg.sim_size
