@@ -242,10 +242,10 @@ def cpu_sample(args, reps=1, warmup=0):
     except (AttributeError, OSError):
         oengine.set_threads(os.cpu_count() or 1)
     frac = args.cpu_fraction
-    cfg = scenes.workload_config(args.workload, **sub_box(args.workload, frac))
+    cfg = scenes.measured_config(args.workload, **sub_box(args.workload, frac))
     n, nm, box = cfg.num_particles, cfg.num_metabolic_particles, cfg.sim_size
     rng = np.random.default_rng(cfg.seed)
-    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    types, rules = scenes.baseline_types(), scenes.workload_rules()
     p = scenes.uniform_particles(rng, n, box, types)
     m = scenes.uniform_metabolic(rng, nm, box, types, cfg.num_metabolites)
     e = oengine.OracleEngine("port", cfg, types, rules)
@@ -278,9 +278,8 @@ def batched_sample(args, native, torch):
     best, times = autotune.tune(mid, fork=(0,))
     sims = []
     for cfg, types, rules, p, m in reps:
-        cfg, env = autotune.apply(cfg, best)
-        with autotune._env(**env):
-            s = native.Simulation(cfg, types, rules)
+        cfg = autotune.apply(cfg, best)
+        s = native.Simulation(cfg, types, rules)
         s.load_state(p, m)
         s.prepare()
         s.step(1)  # warm-up: captures the step graphs

@@ -147,12 +147,20 @@ typedef struct sc_rule {
     int32_t transition_to;               /* 28 */
     int32_t polymerize;                  /* 32 */
     uint8_t break_after_transition;      /* 36 */
-    uint8_t _pad2[11];
+    /* extension, in the reference struct's padding (honoured only by sims
+       created with sc_config.rule_probabilities = 1): when use_probability
+       is set, complexify forms a bond under this rule only with the given
+       probability per step, drawn from Philox keyed by (seed, rule id, step,
+       lower id, higher id) so both partners draw the same number
+       (complexification.json key "probability") */
+    uint8_t use_probability;             /* 37 */
+    uint8_t _pad2[10];
     float relative_orientation[4];       /* 48 */
     float orientation_alignment_threshold; /* 64 */
     float relative_position[3];          /* 68 */
     float position_alignment_threshold;  /* 80 */
-    float _pad3[3];
+    float probability;                   /* 84 (extension, see use_probability) */
+    float _pad3[2];
 } sc_rule;
 
 /* config.json (spatial_cell_sim/config.json, config.cuh:15-75) plus
@@ -185,6 +193,31 @@ typedef struct sc_config {
                                  positions to [0, simSize]; 1 reflecting walls (a step
                                  past a wall is mirrored back into the box) */
     uint64_t seed;            /* Philox key of the Brownian noise */
+    /* execution switches of one sim (results do not depend on them; the
+       values of sc_config_defaults are the production settings) */
+    int32_t graphs;           /* 1: each step replayed as a captured CUDA graph; 0: launched
+                                 phase by phase */
+    int32_t class_streams;    /* particle relax work classes: 0 chosen by size (three streams
+                                 when the particles fill the device), 1 on the sim's stream,
+                                 3 on three streams */
+    int32_t tiles;            /* metabolic sweeps: 0 per-item pair lists, 1 shared-memory tiles */
+    int32_t pair_list_limit;  /* -1: pair lists at full capacity; n >= 0: at most n entries per
+                                 list (the items beyond take the neighbourhood-scan paths) */
+    int32_t pool_per_item;    /* -1: the metabolic pair pool starts sized by the list capacity;
+                                 n >= 0: it starts at n entries per metabolic item (it grows to
+                                 its demand at the next synchronisation either way) */
+    /* complexify extension: 0 the reference's per-item scan (every passing
+       rule appends a bond on the scanning item's side); 1 deterministic pair
+       claim: every item offers itself to each neighbour that passes a rule's
+       gates with the 64-bit key (distance bits, item slot) by atomicMin, and
+       two items bond only when each holds the other's key -- at most one new
+       rule bond per item per step, always on both sides */
+    int32_t pair_claim;
+    /* 1: honour the probability extension of the rule records
+       (sc_rule.use_probability / probability); 0: ignore those bytes, which
+       are padding in the reference's own records and may hold anything */
+    int32_t rule_probabilities;
+    int32_t _reserved;
 } sc_config;
 
 /* Counters of a sim (the reference's nActiveParticles, lastActiveParticle,

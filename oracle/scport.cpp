@@ -544,8 +544,19 @@ inline bool group_active(const PP &a, int group) {
     return false;
 }
 
+// The binding draw of a rule with a probability (extension; the reference's
+// rules always pass).
+inline bool bind_draw(const scp_sim &s, const sc_rule &r, int pid, int tid, int step) {
+    return !r.use_probability || sc_bind_uniform(s.cfg.seed, r.id, pid, tid, step) < r.probability;
+}
+
+void complexify_claim(scp_sim &s, int step);
+
 // ---- interactions.cuh:216-346 complexify -------------------------------------
-void complexify(scp_sim &s) {
+// step: the kernel's step argument (-1 in the start-up sequence); it only
+// keys the binding draws of rules with a probability.
+void complexify(scp_sim &s, int step) {
+    if (s.cfg.pair_claim) { complexify_claim(s, step); return; }
     const int n = s.nActive;
     const float lim = s.cfg.max_interaction_distance;
     const std::vector<PP> &cur = s.p;
@@ -576,7 +587,7 @@ void complexify(scp_sim &s) {
                     alignment(p, tp, up, tup, delta, pii, &oa, &rpa);
                     if (oa > pii.orientation_alignment_threshold &&
                         fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold) &&
-                        states_match(p, tp, pii)) {
+                        states_match(p, tp, pii) && bind_draw(s, pii, p.id, tp.id, step)) {
                         p.bonds[p.nb].type = pii.id;
                         p.bonds[p.nb].group = pii.group;
                         p.bonds[p.nb].partner_id = tp.id;
@@ -584,6 +595,81 @@ void complexify(scp_sim &s) {
                     }
                 }
             });
+        }
+        s.pn[i] = p;
+    }
+    clear_tail(s.pn, n);
+    s.p.swap(s.pn);
+}
+
+// Complexify by deterministic pair claim (sc_config.pair_claim, an
+// extension): every item with a free bond slot offers itself to each
+// neighbour that some rule would bond it to, with the key (bits of
+// |delta|^2 << 32 | its slot); every item keeps the lowest key offered to it,
+// and two items bond when each holds the other's key, under the first rule
+// that passes for the pair as seen from the lower slot.  At most one rule
+// bond forms per item per step, on both sides.
+int claim_rule(const scp_sim &s, const PP &a, const PP &b, sc_f3 delta, int step) {
+    if (a.nb >= SC_MAX_ACTIVE_INTERACTIONS) return -1;
+    int cs = 0, ce = 0;
+    if (a.type >= 0 && (size_t)a.type * 2 + 1 < s.pidx.size()) { cs = s.pidx[a.type * 2]; ce = s.pidx[a.type * 2 + 1]; }
+    const sc_f3 up = sc_rotate(sc_up(), a.rot), tup = sc_rotate(sc_up(), b.rot);
+    for (int k = cs; k < ce; k++) {
+        const sc_rule &pii = s.prules[(size_t)k];
+        if (!((a.type == pii.first_partner_type && b.type == pii.second_partner_type) ||
+              (a.type == pii.second_partner_type && b.type == pii.first_partner_type)) ||
+            pii.only_via_transition)
+            continue;
+        if (pii.group >= 0 && (group_active(a, pii.group) || group_active(b, pii.group))) continue;
+        float oa, rpa;
+        alignment(a, b, up, tup, delta, pii, &oa, &rpa);
+        if (oa > pii.orientation_alignment_threshold &&
+            fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold) && states_match(a, b, pii) &&
+            bind_draw(s, pii, a.id, b.id, step))
+            return k;
+    }
+    return -1;
+}
+
+void complexify_claim(scp_sim &s, int step) {
+    const int n = s.nActive;
+    const float lim = s.cfg.max_interaction_distance;
+    const std::vector<PP> &cur = s.p;
+    std::vector<uint64_t> claim((size_t)std::max(n, 1), ~0ull);
+    // offers, gathered per receiving item: the lowest key wins, so the order
+    // in which they are made does not matter
+    for (int i = 0; i < n; i++) {
+        const PP &a = cur[i];
+        if (!(a.flags & kActive) || a.nb >= SC_MAX_ACTIVE_INTERACTIONS) continue;
+        s.scan(s.rangesP, a.pos, [&](int j) {
+            if (j == i) return;
+            const PP &b = cur[j];
+            if (!(b.flags & kActive)) return;
+            sc_f3 delta = s.img(b.pos, a.pos) - a.pos;
+            if (outside_cube(delta, lim)) return;
+            if (claim_rule(s, a, b, delta, step) < 0) return;
+            const uint64_t key = ((uint64_t)sc_f2u(sc_normsq3(delta)) << 32) | (uint32_t)i;
+            if (key < claim[(size_t)j]) claim[(size_t)j] = key;
+        });
+    }
+    SC_OMP_FOR
+    for (int i = 0; i < n; i++) {
+        PP p = cur[i];
+        const uint64_t key = claim[(size_t)i];
+        if ((p.flags & kActive) && key != ~0ull) {
+            const int j = (int)(uint32_t)key;
+            if ((int)(uint32_t)claim[(size_t)j] == i) {
+                const int lo = std::min(i, j), hi = std::max(i, j);
+                const PP &a = cur[lo], &b = cur[hi];
+                const int k = claim_rule(s, a, b, s.img(b.pos, a.pos) - a.pos, step);
+                if (k >= 0 && p.nb < SC_MAX_ACTIVE_INTERACTIONS) {
+                    const sc_rule &pii = s.prules[(size_t)k];
+                    p.bonds[p.nb].type = pii.id;
+                    p.bonds[p.nb].group = pii.group;
+                    p.bonds[p.nb].partner_id = i == lo ? b.id : a.id;
+                    p.nb++;
+                }
+            }
         }
         s.pn[i] = p;
     }
@@ -972,6 +1058,10 @@ scp_sim *scp_create(const sc_config *cfg, const sc_type_info *types, int n_types
         if (id < 0 || seen[(size_t)id]) continue;
         seen[(size_t)id] = 1;
         s->flat[(size_t)id] = rules[i];
+        if (!cfg->rule_probabilities) {  // padding in the reference's records
+            s->flat[(size_t)id].use_probability = 0;
+            s->flat[(size_t)id].probability = 0.0f;
+        }
     }
     // partner index (interactions.cuh:79-145), rules in ascending id per type
     s->pidx.assign(((size_t)maxId + 1) * 2, 0);
@@ -1038,7 +1128,7 @@ int scp_run_phase(scp_sim *s, int phase, int arg) {
             apply_velocities(*s, s->p, s->nActive, 0.45f);
             apply_velocities(*s, s->m, s->nActiveM, 0.45f);
             break;
-        case SC_PHASE_COMPLEXIFY: complexify(*s); break;
+        case SC_PHASE_COMPLEXIFY: complexify(*s, arg == -1 ? -1 : s->step); break;
         case SC_PHASE_TRANSITION: transition(*s); break;
         case SC_PHASE_POLYMERIZE: polymerize(*s); break;
         case SC_PHASE_DIFFUSE: diffuse(*s); break;

@@ -45,13 +45,18 @@ TYPE_INFO_DTYPE = np.dtype({"names": ["radius", "hydrophobic"], "formats": ["<f4
 RULE_DTYPE = np.dtype({
     "names": ["id", "group", "first_partner_type", "first_partner_state", "second_partner_type",
               "second_partner_state", "propagate_state", "set_state", "wait_for_state", "wait_for_alignment",
-              "only_via_transition", "transition_to", "polymerize", "break_after_transition",
+              "only_via_transition", "transition_to", "polymerize", "break_after_transition", "use_probability",
               "relative_orientation", "orientation_alignment_threshold", "relative_position",
-              "position_alignment_threshold"],
-    "formats": ["<i4", "<i4", "<i4", "i1", "<i4", "i1", "u1", "u1", "u1", "u1", "u1", "<i4", "<i4", "u1",
-                ("<f4", 4), "<f4", ("<f4", 3), "<f4"],
-    "offsets": [0, 4, 8, 12, 16, 20, 21, 22, 23, 24, 25, 28, 32, 36, 48, 64, 68, 80],
+              "position_alignment_threshold", "probability"],
+    "formats": ["<i4", "<i4", "<i4", "i1", "<i4", "i1", "u1", "u1", "u1", "u1", "u1", "<i4", "<i4", "u1", "u1",
+                ("<f4", 4), "<f4", ("<f4", 3), "<f4", "<f4"],
+    "offsets": [0, 4, 8, 12, 16, 20, 21, 22, 23, 24, 25, 28, 32, 36, 37, 48, 64, 68, 80, 84],
     "itemsize": 96})
+
+# The fields of the reference's ParticleInteractionInfo (the extension fields
+# sit in its padding, which the reference leaves unset).
+RULE_EXTENSION_FIELDS = ("use_probability", "probability")
+RULE_REFERENCE_FIELDS = [n for n in RULE_DTYPE.names if n not in RULE_EXTENSION_FIELDS]
 
 # sc_scene_group (include/spatialcell.h)
 SCENE_UNIFORM_BOX = 0
@@ -140,6 +145,14 @@ class Config(ctypes.Structure):
         ("periodic", ctypes.c_int32),
         ("walls", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
+        ("graphs", ctypes.c_int32),
+        ("class_streams", ctypes.c_int32),
+        ("tiles", ctypes.c_int32),
+        ("pair_list_limit", ctypes.c_int32),
+        ("pool_per_item", ctypes.c_int32),
+        ("pair_claim", ctypes.c_int32),
+        ("rule_probabilities", ctypes.c_int32),
+        ("_reserved", ctypes.c_int32),
     ]
 
     def as_dict(self):
@@ -169,7 +182,7 @@ class Observables(ctypes.Structure):
     ]
 
 
-assert ctypes.sizeof(Config) == 88
+assert ctypes.sizeof(Config) == 120
 assert ctypes.sizeof(Counters) == 32
 
 # Reference defaults (spatial_cell_sim/config.json) and extension defaults.
@@ -178,7 +191,9 @@ DEFAULT_CONFIG = dict(num_particles=65536, num_metabolic_particles=65536, steps=
                       movement_noise_scale=0.7, rotation_noise_scale=0.05, metabolite_movement_noise_scale=1.5,
                       velocity_decay=0.7, angular_velocity_decay=0.7, noise_coordination_steps=16,
                       relaxation_steps=32, metabolite_diffusion_steps=8, persist_every_nth_frame=1,
-                      report_every_nth_frame=10, num_metabolites=10, periodic=0, walls=0, seed=42)
+                      report_every_nth_frame=10, num_metabolites=10, periodic=0, walls=0, seed=42, graphs=1,
+                      class_streams=0, tiles=0, pair_list_limit=-1, pool_per_item=-1, pair_claim=0,
+                      rule_probabilities=0)
 
 
 def make_config(**kw):
@@ -190,6 +205,17 @@ def make_config(**kw):
     c = Config()
     for k, v in d.items():
         setattr(c, k, v)
+    return c
+
+
+def config_from_bytes(raw):
+    """A Config from its bytes; a shorter record written before the
+    execution-switch fields existed (the first 88 bytes: the config.json keys,
+    num_metabolites, periodic, walls, seed) takes their defaults."""
+    raw = bytes(raw)
+    c = make_config()
+    n = min(len(raw), ctypes.sizeof(Config))
+    ctypes.memmove(ctypes.addressof(c), raw, n)
     return c
 
 

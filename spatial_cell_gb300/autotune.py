@@ -9,29 +9,13 @@ shared-memory tiles.  The tuner times every candidate on a device-generated
 scene of the cell's size and mix and returns the fastest; its choice is then
 used for every replica of that size class.  Results at the chosen settings
 are checked against the oracle like any other configuration (the oracle
-takes the same config).
+takes the same config).  Every choice is a field of the sim's sc_config, so
+tuning touches no process-wide state.
 """
-import contextlib
 import itertools
-import os
 import time
 
 from . import abi, native, scenes
-
-
-@contextlib.contextmanager
-def _env(**kv):
-    old = {k: os.environ.get(k) for k in kv}
-    try:
-        for k, v in kv.items():
-            os.environ[k] = str(v)
-        yield
-    finally:
-        for k, v in old.items():
-            if v is None:
-                os.environ.pop(k, None)
-            else:
-                os.environ[k] = v
 
 
 def candidates(cfg, cells=(6.0, 7.0, 8.0), fork=(0, 1), tiles=(0, 1)):
@@ -51,11 +35,8 @@ def candidates(cfg, cells=(6.0, 7.0, 8.0), fork=(0, 1), tiles=(0, 1)):
 
 def time_candidate(cfg, types, rules, kinds, fractions, seed, steps, cell, fork, tiles):
     """Seconds per step of one candidate on a device-generated scene."""
-    d = cfg.as_dict()
-    d["grid_cell_size"] = cell
-    c = abi.make_config(**d)
-    with _env(SC_FORK=fork, SC_TILES=tiles):
-        sim = native.Simulation(c, types, rules)
+    c = apply(cfg, (cell, fork, tiles))
+    sim = native.Simulation(c, types, rules)
     try:
         sim.generate_uniform(c.num_particles, c.num_metabolic_particles, kinds, fractions, seed)
         sim.prepare()
@@ -85,7 +66,10 @@ def tune(cfg, types=None, rules=None, kinds=(scenes.LIPID, scenes.DUMMY, scenes.
 
 
 def apply(cfg, choice):
-    """cfg with the chosen cell size, and the environment to create its sims in."""
+    """cfg with the chosen (cell size, fork, tiles): fork 1 runs the particle
+    work classes on three streams, 0 on the sim's stream."""
     d = cfg.as_dict()
     d["grid_cell_size"] = choice[0]
-    return abi.make_config(**d), {"SC_FORK": str(choice[1]), "SC_TILES": str(choice[2])}
+    d["class_streams"] = 3 if choice[1] else 1
+    d["tiles"] = int(choice[2])
+    return abi.make_config(**d)

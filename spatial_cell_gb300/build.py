@@ -22,7 +22,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["sc_grid.cu", "sc_step.cu", "sc_sim.cu", "sc_noalloc.cu", "sc_observe.cu"]
 CPP_SOURCES = ["sc_host.cpp"]
-HEADERS = ["scmath.h", "sc_dev.cuh", "sc_launch.h", "sc_json.hpp"]
+HEADERS = ["scmath.h", "sc_dev.cuh", "sc_launch.h", "sc_json.hpp", "sc_tile.cuh", "sc_gen.h"]
 
 
 def _deps():

@@ -118,6 +118,7 @@ struct ScParams {
     int listLimit;            // effective pair-list capacity (<= each list's size; smaller only in tests)
     int periodic;             // periodic box extension (sc_config.periodic)
     int walls;                // walled box: 0 clamp (reference), 1 reflect (sc_config.walls)
+    int pairClaim;            // complexify by deterministic pair claim (sc_config.pair_claim)
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
     int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
     int tileCapM, tileCapP;   // tile capacities (slots) of the metabolic sweeps; 0: tiles off

@@ -103,6 +103,13 @@ extern "C" void sc_config_defaults(sc_config *c) {
     c->report_every_nth_frame = 10;
     c->num_metabolites = SC_AOS_NUM_METABOLITES;
     c->seed = 42;
+    c->graphs = 1;
+    c->class_streams = 0;
+    c->tiles = 0;
+    c->pair_list_limit = -1;
+    c->pool_per_item = -1;
+    c->pair_claim = 0;
+    c->rule_probabilities = 0;
 }
 
 extern "C" int sc_config_load_json(const char *path, sc_config *c) {
@@ -133,6 +140,8 @@ extern "C" int sc_config_load_json(const char *path, sc_config *c) {
     I("numMetabolites", &c->num_metabolites);
     I("periodic", &c->periodic);
     I("walls", &c->walls);
+    I("pairClaim", &c->pair_claim);
+    I("ruleProbabilities", &c->rule_probabilities);
     if (const scjson::Value *m = v.find("seed")) c->seed = (uint64_t)(m->type == scjson::Value::Int ? m->i : (long long)m->as_double());
     return SC_OK;
 }
@@ -202,6 +211,11 @@ extern "C" int sc_rules_load_json(const char *path, sc_rule *out, int32_t capaci
         r.orientation_alignment_threshold = get_float(c, "orientationAlignmentThreshold", 0.8);
         for (int k = 0; k < 3; k++) r.relative_position[k] = as_float(elem(rp, (size_t)k));
         r.position_alignment_threshold = get_float(c, "positionAlignmentThreshold", 0.8);
+        // extension key (not read by the reference): a per-step binding probability
+        if (const scjson::Value *pr = c.find("probability")) {
+            r.use_probability = 1;
+            r.probability = as_float(pr);
+        }
     }
     return SC_OK;
 }

@@ -52,6 +52,7 @@ struct ScBuffers {
     int *ovfPP, *ovfM;            // overflowed items
     int *warpOffM;                // metabolic pair pool: first entry of every warp's region
     int *workP;                   // particle work list (the items complexify scans)
+    unsigned long long *claimP;   // pair-claim keys, one per particle slot (sc_config.pair_claim)
     size_t poolCapM;              // entries (16 bytes) the metabolic pair pool (listM) holds
     int *warpOffLM;               // lipid-metabolic pair pool: the same
     uint8_t *lipidP;              // per sorted particle slot: active lipid (after each particle sort)
@@ -153,7 +154,9 @@ void sc_phase_relax(ScLaunchCtx &c);
 void sc_phase_relax_metab(ScLaunchCtx &c);
 void sc_phase_relax_partners(ScLaunchCtx &c);
 void sc_phase_apply_velocities(ScLaunchCtx &c);
-void sc_phase_complexify(ScLaunchCtx &c);
+// prep: the complexify of the start-up sequence (main.cu:324-336, step
+// argument -1); otherwise the step's own, at the device step counter
+void sc_phase_complexify(ScLaunchCtx &c, bool prep);
 void sc_phase_transition(ScLaunchCtx &c);
 void sc_phase_polymerize(ScLaunchCtx &c);
 void sc_phase_diffuse(ScLaunchCtx &c);

@@ -390,7 +390,7 @@ int run_phase(sc_sim *s, int phase, int arg) {
         case SC_PHASE_RELAX_METAB: sc_phase_relax_metab(c); break;
         case SC_PHASE_RELAX_PARTNERS: sc_phase_relax_partners(c); break;
         case SC_PHASE_APPLY_VELOCITIES: sc_phase_apply_velocities(c); break;
-        case SC_PHASE_COMPLEXIFY: sc_phase_complexify(c); break;
+        case SC_PHASE_COMPLEXIFY: sc_phase_complexify(c, arg == -1); break;
         case SC_PHASE_TRANSITION: sc_phase_transition(c); break;
         case SC_PHASE_POLYMERIZE: sc_phase_polymerize(c); break;
         case SC_PHASE_DIFFUSE: sc_phase_diffuse(c); break;
@@ -546,8 +546,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     cudaGetDevice(&s->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    // SC_GRAPHS=0 launches every step phase by phase instead of as a CUDA graph
-    if (const char *g = getenv("SC_GRAPHS")) s->useGraphs = atoi(g) != 0;
+    s->useGraphs = cfg->graphs != 0;
     device_init(s->device);
     {
         cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
@@ -585,22 +584,22 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.Nm = cfg->num_metabolic_particles;
     // Concurrent work classes pay off for a sim whose particles fill the
     // device; smaller sims keep one stream, so many of them run side by side
-    // without the cross-stream joins (SC_FORK=0/1 overrides).
-    s->forkClasses = (int64_t)P.N >= (int64_t)s->gridCap * SC_THREADS;
-    if (const char *g = getenv("SC_FORK")) s->forkClasses = atoi(g) != 0;
+    // without the cross-stream joins (class_streams 1 / 3 overrides).
+    s->forkClasses = cfg->class_streams == 0 ? (int64_t)P.N >= (int64_t)s->gridCap * SC_THREADS
+                                             : cfg->class_streams > 1;
     P.coordSteps = cfg->noise_coordination_steps;
     P.seed = cfg->seed;
-    // SC_PAIR_LIST_LIMIT caps the pair lists (tests use it to run the
-    // neighbourhood-scan path of every kernel); unset means full capacity.
-    P.listLimit = 1 << 30;
+    // pair_list_limit >= 0 caps the pair lists (tests use it to run the
+    // neighbourhood-scan path of every kernel); -1 means full capacity.
+    P.listLimit = cfg->pair_list_limit >= 0 ? cfg->pair_list_limit : 1 << 30;
     P.periodic = cfg->periodic != 0;
     P.walls = cfg->walls != 0;
+    P.pairClaim = cfg->pair_claim != 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
     if (cfg->periodic) P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
-    if (const char *lim = getenv("SC_PAIR_LIST_LIMIT")) P.listLimit = std::max(0, atoi(lim));
     // Tile capacities of the metabolic sweeps from the mean occupancy of the
     // cells a tile spans, with room for fluctuations.  The tiled sweep is
-    // selected with SC_TILES=1 (the per-item list sweep is faster at present);
+    // selected with tiles = 1 (the per-item list sweep is faster at present);
     // it is off when the tile would not fit in shared memory.
     {
         const double cells = std::pow((double)std::max(P.nUsed, 1), 3.0);
@@ -611,8 +610,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         };
         P.tileCapM = cap((double)P.Nm);
         P.tileCapP = cap((double)P.N);
-        const char *tilesEnv = getenv("SC_TILES");
-        if (!(tilesEnv && atoi(tilesEnv) == 1) || P.tileCapM + P.tileCapP > 65535 ||
+        if (cfg->tiles != 1 || P.tileCapM + P.tileCapP > 65535 ||
             sc_tile_bytes(P.tileCapM, P.tileCapP, 32) > 200 * 1024)
             P.tileCapM = P.tileCapP = 0;
     }
@@ -633,6 +631,10 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         if (id < 0 || seen[(size_t)id]) continue;
         seen[(size_t)id] = 1;
         flat[(size_t)id] = rules[i];
+        if (!cfg->rule_probabilities) {  // padding in the reference's records
+            flat[(size_t)id].use_probability = 0;
+            flat[(size_t)id].probability = 0.0f;
+        }
     }
     std::map<int, std::vector<int>> byType;
     for (int id = 0; id <= maxId; id++) {
@@ -706,6 +708,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_DBUF, (int)Nm))) ||
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
         (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)) || (rc = dalloc(s, &B.workP, N)) ||
+        (rc = dalloc(s, &B.claimP, P.pairClaim ? N : 1)) ||
         (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)) || (rc = dalloc(s, &B.warpOffLM, (size_t)N / 32 + 1)) ||
         (rc = dalloc(s, &B.lipidP, N)))
         return bail(rc);
@@ -717,9 +720,9 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     }
     B.invalidateLists();
     B.poolCapM = std::min<size_t>(sc_list_words(SC_LIST_M, (int)Nm) / 4, (size_t)INT_MAX - 1024);
-    // SC_POOL_M_PER_ITEM=n starts the metabolic pair pool at n entries per item
-    if (const char *pp = getenv("SC_POOL_M_PER_ITEM"))
-        B.poolCapM = std::min(B.poolCapM, (size_t)std::max(0, atoi(pp)) * (size_t)std::max<int64_t>(Nm, 1));
+    // pool_per_item = n >= 0 starts the metabolic pair pool at n entries per item
+    if (cfg->pool_per_item >= 0)
+        B.poolCapM = std::min(B.poolCapM, (size_t)cfg->pool_per_item * (size_t)std::max<int64_t>(Nm, 1));
     B.polyCap = 4096;
     P.lipidP = B.lipidP;
     cudaMemsetAsync(B.ctr, 0, sizeof(ScCounters), s->st);

@@ -1644,10 +1644,18 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify_select(ScParams P, co
     if (open) work[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
+// The binding draw of a rule with a probability (an extension; the
+// reference's rules carry none and always pass).
+__device__ __forceinline__ bool bind_draw(const ScParams &P, const sc_rule &r, int pid, int tid, int step) {
+    return !r.use_probability || sc_bind_uniform(P.seed, r.id, pid, tid, step) < r.probability;
+}
+
 __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
     const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
-    const int *__restrict__ state, const int *__restrict__ nbIn, int *__restrict__ nbOut, int *bonds) {
+    const int *__restrict__ state, const int *__restrict__ nbIn, int *__restrict__ nbOut, int *bonds,
+    const int *__restrict__ stepPtr, int prep) {
+  const int step = prep ? -1 : *stepPtr;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
     const int i = work[t];
     int4 in = info[i];
@@ -1687,7 +1695,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
             alignment(ord, prot, trot, up, tup, delta, pii, &oa, &rpa);
             if (oa > pii.orientation_alignment_threshold &&
                 fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold) &&
-                states_match(ord, pstate, state[j], pii)) {
+                states_match(ord, pstate, state[j], pii) && bind_draw(P, pii, pid, tin.x, step)) {
                 pb[3 * pnb] = pii.id;
                 pb[3 * pnb + 1] = pii.group;
                 pb[3 * pnb + 2] = tin.x;
@@ -1696,6 +1704,128 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
         }
     });
     (void)nb0;
+    nbOut[i] = pnb;
+  }
+}
+
+// ---- complexify by deterministic pair claim (sc_config.pair_claim) ----------
+// The reference's scan appends a bond on the scanning item's side only, so
+// two items can both bond a third that keeps just one of them (the TODO at
+// interactions.cuh:297).  Here a step forms rule bonds in two kernels:
+//   offer: every open item i that has a free bond slot visits its
+//          neighbours as complexify does and, for each neighbour j that some
+//          rule would bond it to, lowers claim[j] to the 64-bit key
+//          (bits of |delta|^2, i) with atomicMin;
+//   bind:  i and j bond when claim[i] names j and claim[j] names i.  Both
+//          sides take the first rule that passes for the pair as seen from
+//          the lower slot, so the two records always agree.
+// At most one rule bond forms per item per step.  Keys and slots are fixed by
+// the sort, so the result does not depend on thread scheduling.
+struct ClaimItem {
+    sc_f3 pos, up;
+    sc_f4 rot;
+    int id, type, state, nb, cs, ce;
+    const int *b;
+};
+__device__ __forceinline__ ClaimItem claim_item(const ScParams &P, const float4 *__restrict__ pos,
+                                                const float4 *__restrict__ rot, const int4 *__restrict__ info,
+                                                const int *__restrict__ state, const int *__restrict__ nbIn,
+                                                const int *bonds, int i) {
+    ClaimItem a;
+    const float4 p4 = pos[i];
+    a.pos = sc_make_f3(p4.x, p4.y, p4.z);
+    a.rot = ld4(rot, i);
+    a.up = sc_rotate(sc_up(), a.rot);
+    const int4 in = info[i];
+    a.id = in.x;
+    a.type = in.y;
+    a.state = state[i];
+    a.nb = nbIn[i];
+    a.b = bonds + (size_t)i * 24;
+    a.cs = a.ce = 0;
+    if (in.y >= 0 && 2 * in.y + 1 < P.nPidx) {
+        a.cs = P.pidx[2 * in.y];
+        a.ce = P.pidx[2 * in.y + 1];
+    }
+    return a;
+}
+// The partner-mapped index of the first rule of a's type that would bond a
+// to b (delta = b's position seen from a, minus a's), or -1.
+__device__ __forceinline__ int claim_rule(const ScParams &P, const ClaimItem &a, const ClaimItem &b, sc_f3 delta,
+                                          int step) {
+    if (a.nb >= SC_MAX_ACTIVE_INTERACTIONS) return -1;
+    const bool ord = p_order(a.type, a.id, b.type, b.id);
+    for (int k = a.cs; k < a.ce; k++) {
+        const sc_rule &pii = P.prules[k];
+        if (!((a.type == pii.first_partner_type && b.type == pii.second_partner_type) ||
+              (a.type == pii.second_partner_type && b.type == pii.first_partner_type)) ||
+            pii.only_via_transition)
+            continue;
+        if (pii.group >= 0 && (group_active_in(a.b, a.nb, pii.group) || group_active_in(b.b, b.nb, pii.group)))
+            continue;
+        float oa, rpa;
+        alignment(ord, a.rot, b.rot, a.up, b.up, delta, pii, &oa, &rpa);
+        if (oa > pii.orientation_alignment_threshold &&
+            fabs((double)rpa - 1.0) < (1.0 - (double)pii.position_alignment_threshold) &&
+            states_match(ord, a.state, b.state, pii) && bind_draw(P, pii, a.id, b.id, step))
+            return k;
+    }
+    return -1;
+}
+__device__ __forceinline__ unsigned long long claim_key(sc_f3 delta, int i) {
+    return ((unsigned long long)sc_f2u(sc_normsq3(delta)) << 32) | (unsigned)i;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_claim_offer(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
+    const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
+    const int *__restrict__ state, const int *__restrict__ nbIn, const int *__restrict__ bonds,
+    const int *__restrict__ stepPtr, int prep, unsigned long long *claim) {
+  const int step = prep ? -1 : *stepPtr;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
+    const int i = work[t];
+    const ClaimItem a = claim_item(P, pos, rot, info, state, nbIn, bonds, i);
+    if (a.nb >= SC_MAX_ACTIVE_INTERACTIONS) continue;
+    const Imager IM(P, a.pos, SC_BINNED_P);
+    const float lim = P.maxInt;
+    scan27(P, cellStart, a.pos, reach(P, a.pos, lim, SC_BINNED_P), [&](int j) {
+        if (j == i) return;
+        const float4 t4 = pos[j];
+        const sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - a.pos;
+        if (outside_cube(delta, lim)) return;
+        if (!(info[j].z & SC_ACTIVE)) return;
+        const ClaimItem b = claim_item(P, pos, rot, info, state, nbIn, bonds, j);
+        if (claim_rule(P, a, b, delta, step) >= 0) atomicMin(&claim[j], claim_key(delta, i));
+    });
+  }
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_claim_bind(
+    ScParams P, const int *__restrict__ work, const int *__restrict__ workCount, const float4 *__restrict__ pos,
+    const float4 *__restrict__ rot, const int4 *__restrict__ info, const int *__restrict__ state,
+    const int *__restrict__ nbIn, int *__restrict__ nbOut, int *bonds, const int *__restrict__ stepPtr, int prep,
+    const unsigned long long *__restrict__ claim) {
+  const int step = prep ? -1 : *stepPtr;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
+    const int i = work[t];
+    int pnb = nbIn[i];
+    const unsigned long long key = claim[i];
+    const int j = (int)(unsigned)(key & 0xffffffffull);
+    if (key != ~0ull && (int)(unsigned)(claim[j] & 0xffffffffull) == i) {
+        const int lo = min(i, j), hi = max(i, j);
+        const ClaimItem a = claim_item(P, pos, rot, info, state, nbIn, bonds, lo);
+        const ClaimItem b = claim_item(P, pos, rot, info, state, nbIn, bonds, hi);
+        const Imager IM(P, a.pos, SC_BINNED_P);
+        const int k = claim_rule(P, a, b, IM(b.pos) - a.pos, step);
+        if (k >= 0 && pnb < SC_MAX_ACTIVE_INTERACTIONS) {
+            const sc_rule &pii = P.prules[k];
+            int *pb = bonds + (size_t)i * 24;
+            pb[3 * pnb] = pii.id;
+            pb[3 * pnb + 1] = pii.group;
+            pb[3 * pnb + 2] = i == lo ? b.id : a.id;
+            pnb++;
+        }
+    }
     nbOut[i] = pnb;
   }
 }
@@ -2386,17 +2516,27 @@ void sc_phase_apply_velocities(ScLaunchCtx &c) {
     }
 }
 
-void sc_phase_complexify(ScLaunchCtx &c) {
+void sc_phase_complexify(ScLaunchCtx &c, bool prep) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     PFields F = B.P(), X = B.Pnext();
     cudaMemsetAsync(&B.ctr->workCount, 0, sizeof(int), c.st);
     k_complexify_select<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, &B.ctr->nActive, F.info, F.nb, X.nb, F.bonds,
                                                                   B.workP, &B.ctr->workCount);
-    k_complexify<<<std::min(nblocks(c.P.N), c.gridCap), SC_THREADS, 0, c.st>>>(
-        c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot, F.info, F.state, F.nb, X.nb, F.bonds);
+    const int blocks = std::min(nblocks(c.P.N), c.gridCap);
+    if (!c.P.pairClaim) {
+        k_complexify<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
+                                                      F.info, F.state, F.nb, X.nb, F.bonds, &B.ctr->step, prep);
+        (*c.launches) += 2;
+    } else {
+        cudaMemsetAsync(B.claimP, 0xff, (size_t)c.P.N * sizeof(unsigned long long), c.st);
+        k_claim_offer<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
+                                                       F.info, F.state, F.nb, F.bonds, &B.ctr->step, prep, B.claimP);
+        k_claim_bind<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.workP, &B.ctr->workCount, F.pos, F.rot, F.info, F.state,
+                                                      F.nb, X.nb, F.bonds, &B.ctr->step, prep, B.claimP);
+        (*c.launches) += 3;
+    }
     B.cp[FP_NB] ^= 1;
-    (*c.launches) += 2;
 }
 
 void sc_phase_transition(ScLaunchCtx &c) {

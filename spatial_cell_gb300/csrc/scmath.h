@@ -331,10 +331,21 @@ SC_HD sc_u4 sc_draw_block(uint64_t seed, uint32_t stream, uint32_t id, uint32_t 
 }
 
 // The d-th uniform of (id, step): word d&3 of block d>>2.
+// The binding draw of a rule with a probability (complexify extension): one
+// uniform per (rule, step, unordered pair of ids), the same from either side.
+// Its stream word carries the top bit and the rule id, so it shares no
+// counter with the Brownian draws (streams 0..3).
+SC_HD float sc_bind_uniform(uint64_t seed, int rule_id, int id_a, int id_b, int step);
+
 SC_HD float sc_uniform(uint64_t seed, uint32_t stream, uint32_t id, uint32_t step, uint32_t d) {
     sc_u4 b = sc_draw_block(seed, stream, id, step, d >> 2);
     uint32_t w = (d & 3u) == 0 ? b.x : (d & 3u) == 1 ? b.y : (d & 3u) == 2 ? b.z : b.w;
     return sc_u01(w);
+}
+
+SC_HD float sc_bind_uniform(uint64_t seed, int rule_id, int id_a, int id_b, int step) {
+    const uint32_t lo = (uint32_t)(id_a < id_b ? id_a : id_b), hi = (uint32_t)(id_a < id_b ? id_b : id_a);
+    return sc_uniform(seed, 0x80000000u | ((uint32_t)rule_id & 0x7fffffffu), lo, (uint32_t)step, hi);
 }
 
 #define SC_2PI_F 6.2831854820251465f

@@ -73,10 +73,16 @@ def rule(rid, first, second, group=None, first_state=-1, second_state=-1, set_st
     return r
 
 
-def baseline_rules():
+def baseline_rules(probability=None):
     """A + B bind when their centres pass the interaction cube (alignment gates
-    left open): one rule, group = id so each particle holds one such bond."""
-    return rule(1001, TYPE_A, TYPE_B, rel_pos=(0.0, 5.0, 0.0), ori_thr=-2.0, pos_thr=-100.0)
+    left open): one rule, group = id so each particle holds one such bond.
+    With a probability the rule binds with it per step (an extension; the
+    sim must be created with rule_probabilities = 1)."""
+    r = rule(1001, TYPE_A, TYPE_B, rel_pos=(0.0, 5.0, 0.0), ori_thr=-2.0, pos_thr=-100.0)
+    if probability is not None:
+        r["use_probability"] = 1
+        r["probability"] = probability
+    return r
 
 
 def uniform_particles(rng, n, box, types, fractions=((LIPID, 0.4), (DUMMY, 0.4), (TYPE_A, 0.1), (TYPE_B, 0.1))):
@@ -118,6 +124,24 @@ WORKLOADS = {
 }
 
 
+# The A + B binding probability per step of the measured workloads, and the
+# extension switches they run with: complexify by deterministic pair claim,
+# rule probabilities honoured.  (workload_config alone keeps the reference's
+# complexify, for comparisons with the reference's own kernels.)
+WORKLOAD_BIND_PROBABILITY = 0.1
+WORKLOAD_EXTENSIONS = dict(pair_claim=1, rule_probabilities=1)
+
+
+def workload_rules():
+    """The measured workloads' rule table: A + B bind with probability 0.1 per step."""
+    return baseline_rules(probability=WORKLOAD_BIND_PROBABILITY)
+
+
+def measured_config(name, **overrides):
+    """workload_config with the measured workloads' extension switches."""
+    return workload_config(name, **{**WORKLOAD_EXTENSIONS, **overrides})
+
+
 def workload_config(name, **overrides):
     w = WORKLOADS[name]
     kw = dict(num_particles=w["n"], num_metabolic_particles=w["nm"], sim_size=w["box"], grid_cell_size=6.0,
@@ -134,14 +158,14 @@ def batch_replicas(count, seed=3, n_lo=2048, n_hi=262144):
     (lipid, dummy, A, B) ~ Dirichlet(2, 2, 1, 1).  Returns a list of
     (config, types, rules, particles, metabolic) for seeds seed*1000 + r."""
     rng = np.random.default_rng(seed)
-    types, rules = baseline_types(), baseline_rules()
+    types, rules = baseline_types(), workload_rules()
     out = []
     for r in range(count):
         n = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
         nm = 2 * n
         box = float(200.0 * (n / 65536.0) ** (1.0 / 3.0))
         mix = rng.dirichlet([2.0, 2.0, 1.0, 1.0])
-        cfg = workload_config("plain_small", num_particles=n, num_metabolic_particles=nm, sim_size=box,
+        cfg = measured_config("plain_small", num_particles=n, num_metabolic_particles=nm, sim_size=box,
                               seed=seed * 1000 + r)
         rr = np.random.default_rng(seed * 1000 + r)
         p = uniform_particles(rr, n, box, types, fractions=tuple(zip((LIPID, DUMMY, TYPE_A, TYPE_B), mix)))
@@ -193,11 +217,12 @@ def vesicle_workload(scale=1.0):
 
 
 def build_workload(name, **overrides):
-    """Config, tables and initial state of a measured workload."""
-    cfg = workload_config(name, **overrides)
+    """Config, tables and initial state of a measured workload (the A + B rule
+    at probability 0.1 per step, complexify by pair claim, periodic box)."""
+    cfg = measured_config(name, **overrides)
     rng = np.random.default_rng(cfg.seed)
     types = baseline_types()
-    rules = baseline_rules()
+    rules = workload_rules()
     p = uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
     m = uniform_metabolic(rng, cfg.num_metabolic_particles, cfg.sim_size, types, cfg.num_metabolites)
     return cfg, types, rules, p, m

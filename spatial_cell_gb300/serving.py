@@ -46,12 +46,12 @@ class Request:
     def config(self):
         """The request's cell: the small workload's density and physics."""
         box = float(200.0 * (self.n / 65536.0) ** (1.0 / 3.0))
-        return scenes.workload_config("plain_small", num_particles=self.n, num_metabolic_particles=self.nm,
+        return scenes.measured_config("plain_small", num_particles=self.n, num_metabolic_particles=self.nm,
                                       sim_size=box, seed=self.seed)
 
     def start(self):
         """A simulation of the request, its scene generated on the device."""
-        sim = native.Simulation(self.config(), scenes.baseline_types(), scenes.baseline_rules())
+        sim = native.Simulation(self.config(), scenes.baseline_types(), scenes.workload_rules())
         sim.generate_uniform(self.n, self.nm, (scenes.LIPID, scenes.DUMMY, scenes.TYPE_A, scenes.TYPE_B), self.mix,
                              self.seed)
         sim.prepare()

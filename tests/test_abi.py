@@ -47,6 +47,8 @@ def test_config_defaults_match_reference_config_json(product):
     product.lib().sc_config_defaults(ctypes.byref(c))
     ref = abi.make_config()
     for k, _ in abi.Config._fields_:
+        if k.startswith("_"):
+            continue
         assert getattr(c, k) == getattr(ref, k), k
 
 

@@ -23,8 +23,8 @@ def test_tune_picks_the_fastest_and_breaks_ties_deterministically():
     best, times = autotune.tune(cfg, timer=lambda c, f, t: cost[c] + 0.5 * t)
     assert best == (7.0, 0, 0)
     assert len(times) == 12
-    cfg2, env = autotune.apply(cfg, best)
-    assert cfg2.grid_cell_size == 7.0 and env == {"SC_FORK": "0", "SC_TILES": "0"}
+    cfg2 = autotune.apply(cfg, best)
+    assert cfg2.grid_cell_size == 7.0 and cfg2.class_streams == 1 and cfg2.tiles == 0
     assert cfg2.num_particles == cfg.num_particles and cfg2.seed == cfg.seed
 
 
@@ -45,13 +45,12 @@ def test_tuned_config_runs_and_matches_the_oracle(product):
                                  sim_size=200.0 * (n / 65536.0) ** (1.0 / 3.0), seed=9)
     best, times = autotune.tune(cfg, steps=2, cells=(6.0, 8.0))
     assert best in times and all(t > 0 for t in times.values())
-    cfg2, env = autotune.apply(cfg, best)
+    cfg2 = autotune.apply(cfg, best)
     rng = np.random.default_rng(9)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, n, cfg2.sim_size, types)
     m = scenes.uniform_metabolic(rng, nm, cfg2.sim_size, types, cfg2.num_metabolites)
-    with autotune._env(**env):
-        gpu = product.Simulation(cfg2, types, rules)
+    gpu = product.Simulation(cfg2, types, rules)
     cpu = OracleEngine("port", cfg2, types, rules)
     for e in (gpu, cpu):
         e.load_state(p, m, step=0, next_particle_id=n)

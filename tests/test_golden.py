@@ -17,8 +17,10 @@ NAMES = ["golden_mixed", "golden_workload", "golden_tables"]
 
 
 def _load(name):
-    g = np.load(os.path.join(HERE, name + ".npz"))
-    cfg = abi.Config.from_buffer_copy(g["config"].tobytes())
+    g = dict(np.load(os.path.join(HERE, name + ".npz")))
+    cfg = abi.config_from_bytes(g["config"].tobytes())
+    # rule records are 96 bytes in every layout version; view them in the current one
+    g["rules"] = np.frombuffer(g["rules"].tobytes(), abi.RULE_DTYPE)
     return g, cfg
 
 

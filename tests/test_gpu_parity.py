@@ -78,16 +78,13 @@ def test_whole_steps(product, species, periodic):
     assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
 
 
-@pytest.mark.parametrize("periodic,tiles,fork",
-                         [(1, "1", "0"), (0, "1", "0"), (1, "0", "0"), (0, "0", "0"), (1, "0", "1"), (0, "0", "1")])
-def test_measured_workload_small(product, monkeypatch, periodic, tiles, fork):
+@pytest.mark.parametrize("periodic,tiles,streams", [(1, 1, 1), (0, 1, 1), (1, 0, 1), (0, 0, 1), (1, 0, 3), (0, 0, 3)])
+def test_measured_workload_small(product, periodic, tiles, streams):
     """The measured workload's physics at a reduced size (same density), with
     the metabolic sweeps on shared-memory tiles and on per-item lists, and
     the particle work classes on one stream or forked onto three."""
-    monkeypatch.setenv("SC_TILES", tiles)
-    monkeypatch.setenv("SC_FORK", fork)
     cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
-                                 seed=3, periodic=periodic)
+                                 seed=3, periodic=periodic, tiles=tiles, class_streams=streams)
     rng = np.random.default_rng(3)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
@@ -117,32 +114,32 @@ def test_deterministic(product):
 
 
 @pytest.mark.parametrize("limit,periodic,tiles",
-                         [("0", 0, "1"), ("2", 0, "1"), ("2", 1, "1"), ("2", 1, "0"), ("3", 0, "0"), ("5", 1, "0"),
-                          ("9", 1, "0"), ("12", 0, "0")])
-def test_pair_list_overflow_paths(product, monkeypatch, limit, periodic, tiles):
+                         [(0, 0, 1), (2, 0, 1), (2, 1, 1), (2, 1, 0), (3, 0, 0), (5, 1, 0), (9, 1, 0), (12, 0, 0)])
+def test_pair_list_overflow_paths(product, limit, periodic, tiles):
     """Items whose pair list overflows are handled by scanning their
     neighbourhood; with the list capacity capped, both paths run side by side
     and must still match the oracle bit for bit."""
-    monkeypatch.setenv("SC_PAIR_LIST_LIMIT", limit)
-    monkeypatch.setenv("SC_TILES", tiles)
-    cfg, gpu, cpu = _engines(product, scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic))
+    scene = scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic)
+    scene[0].pair_list_limit = limit
+    scene[0].tiles = tiles
+    cfg, gpu, cpu = _engines(product, scene)
     for e in (gpu, cpu):
         e.prepare()
         e.step(2)
     _same(cfg, gpu, cpu, f"2 steps with pair lists capped at {limit}")
 
 
-@pytest.mark.parametrize("fork", ["0", "1"])
-def test_step_graphs_equal_direct_launches(product, monkeypatch, fork):
+@pytest.mark.parametrize("streams", [1, 3])
+def test_step_graphs_equal_direct_launches(product, streams):
     """Steps replayed from captured CUDA graphs give the bytes of steps
     launched phase by phase (several steps: both buffer parities replayed),
     with the particle work classes on one stream or forked onto three."""
-    monkeypatch.setenv("SC_FORK", fork)
     scene = scenes.test_scene(12, n=900, nm=1800, box=42.0, periodic=1)
     out = []
-    for graphs in ("1", "0"):
-        monkeypatch.setenv("SC_GRAPHS", graphs)
+    for graphs in (1, 0):
         cfg, types, rules, p, m, nid = scene
+        cfg.class_streams = streams
+        cfg.graphs = graphs
         s = product.Simulation(cfg, types, rules)
         s.load_state(p, m, next_particle_id=nid)
         s.prepare()
@@ -198,12 +195,13 @@ def test_capacity_exactly_full(product):
     _same(cfg, gpu, cpu, "2 steps at full capacity")
 
 
-def test_metabolic_pool_grows_and_results_do_not_change(product, monkeypatch):
+def test_metabolic_pool_grows_and_results_do_not_change(product):
     """A metabolic pair pool too small for the lists: the blocks it has no
     room for scan their neighbourhoods, the pool grows at the next
     synchronisation, and every step matches the oracle bit for bit."""
-    monkeypatch.setenv("SC_POOL_M_PER_ITEM", "2")
-    cfg, gpu, cpu = _engines(product, scenes.test_scene(15, n=900, nm=1800, box=42.0, periodic=1))
+    scene = scenes.test_scene(15, n=900, nm=1800, box=42.0, periodic=1)
+    scene[0].pool_per_item = 2
+    cfg, gpu, cpu = _engines(product, scene)
     for e in (gpu, cpu):
         e.prepare()
         e.step(1)
