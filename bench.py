@@ -387,6 +387,95 @@ def vesicle_sample(args, native, torch):
     return out
 
 
+def same_state_bits(a, b, species):
+    """Whether two exported states hold the same bits in every field that
+    carries state: interaction slots at and beyond n_active_interactions and
+    metabolite species at and beyond the simulated count are left out (the
+    reference keeps stale values there that no kernel reads)."""
+    for x, y in zip(a, b):
+        x, y = x.copy(), y.copy()
+        for arr in (x, y):
+            nb = np.clip(arr["n_active_interactions"], 0, abi.MAX_ACTIVE_INTERACTIONS)
+            arr["interactions"][np.arange(abi.MAX_ACTIVE_INTERACTIONS)[None, :] >= nb[:, None]] = 0
+            if "metabolites" in arr.dtype.names:
+                arr["metabolites"][:, species:] = 0
+        if x.tobytes() != y.tobytes():
+            return False
+    return True
+
+
+def reference_cuda_sample(args, native, torch):
+    """The reference's own CUDA step on this GPU beside this build's step on
+    the same state: oracle/_ref/ref_step.cubin (the reference's kernels,
+    compiled for sm_103a) in main.cu's launch sequence with the CUDA
+    toolkit's CUB sort (oracle/ref_device.cu).  Both run the reference's
+    semantics -- its walled box and its complexify, without the binding
+    probability it has no notion of -- on the workload's sizes and seed.  At
+    this density the reference's walled box turns positions non-finite after
+    a few steps, after which its cell 0 collects every such item; steps are
+    timed only while both states stay finite (checked after every step).
+    Wall clock per step with the device synchronised (the reference
+    synchronises inside its step); the first step of each is reported apart
+    (this build captures its step graph there)."""
+    from oracle import build as obuild
+    from oracle.engine import OracleEngine
+    if not os.path.exists(obuild.ref_cubin_path()):
+        return {"unavailable": "oracle/_ref/ref_step.cubin absent (built where the reference tree is present)"}
+    cfg = scenes.workload_config(args.workload, periodic=0, walls=0, **sub_box(args.workload, args.fraction))
+    rng = np.random.default_rng(cfg.seed)
+    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    p = scenes.uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
+    m = scenes.uniform_metabolic(rng, cfg.num_metabolic_particles, cfg.sim_size, types, cfg.num_metabolites)
+    items = cfg.num_particles + cfg.num_metabolic_particles
+
+    def finite_state(e):
+        ep, em = e.export_state()
+        return bool(np.isfinite(ep["pos"][(ep["flags"] & 1) != 0]).all()
+                    and np.isfinite(em["pos"][(em["flags"] & 1) != 0]).all())
+
+    def run(e, sync, finite, limit):
+        times = []
+        for _ in range(limit):
+            t0 = time.perf_counter()
+            e.step(1)
+            sync()
+            times.append(time.perf_counter() - t0)
+            if not finite():
+                return times, False
+        return times, True
+
+    ref = OracleEngine("ref_device", cfg, types, rules)
+    ref.load_state(p, m)
+    ref.prepare()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        ref_t, ref_ok = run(ref, lambda: None, lambda: ref.nonfinite() == (0, 0), args.ref_steps)
+    ref_state = ref.export_state()
+    guards = ref.guards()
+    ref.close()
+    sim = native.Simulation(cfg, types, rules)
+    sim.load_state(p, m)
+    sim.prepare()
+    ours_t, ours_ok = run(sim, sim.sync, lambda: finite_state(sim), len(ref_t))
+    ours_state = sim.export_state()
+    sim.close()
+    same = (same_state_bits(ours_state, ref_state, cfg.num_metabolites) if len(ours_t) == len(ref_t) else None)
+    steady = slice(1, None) if len(ref_t) > 1 else slice(0, None)
+    ref_ms = 1e3 * statistics.mean(ref_t[steady])
+    ours_ms = 1e3 * statistics.mean(ours_t[steady])
+    return {"kernels": "the reference's spatial_cell_sim/src/*.cuh compiled for sm_103a, launched in main.cu's "
+                       "sequence with cub::DeviceRadixSort::SortPairs of whole structs",
+            "config": {"particles": cfg.num_particles, "metabolic_particles": cfg.num_metabolic_particles,
+                       "box_nm": cfg.sim_size, "box": "walled (clamp), the reference's", "complexify": "reference",
+                       "seed": cfg.seed},
+            "steps_timed": len(ref_t), "state_finite_after": ref_ok,
+            "reference_ms_per_step": ref_ms, "reference_first_step_ms": 1e3 * ref_t[0],
+            "reference_value": items / (ref_ms / 1e3),
+            "ours_ms_per_step": ours_ms, "ours_first_step_ms": 1e3 * ours_t[0], "ours_value": items / (ours_ms / 1e3),
+            "speedup": ref_ms / ours_ms, "unit": UNIT, "same_state_bits": same,
+            "reference_stores_outside_buffers": guards, "clocks": clocks.summary(),
+            "timing": "wall clock per step, device synchronised; mean over steps 2.. when more than one"}
+
+
 def run_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
@@ -515,6 +604,7 @@ def run_ours(args):
     served = (serving_sample(args, batched["value"] if batched else value)
               if args.serve_requests > 0 and world == 1 else None)
     vesicle = vesicle_sample(args, native, torch) if args.vesicle_scale > 0 and world == 1 else None
+    ref_cuda = reference_cuda_sample(args, native, torch) if args.ref_steps > 0 and world == 1 else None
 
     line = None
     if rank == 0:
@@ -550,6 +640,7 @@ def run_ours(args):
             "batched": batched,
             "serving": served,
             "vesicle": vesicle,
+            "reference_cuda": ref_cuda,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -573,6 +664,8 @@ def main():
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
     ap.add_argument("--vesicle-steps", type=int, default=6)
+    ap.add_argument("--ref-steps", type=int, default=4,
+                    help="steps of the reference's CUDA step timed beside this build's (0: skip)")
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
     args = ap.parse_args()

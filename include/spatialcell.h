@@ -360,10 +360,11 @@ int sc_frame_wait(sc_sim *sim, int64_t ticket);
  * Limit: n <= 262144; larger n returns SC_E_INVALID and launches nothing.
  * The static array (about 4.3 MB) stays on every GPU that loads the library
  * until the process exits.  All calls on a GPU share it, so calls whose work
- * overlaps on that GPU race; order them on one stream.  The first call on a
- * device looks up the array's address with that device current, and should
- * come before any stream capture on the device.  Returns once the results
- * are in perm / cell_start; SC_E_DEVICE if the sort reported an error. */
+ * overlaps on that GPU race; order them on one stream.  Every call looks up
+ * the array's address on the current device (no allocation) and waits for
+ * its own results: it returns once they are in perm / cell_start, so it is
+ * synchronous and cannot be made while the stream is being captured.
+ * SC_E_DEVICE if the sort reported an error. */
 int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info, int32_t n, uint32_t *perm,
                          uint32_t *cell_start, void *stream);
 

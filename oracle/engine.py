@@ -1,9 +1,12 @@
-"""ctypes drivers of the CPU oracle libraries (TEST INFRASTRUCTURE ONLY).
+"""ctypes drivers of the oracle libraries (TEST INFRASTRUCTURE ONLY).
 
 ``OracleEngine("port")`` drives oracle/_build/libscport.so (the CPU
 restatement); ``OracleEngine("ref")`` drives oracle/_ref/libscref.so (the
-reference's own kernels compiled for the host).  Both expose the same calls
-as the product's C ABI, so a test can run one scenario through all of them.
+reference's own kernels compiled for the host); ``OracleEngine("ref_device")``
+drives oracle/_build/librefdev.so, the reference's own kernels compiled for
+sm_103a (oracle/_ref/ref_step.cubin) run on the GPU in main.cu's launch
+sequence.  All expose the same calls as the product's C ABI, so a test can
+run one scenario through all of them.
 """
 import ctypes
 
@@ -41,6 +44,10 @@ def load(kind):
         path, prefix = build.build_ref(), "oref_"
         if path is None:
             raise FileNotFoundError("the reference tree is not present; the reference harness cannot be built")
+    elif kind == "ref_device":
+        if build.build_ref_cubin() is None:
+            raise FileNotFoundError("no oracle/_ref/ref_step.cubin: it is built where the reference tree is present")
+        path, prefix = build.build_ref_device(), "refdev_"
     else:
         raise ValueError(kind)
     lib = ctypes.CDLL(path)
@@ -48,8 +55,18 @@ def load(kind):
     for name, (res, args) in _SIGS.items():
         f = getattr(lib, prefix + name)
         f.restype = res
-        f.argtypes = args
+        f.argtypes = args if not (kind == "ref_device" and name == "create") else [ctypes.c_char_p] + args
         fns[name] = f
+    if kind == "ref_device":
+        lib.refdev_last_error.restype = ctypes.c_char_p
+        lib.refdev_last_error.argtypes = [ctypes.c_void_p]
+        lib.refdev_nonfinite.restype = ctypes.c_int
+        lib.refdev_nonfinite.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.refdev_guards.restype = ctypes.c_int
+        lib.refdev_guards.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        fns["last_error"] = lib.refdev_last_error
+        fns["nonfinite"] = lib.refdev_nonfinite
+        fns["guards"] = lib.refdev_guards
     if kind == "port":
         lib.scp_set_threads.argtypes = [ctypes.c_int]
         lib.scp_max_threads.restype = ctypes.c_int
@@ -74,10 +91,13 @@ class OracleEngine:
         self.cfg = cfg
         self.types = np.ascontiguousarray(types, dtype=abi.TYPE_INFO_DTYPE)
         self.rules = np.ascontiguousarray(rules, dtype=abi.RULE_DTYPE)
-        self.h = self.f["create"](ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules),
-                                  len(self.rules))
+        args = (ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules), len(self.rules))
+        if kind == "ref_device":
+            args = (build.ref_cubin_path().encode(),) + args
+        self.h = self.f["create"](*args)
         if not self.h:
-            raise ValueError("oracle rejected the configuration")
+            why = self.f["last_error"](None).decode() if kind == "ref_device" else ""
+            raise ValueError("oracle rejected the configuration " + why)
         self.n_grid, self.bits, self.cells = abi.grid_dims(cfg)
 
     def close(self):
@@ -90,7 +110,26 @@ class OracleEngine:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise RuntimeError(f"{self.kind}: {what} failed ({rc})")
+            why = self.f["last_error"](self.h).decode() if self.kind == "ref_device" else ""
+            raise RuntimeError(f"{self.kind}: {what} failed ({rc}) {why}")
+
+    def nonfinite(self):
+        """Active particles and metabolic items with a non-finite position
+        (ref_device only)."""
+        out = (ctypes.c_int64 * 2)()
+        self._check(self.f["nonfinite"](self.h, out), "nonfinite")
+        return int(out[0]), int(out[1])
+
+    def guards(self, cap=64):
+        """[(buffer, byte offset)] of the non-zero words in the guard bytes
+        around the harness's buffers (ref_device only): stores the reference
+        made outside its buffers."""
+        names = ctypes.create_string_buffer(32 * cap)
+        offs = (ctypes.c_int64 * cap)()
+        n = self.f["guards"](self.h, names, 32, offs, cap)
+        if n < 0:
+            raise RuntimeError("guards failed")
+        return [(names.raw[32 * k:32 * (k + 1)].split(b"\0")[0].decode(), int(offs[k])) for k in range(min(n, cap))]
 
     def load_state(self, particles, metabolic, step=0, next_particle_id=None):
         p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)

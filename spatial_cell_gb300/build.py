@@ -1,11 +1,14 @@
-"""Builds libspatialcell.so in-tree for sm_103a (GB300).
+"""Builds libspatialcell.so and its driver sc_run in-tree for sm_103a (GB300).
 
     python -m spatial_cell_gb300.build [--force]
 
 Each translation unit is compiled in parallel with nvcc
 (``-gencode arch=compute_103a,code=sm_103a``, ``-fmad=false`` so no
 multiply-add is fused and every operation rounds as written), the host C++
-with g++, and the objects are linked into spatial_cell_gb300/_lib/.
+with g++, and the objects are linked into spatial_cell_gb300/_lib/.  The
+top-level CMakeLists.txt builds the same library and driver with the same
+flags; this script calls the compilers directly so it runs where CMake is
+not installed.
 """
 import os
 import subprocess
@@ -18,6 +21,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libspatialcell.so")
+DRIVER = os.path.join(OUT_DIR, "sc_run")
+DRIVER_SRC = os.path.join(HERE, "driver", "sc_run.cpp")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["sc_grid.cu", "sc_step.cu", "sc_sim.cu", "sc_noalloc.cu", "sc_observe.cu"]
@@ -37,10 +43,10 @@ def _run(cmd):
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not (os.path.exists(LIB) and os.path.exists(DRIVER)):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(d) <= t for d in _deps())
+    t = min(os.path.getmtime(LIB), os.path.getmtime(DRIVER))
+    return all(os.path.getmtime(d) <= t for d in _deps() + [DRIVER_SRC])
 
 
 def build(force=False, verbose=False):
@@ -66,6 +72,11 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     _run([NVCC, *ARCH, "-shared", "-o", tmp, *[j[0] for j in jobs]])
     os.replace(tmp, LIB)
+    tmp = DRIVER + ".tmp"
+    _run(["g++", "-std=c++17", "-O2", "-I", INCLUDE, "-I", os.path.join(CUDA_HOME, "include"), DRIVER_SRC, "-o", tmp,
+          "-L", OUT_DIR, "-lspatialcell", "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart",
+          "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")])
+    os.replace(tmp, DRIVER)
     return LIB
 
 

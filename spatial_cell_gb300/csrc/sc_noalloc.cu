@@ -18,13 +18,13 @@
 //     them on one stream, or wait for one to finish before the next starts;
 //   * the counters that must start at zero (histograms, look-back words, tile
 //     counters, error flag) are cleared by each call; the rest is written
-//     before it is read.
-//   * the first call on a device resolves the array's device address (with
-//     that device current) and keeps it for later calls; make that first
-//     call before beginning any stream capture on the device.
+//     before it is read;
+//   * every call looks up the array's device address on the current device
+//     (a symbol lookup, no allocation; an address kept from an earlier call
+//     could be stale after a device reset) and waits for its own results
+//     before returning, so it is synchronous and cannot be made while the
+//     stream is being captured into a CUDA graph.
 #include <string.h>
-
-#include <mutex>
 
 #include "sc_launch.h"
 
@@ -45,9 +45,6 @@ constexpr size_t kBytes = ((kCtrOff + sizeof(ScCounters) + 255) / 256) * 256;
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kBytes];
 
-std::mutex g_mu;
-void *g_scratch_ptr[64];  // device address of g_sort_scratch, per device
-
 }  // namespace
 
 extern "C" int sc_sort_cells_static(const sc_config *cfg, const void *pos, const void *info, int32_t n,
@@ -57,20 +54,10 @@ extern "C" int sc_sort_cells_static(const sc_config *cfg, const void *pos, const
         return SC_E_INVALID;
     int32_t ngrid = 0, bits = 0;
     if (sc_config_grid(cfg, &ngrid, &bits) != SC_OK) return SC_E_INVALID;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SC_E_CUDA;
+    // The array's address on the current device: host code sees only a host
+    // stand-in of g_sort_scratch, which no kernel may be given.
     void *base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            cudaError_t e = cudaGetSymbolAddress(&g_scratch_ptr[dev], g_sort_scratch);
-            if (e != cudaSuccess) {
-                g_scratch_ptr[dev] = nullptr;
-                return SC_E_CUDA;
-            }
-        }
-        base = g_scratch_ptr[dev];
-    }
+    if (cudaGetSymbolAddress(&base, g_sort_scratch) != cudaSuccess || !base) return SC_E_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *b = (unsigned char *)base;
     uint32_t *keys[2] = {(uint32_t *)(b + kKeysOff), (uint32_t *)(b + kKeysOff) + kWords};

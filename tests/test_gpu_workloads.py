@@ -92,8 +92,6 @@ def test_large_workload_one_step(product):
     gpu.step(1)
     cpu.step(1)
     _compare_step(cfg, gpu, cpu, "large workload, step 1")
-    ovf = gpu.list_overflows()
-    assert min(ovf) >= 0
     gpu.close()
     cpu.close()
 
