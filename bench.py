@@ -504,6 +504,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
     cfg, types, rules, p, m = scenes.build_workload(args.workload, seed=replica_seed(args.workload, rank),
+                                                    metabolic_pairs=args.metabolic_pairs,
                                                     **sub_box(args.workload, args.fraction))
     N, Nm, S = cfg.num_particles, cfg.num_metabolic_particles, cfg.num_metabolites
     items = N + Nm
@@ -621,6 +622,9 @@ def run_ours(args):
                        "sub_iterations": [cfg.noise_coordination_steps, cfg.relaxation_steps,
                                           cfg.metabolite_diffusion_steps],
                        "l2": "inputs larger than L2 (state of several GB)",
+                       "complexify": "pair claim, A + B bind at probability %g per step"
+                                     % scenes.WORKLOAD_BIND_PROBABILITY,
+                       "metabolic_pairs": "4-byte entries" if args.metabolic_pairs == 0 else "16-byte entries",
                        "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -664,6 +668,9 @@ def main():
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
     ap.add_argument("--vesicle-steps", type=int, default=6)
+    ap.add_argument("--metabolic-pairs", type=int, default=0, choices=[0, 1],
+                    help="metabolic relaxation pairs: 0 4-byte entries (geometry per sub-iteration), "
+                         "1 16-byte entries with the geometry frozen per step")
     ap.add_argument("--ref-steps", type=int, default=4,
                     help="steps of the reference's CUDA step timed beside this build's (0: skip)")
     ap.add_argument("--fraction", type=float, default=1.0,

@@ -119,6 +119,8 @@ struct ScParams {
     int periodic;             // periodic box extension (sc_config.periodic)
     int walls;                // walled box: 0 clamp (reference), 1 reflect (sc_config.walls)
     int pairClaim;            // complexify by deterministic pair claim (sc_config.pair_claim)
+    int metabLean;            // metabolic pair pool of 4-byte entries, geometry evaluated per sub-iteration
+                              // (sc_config.metabolic_pairs 0); else 16-byte entries with it frozen (1)
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
     int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
     int tileCapM, tileCapP;   // tile capacities (slots) of the metabolic sweeps; 0: tiles off

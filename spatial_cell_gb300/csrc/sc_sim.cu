@@ -595,6 +595,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.periodic = cfg->periodic != 0;
     P.walls = cfg->walls != 0;
     P.pairClaim = cfg->pair_claim != 0;
+    P.metabLean = cfg->metabolic_pairs == 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
     if (cfg->periodic) P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
     // Tile capacities of the metabolic sweeps from the mean occupancy of the
@@ -719,7 +720,8 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
         return bail(rc);
     }
     B.invalidateLists();
-    B.poolCapM = std::min<size_t>(sc_list_words(SC_LIST_M, (int)Nm) / 4, (size_t)INT_MAX - 1024);
+    B.poolEntryWords = P.metabLean ? 1 : 4;
+    B.poolCapM = std::min<size_t>(sc_list_words(SC_LIST_M, (int)Nm) / B.poolEntryWords, (size_t)INT_MAX - 1024);
     // pool_per_item = n >= 0 starts the metabolic pair pool at n entries per item
     if (cfg->pool_per_item >= 0)
         B.poolCapM = std::min(B.poolCapM, (size_t)cfg->pool_per_item * (size_t)std::max<int64_t>(Nm, 1));
@@ -849,7 +851,7 @@ static int grow_pools(sc_sim *s) {
     if (need <= B.poolCapM || B.poolCapM >= most) return SC_OK;
     const size_t cap = std::min<size_t>((size_t)need + (size_t)need / 4 + 1024, most);
     uint32_t *grown = nullptr;
-    int rc = dalloc(s, &grown, cap * 4);
+    int rc = dalloc(s, &grown, cap * B.poolEntryWords);
     if (rc) {  // no room: keep the pool (the overflowing blocks keep scanning)
         cudaGetLastError();
         s->err.clear();

@@ -951,12 +951,13 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
 // how many pairs to write and where its first one goes (entry k at
 // out[32 k]).  With `items`, thread t of the block stands for item
 // items[b0 + t] (a compacted list) and perm holds those items.
+template <class T>
 struct PoolSlot {
     int i, n;
-    uint4 *out;
+    T *out;
 };
-template <int K>
-__device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int c, uint4 *__restrict__ pool,
+template <int K, class T>
+__device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, int c, T *__restrict__ pool,
                                               int poolCap, unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
                                               int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                               int *__restrict__ ovf, int *__restrict__ ovfCount,
@@ -994,7 +995,7 @@ __device__ __forceinline__ PoolSlot pool_take(const ScParams &P, bool valid, int
         if (lane == 0) warpOff[g >> 5] = s_base < 0 ? 0 : off;
     }
     if (ovfl && ovf) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
-    PoolSlot r;
+    PoolSlot<T> r;
     r.i = cs >= 0 && items ? items[b0 + src] : b0 + src;
     r.n = n;
     r.out = pool + (n ? off : 0) + lane;
@@ -1019,7 +1020,7 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int 
                                              uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
                                              int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
                                              int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
-    const PoolSlot S =
+    const PoolSlot<uint4> S =
         pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
     if (S.n == 0) return;
     const int i = S.i;
@@ -1041,12 +1042,30 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int 
     }
 }
 
+// The lean form of the same pool (ScParams.metabLean): 4-byte entries
+// {neighbour | kind} only, in the same count-ordered warp regions; the
+// relaxation re-evaluates the geometry from the neighbour's position each
+// sub-iteration (a 16-byte gather that nearby items share in L1 / L2, and a
+// square root and a division per pair) instead of streaming 12 more bytes
+// per pair from HBM.
+__device__ __forceinline__ void emit_m_pairs_lean(const ScParams &P, bool valid, int c, const uint32_t *scratch,
+                                                  uint32_t *__restrict__ pool, int poolCap,
+                                                  unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                                  int *__restrict__ cnt, int *__restrict__ perm, int cap,
+                                                  int *__restrict__ ovf, int *__restrict__ ovfCount) {
+    const PoolSlot<uint32_t> S =
+        pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+    for (int k = 0; k < S.n; k++) S.out[(size_t)k * 32] = scratch[sc_list_at(SC_LIST_M, S.i, k)];
+}
+
+template <bool LEAN>
 __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
                                                         const uint32_t *__restrict__ cellStartP,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                        uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
+                                                        uint32_t *__restrict__ pool, int poolCap,
+                                                        unsigned long long *__restrict__ poolUsed,
                                                         int *__restrict__ warpOff, uint32_t *scratch,
                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
@@ -1054,7 +1073,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
     const bool valid = i < *nActivePtr;
     int c = 0;
     if (valid && (minfo[i].z & SC_ACTIVE)) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
-    emit_m_pairs(P, valid, c, scratch, mpos, ppos_, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+    if (LEAN)
+        emit_m_pairs_lean(P, valid, c, scratch, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+    else
+        emit_m_pairs(P, valid, c, scratch, mpos, ppos_, reinterpret_cast<uint4 *>(pool), poolCap, poolUsed, warpOff,
+                     cnt, perm, cap, ovf, ovfCount);
 }
 
 
@@ -1136,6 +1159,66 @@ __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, Relax
                 const sc_f3 a = sc_make_f3(__uint_as_float(E[q].y), __uint_as_float(E[q].z), __uint_as_float(E[q].w));
                 w += kw;
                 dV += (a + sc_make_f3(tv[q].x, tv[q].y, tv[q].z) - ppv) * 0.9f * kw;
+            }
+            E[q] = En[q];
+        }
+    }
+    st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+}
+
+// The lean pool's sweep: per pair the neighbour's position and velocity are
+// gathered and the reference's term (metab_pair) evaluated in full, pairs
+// taken SC_METAB_GROUP at a time as in k_relax_metab.  The image test of a
+// periodic box is decided once per item (Imager), the collision distance per
+// neighbour kind (the lipids' and the metabolic items' radii are each one
+// value in practice, CollisionDistCache recomputes it when they are not).
+__global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab_lean(ScParams P, RelaxMArgs A) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
+    if (g >= *A.nActivePtr) return;
+    const int i = A.L.perm[g];
+    if (i < 0) return;
+    const float4 v4 = A.mvelIn[i];
+    const bool act = P.mAllActive ? i < (int)A.cellStartM[P.cells] : (A.minfo[i].z & SC_ACTIVE) != 0;
+    if (!act) {
+        A.mvelOut[i] = v4;
+        return;
+    }
+    const int c = A.L.cnt[g];
+    if (c > min(SC_LIST_M, P.listLimit)) return;
+    const float4 p4 = A.mpos[i];
+    const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
+    const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+    const sc_f3 ppv = pp + pv;
+    sc_f3 dV = sc_zero3();
+    float w = 0.0f;
+    CollisionDistCache cm, cp;
+    const uint32_t *pairs = reinterpret_cast<const uint32_t *>(A.pool) + A.warpOff[g >> 5] + (g & 31);
+    uint32_t E[SC_METAB_GROUP];
+#pragma unroll
+    for (int q = 0; q < SC_METAB_GROUP; q++) E[q] = q < c ? __ldcs(pairs + (size_t)q * 32) : 0u;
+    for (int k0 = 0; k0 < c; k0 += SC_METAB_GROUP) {
+        float4 t4[SC_METAB_GROUP], tv[SC_METAB_GROUP];
+        uint32_t En[SC_METAB_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) {
+            const bool on = k0 + q < c;
+            const bool fromP = (E[q] & SC_M_FROM_P) != 0;
+            const int j = (int)(E[q] & SC_M_INDEX);
+            t4[q] = on ? (fromP ? A.ppos : A.mpos)[j] : make_float4(0, 0, 0, 0);
+            tv[q] = on ? (fromP ? A.pvel : A.mvelIn)[j] : make_float4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) {
+            const int k = k0 + SC_METAB_GROUP + q;
+            En[q] = k < c ? __ldcs(pairs + (size_t)k * 32) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < SC_METAB_GROUP; q++) {
+            if (k0 + q < c) {
+                const bool fromP = (E[q] & SC_M_FROM_P) != 0;
+                const float cd = fromP ? cp.get(p4.w, t4[q].w) : cm.get(p4.w, t4[q].w);
+                metab_pair(IM, pp, ppv, t4[q], tv[q], cd, fromP, dV, w);
             }
             E[q] = En[q];
         }
@@ -1503,7 +1586,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
     const bool valid = t < *lipidCount;
     int c = 0;
     if (valid) build_lm_item(P, cellStartM, lipids[t], ppos_, mpos, minfo, scratch, c);
-    const PoolSlot S = pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr,
+    const PoolSlot<uint4> S = pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr,
                                              nullptr, lipids);
     if (S.n == 0) return;
     const float4 p4 = ppos_[S.i];
@@ -2440,10 +2523,9 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
                 B.cntM, B.ovfM, &B.ctr->ovfM);
         } else {
             cudaMemsetAsync(&B.ctr->poolM, 0, sizeof(B.ctr->poolM), c.st);
-            k_build_m<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
-                c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info,
-                reinterpret_cast<uint4 *>(B.listM), (int)B.poolCapM, &B.ctr->poolM,
-                B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
+            (c.P.metabLean ? k_build_m<true> : k_build_m<false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
+                c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info, B.listM,
+                (int)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
         }
         (*c.launches)++;
         B.validM = true;
@@ -2462,7 +2544,7 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
             B.cellStartM + c.P.cells, &B.ctr->nActiveM, M.vel, X.vel);
         (*c.launches) += 2;
     } else {
-        k_relax_metab<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+        (c.P.metabLean ? k_relax_metab_lean : k_relax_metab)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
         (*c.launches)++;
     }
     k_relax_metab_overflow<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,

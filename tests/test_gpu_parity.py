@@ -78,13 +78,15 @@ def test_whole_steps(product, species, periodic):
     assert rg[1].tobytes() == rc[1].tobytes(), "reduced metabolic frame differs"
 
 
-@pytest.mark.parametrize("periodic,tiles,streams", [(1, 1, 1), (0, 1, 1), (1, 0, 1), (0, 0, 1), (1, 0, 3), (0, 0, 3)])
-def test_measured_workload_small(product, periodic, tiles, streams):
+@pytest.mark.parametrize("periodic,tiles,streams,pairs", [(1, 1, 1, 0), (0, 1, 1, 0), (1, 0, 1, 0), (0, 0, 1, 0),
+                                                           (1, 0, 3, 0), (0, 0, 3, 0), (1, 0, 1, 1), (0, 0, 3, 1)])
+def test_measured_workload_small(product, periodic, tiles, streams, pairs):
     """The measured workload's physics at a reduced size (same density), with
-    the metabolic sweeps on shared-memory tiles and on per-item lists, and
-    the particle work classes on one stream or forked onto three."""
+    the metabolic sweeps on shared-memory tiles and on per-item lists (4-byte
+    entries, or 16-byte entries with the frozen geometry), and the particle
+    work classes on one stream or forked onto three."""
     cfg = scenes.workload_config("plain_small", num_particles=8192, num_metabolic_particles=16384, sim_size=100.0,
-                                 seed=3, periodic=periodic, tiles=tiles, class_streams=streams)
+                                 seed=3, periodic=periodic, tiles=tiles, class_streams=streams, metabolic_pairs=pairs)
     rng = np.random.default_rng(3)
     types, rules = scenes.baseline_types(), scenes.baseline_rules()
     p = scenes.uniform_particles(rng, cfg.num_particles, cfg.sim_size, types)
@@ -113,15 +115,17 @@ def test_deterministic(product):
     assert runs[0][1].tobytes() == runs[1][1].tobytes()
 
 
-@pytest.mark.parametrize("limit,periodic,tiles",
-                         [(0, 0, 1), (2, 0, 1), (2, 1, 1), (2, 1, 0), (3, 0, 0), (5, 1, 0), (9, 1, 0), (12, 0, 0)])
-def test_pair_list_overflow_paths(product, limit, periodic, tiles):
+@pytest.mark.parametrize("limit,periodic,tiles,pairs",
+                         [(0, 0, 1, 0), (2, 0, 1, 0), (2, 1, 1, 0), (2, 1, 0, 0), (3, 0, 0, 0), (5, 1, 0, 0),
+                          (9, 1, 0, 0), (12, 0, 0, 0), (3, 1, 0, 1), (9, 0, 0, 1)])
+def test_pair_list_overflow_paths(product, limit, periodic, tiles, pairs):
     """Items whose pair list overflows are handled by scanning their
     neighbourhood; with the list capacity capped, both paths run side by side
     and must still match the oracle bit for bit."""
     scene = scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic)
     scene[0].pair_list_limit = limit
     scene[0].tiles = tiles
+    scene[0].metabolic_pairs = pairs
     cfg, gpu, cpu = _engines(product, scene)
     for e in (gpu, cpu):
         e.prepare()
@@ -195,12 +199,14 @@ def test_capacity_exactly_full(product):
     _same(cfg, gpu, cpu, "2 steps at full capacity")
 
 
-def test_metabolic_pool_grows_and_results_do_not_change(product):
+@pytest.mark.parametrize("pairs", [0, 1])
+def test_metabolic_pool_grows_and_results_do_not_change(product, pairs):
     """A metabolic pair pool too small for the lists: the blocks it has no
     room for scan their neighbourhoods, the pool grows at the next
     synchronisation, and every step matches the oracle bit for bit."""
     scene = scenes.test_scene(15, n=900, nm=1800, box=42.0, periodic=1)
     scene[0].pool_per_item = 2
+    scene[0].metabolic_pairs = pairs
     cfg, gpu, cpu = _engines(product, scene)
     for e in (gpu, cpu):
         e.prepare()
