@@ -668,7 +668,7 @@ def main():
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
     ap.add_argument("--vesicle-steps", type=int, default=6)
-    ap.add_argument("--metabolic-pairs", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--metabolic-pairs", type=int, default=1, choices=[0, 1],
                     help="metabolic relaxation pairs: 0 4-byte entries (geometry per sub-iteration), "
                          "1 16-byte entries with the geometry frozen per step")
     ap.add_argument("--ref-steps", type=int, default=4,

@@ -217,9 +217,10 @@ typedef struct sc_config {
        (sc_rule.use_probability / probability); 0: ignore those bytes, which
        are padding in the reference's own records and may hold anything */
     int32_t rule_probabilities;
-    /* metabolic relaxation pairs: 0 a 4-byte entry per pair (the neighbour),
-       its geometry evaluated in each sub-iteration; 1 a 16-byte entry with
-       the pair's position-only term evaluated once per step */
+    /* metabolic relaxation pairs: 1 (default) a 16-byte entry per pair with
+       the pair's position-only term evaluated once per step; 0 a 4-byte
+       entry (the neighbour), the term evaluated again in each sub-iteration
+       (a quarter of the pool's memory, about twice the sweep's time) */
     int32_t metabolic_pairs;
 } sc_config;
 

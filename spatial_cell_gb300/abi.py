@@ -193,7 +193,7 @@ DEFAULT_CONFIG = dict(num_particles=65536, num_metabolic_particles=65536, steps=
                       relaxation_steps=32, metabolite_diffusion_steps=8, persist_every_nth_frame=1,
                       report_every_nth_frame=10, num_metabolites=10, periodic=0, walls=0, seed=42, graphs=1,
                       class_streams=0, tiles=0, pair_list_limit=-1, pool_per_item=-1, pair_claim=0,
-                      rule_probabilities=0, metabolic_pairs=0)
+                      rule_probabilities=0, metabolic_pairs=1)
 
 
 def make_config(**kw):

@@ -99,10 +99,23 @@ struct ScCounters {
 #define SC_MATCH_COUNT 0xff
 #define SC_MATCH_INORDER 0x100
 
+// The geometry of one replica of a batched sim (sc_create_batch): its box,
+// its cells, where its cells start in the batch's key space, its noise key.
+struct ScRep {
+    float simSize, cell;
+    int ngrid, bits, nUsed;
+    uint32_t keyBase;
+    uint64_t seed;
+};
+
 struct ScParams {
     float simSize, maxInt, maxDiff, cell;
     int ngrid, bits;
-    uint32_t cells;
+    uint32_t cells;           // cells of the key space (all replicas of a batch)
+    uint32_t keyBase;         // first key of this item's replica (0 outside batches)
+    int keyBits;              // key bits the sort orders (3 * bits + 1 outside batches)
+    int nRep;                 // replicas of a batched sim (1 otherwise)
+    const ScRep *reps;        // their geometry (batched sims)
     float moveNoise, rotNoise, metabNoise, velDecay, angDecay;
     int S, SP;
     int N, Nm;
@@ -120,7 +133,7 @@ struct ScParams {
     int walls;                // walled box: 0 clamp (reference), 1 reflect (sc_config.walls)
     int pairClaim;            // complexify by deterministic pair claim (sc_config.pair_claim)
     int metabLean;            // metabolic pair pool of 4-byte entries, geometry evaluated per sub-iteration
-                              // (sc_config.metabolic_pairs 0); else 16-byte entries with it frozen (1)
+                              // (sc_config.metabolic_pairs 0); else 16-byte entries with it frozen (1, default)
     int nUsed;                // cells per axis the box spans, ceil(simSize / cell)
     int binned;               // SC_BINNED_*: sets whose positions are those their cells were sorted by
     int tileCapM, tileCapP;   // tile capacities (slots) of the metabolic sweeps; 0: tiles off
@@ -208,7 +221,26 @@ __device__ __forceinline__ bool outside_cube(sc_f3 d, float lim) {
 }
 
 __device__ __forceinline__ uint32_t cell_key(const ScParams &P, uint32_t gx, uint32_t gy, uint32_t gz) {
-    return (gx << (2 * P.bits)) | (gy << P.bits) | gz;
+    return P.keyBase + ((gx << (2 * P.bits)) | (gy << P.bits) | gz);
+}
+
+// Batched sims: every item carries its replica in the bits of its info
+// record's w word above the hydrophobicity byte.  A kernel of a batch works
+// on one item at a time with that replica's geometry (its neighbours are in
+// the same replica's cells); outside batches P is used as given.
+__device__ __forceinline__ int item_rep(int infoW) { return (int)((unsigned)infoW >> 8); }
+template <bool BATCH>
+__device__ __forceinline__ void rep_apply(ScParams &P, int infoW) {
+    if (!BATCH) return;
+    const int r = min(item_rep(infoW), P.nRep - 1);
+    const ScRep g = P.reps[r];
+    P.simSize = g.simSize;
+    P.cell = g.cell;
+    P.ngrid = g.ngrid;
+    P.bits = g.bits;
+    P.nUsed = g.nUsed;
+    P.keyBase = g.keyBase;
+    P.seed = g.seed;
 }
 
 // Visits the reference's 27-cell neighbourhood of pos (grid.cuh:13-25 and the
@@ -265,13 +297,13 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
             for (int oy = R.yl; oy <= R.yh; oy++) {
                 uint32_t base = cell_key(P, wrap_cell(cx + ox, n), wrap_cell(cy + oy, n), 0);
                 if (cz + R.zl >= 0 && cz + R.zh <= n - 1) {
-                    for (uint32_t j = cellStart[base | (uint32_t)(cz + R.zl)],
-                                  e = cellStart[(base | (uint32_t)(cz + R.zh)) + 1];
+                    for (uint32_t j = cellStart[base + (uint32_t)(cz + R.zl)],
+                                  e = cellStart[(base + (uint32_t)(cz + R.zh)) + 1];
                          j < e; j++)
                         f((int)j);
                 } else {
                     for (int oz = R.zl; oz <= R.zh; oz++) {
-                        uint32_t key = base | wrap_cell(cz + oz, n);
+                        uint32_t key = base + wrap_cell(cz + oz, n);
                         for (uint32_t j = cellStart[key], e = cellStart[key + 1]; j < e; j++) f((int)j);
                     }
                 }
@@ -285,7 +317,7 @@ __device__ __forceinline__ void scan27(const ScParams &P, const uint32_t *__rest
     for (int gx = x0; gx <= x1; gx++) {
         for (int gy = y0; gy <= y1; gy++) {
             uint32_t base = cell_key(P, (uint32_t)gx, (uint32_t)gy, 0);
-            uint32_t s = cellStart[base | z0], e = cellStart[(base | z1) + 1];
+            uint32_t s = cellStart[base + z0], e = cellStart[(base + z1) + 1];
             for (uint32_t j = s; j < e; j++) f((int)j);
         }
     }

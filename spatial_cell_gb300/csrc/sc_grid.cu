@@ -34,6 +34,9 @@ __device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// In a batched sim the key is the item's replica's key base plus its cell
+// in that replica's grid: replicas sort into consecutive key ranges.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_sort_keys(const float4 *__restrict__ pos, const int4 *__restrict__ info,
                                                           int n, ScParams P, uint32_t inactiveKey, int passes,
                                                           uint32_t *__restrict__ keys, uint32_t *__restrict__ hist) {
@@ -43,7 +46,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_sort_keys(const float4 *__restri
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         uint32_t k = inactiveKey;
-        if (info[i].z & SC_ACTIVE) {
+        const int4 in = info[i];
+        if (in.z & SC_ACTIVE) {
+            rep_apply<BATCH>(P, in.w);
             sc_f3 p = ld3(pos, i);
             int lim = cell_limit(P);
             k = cell_key(P, sc_grid_idx(p.x, P.cell, lim), sc_grid_idx(p.y, P.cell, lim), sc_grid_idx(p.z, P.cell, lim));
@@ -249,6 +254,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_gather_metabolic(const uint32_t 
 // ---- host-side launchers -----------------------------------------------------
 
 int sc_sort_passes(int bits) { return (3 * bits + 1 + 7) / 8; }
+int sc_sort_passes_for(const ScParams &P) { return ((P.keyBits > 0 ? P.keyBits : 3 * P.bits + 1) + 7) / 8; }
 
 size_t sc_sort_lookback_words(int cap) { return (size_t)((cap + SORT_TILE - 1) / SORT_TILE) * 256; }
 
@@ -257,8 +263,8 @@ size_t sc_sort_lookback_words(int cap) { return (size_t)((cap + SORT_TILE - 1) /
 int sc_launch_sort(cudaStream_t st, const float4 *pos, const int4 *info, int n, const ScParams &P,
                    uint32_t *keys[2], uint32_t *vals[2], uint32_t *hist, uint32_t *lookback, ScCounters *ctr,
                    long long *launches) {
-    int passes = sc_sort_passes(P.bits);
-    int keyBits = 3 * P.bits + 1;
+    int passes = sc_sort_passes_for(P);
+    int keyBits = P.keyBits > 0 ? P.keyBits : 3 * P.bits + 1;
     uint32_t inactiveKey = keyBits >= 32 ? 0xffffffffu : ((1u << keyBits) - 1u);
     int tiles = (n + SORT_TILE - 1) / SORT_TILE;
     size_t lbWords = (size_t)tiles * 256;
@@ -267,7 +273,8 @@ int sc_launch_sort(cudaStream_t st, const float4 *pos, const int4 *info, int n, 
     cudaMemsetAsync(ctr->tileCounter, 0, sizeof(ctr->tileCounter), st);
     int blocks = (n + SC_THREADS - 1) / SC_THREADS;
     if (n > 0) {
-        k_sort_keys<<<blocks, SC_THREADS, 0, st>>>(pos, info, n, P, inactiveKey, passes, keys[0], hist);
+        (P.nRep > 1 ? k_sort_keys<true> : k_sort_keys<false>)<<<blocks, SC_THREADS, 0, st>>>(
+            pos, info, n, P, inactiveKey, passes, keys[0], hist);
         (*launches)++;
     }
     int cur = 0;

@@ -110,7 +110,7 @@ extern "C" void sc_config_defaults(sc_config *c) {
     c->pool_per_item = -1;
     c->pair_claim = 0;
     c->rule_probabilities = 0;
-    c->metabolic_pairs = 0;
+    c->metabolic_pairs = 1;
 }
 
 extern "C" int sc_config_load_json(const char *path, sc_config *c) {

@@ -110,6 +110,7 @@ struct ScBuffers {
 
 // sc_grid.cu
 int sc_sort_passes(int bits);
+int sc_sort_passes_for(const ScParams &P);  // passes over P's key bits
 size_t sc_sort_lookback_words(int cap);
 int sc_launch_sort(cudaStream_t st, const float4 *pos, const int4 *info, int n, const ScParams &P, uint32_t *keys[2],
                    uint32_t *vals[2], uint32_t *hist, uint32_t *lookback, ScCounters *ctr, long long *launches);

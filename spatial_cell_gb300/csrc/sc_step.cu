@@ -21,6 +21,7 @@ __device__ __forceinline__ bool p_order(int ta, int ia, int tb, int ib) { return
 
 // ---- dynamics.cuh:19-215: move (its only live effect: debugVector.xyz = 0)
 // fused with brownianMovementAndRotation, in place --------------------------------
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_move_brownian(const int *__restrict__ nActivePtr,
                                                               const int4 *__restrict__ info,
                                                               const float4 *__restrict__ pos, float4 *dbg,
@@ -32,6 +33,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_move_brownian(const int *__restr
     const int step = *stepPtr;
     int4 in = info[i];
     if (!(in.z & SC_ACTIVE)) return;
+    rep_apply<BATCH>(P, in.w);
     float4 d = dbg[i];
     d.x = 0.0f; d.y = 0.0f; d.z = 0.0f;
     dbg[i] = d;
@@ -65,13 +67,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_apply_noise(const int *__restric
 }
 
 // ---- dynamics.cuh:244-282 applyVelocities, in place ---------------------------
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_apply_velocities(const int *__restrict__ nActivePtr,
                                                                  const int4 *__restrict__ info, float4 *pos,
                                                                  float4 *vel, float4 *rot, float4 *angvel,
                                                                  ScParams P, float f) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nActivePtr) return;
-    if (!(info[i].z & SC_ACTIVE)) return;
+    const int4 in = info[i];
+    if (!(in.z & SC_ACTIVE)) return;
+    rep_apply<BATCH>(P, in.w);
     float4 p4 = pos[i];
     sc_f3 p = sc_make_f3(p4.x, p4.y, p4.z);
     sc_f3 v = ld3(vel, i);
@@ -235,6 +240,7 @@ __device__ __forceinline__ uint32_t pp_flags(const ScParams &P, const Imager &IM
 
 // Particle-particle list, built once after the sort; read by coordinateNoise
 // and relax.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint32_t *__restrict__ cellStart,
                                                          const int *__restrict__ nActivePtr,
                                                          const float4 *__restrict__ pos, const int4 *__restrict__ info,
@@ -250,6 +256,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_pp(ScParams P, const uint3
     if (!(in.z & SC_ACTIVE)) {
         cnt[i] = 0;
     } else {
+        rep_apply<BATCH>(P, in.w);
         BondRegs B;
         B.load(nb, bonds, i);
         float4 p4 = pos[i];
@@ -348,8 +355,9 @@ __device__ __forceinline__ void for_pp(const ScParams &P, const uint32_t *__rest
 // bond matches (k_build_pp), in the reference's visiting order; an item
 // whose list overflowed scans its neighbourhood.
 // dynamics.cuh:288-402 for one particle; the new noise goes to pnOut / anOut.
+template <bool BATCH>
 __device__ __forceinline__ void coordinate_noise_item(
-    const ScParams &P, const uint32_t *__restrict__ cellStart, int i, const float4 *__restrict__ pos,
+    const ScParams &P0, const uint32_t *__restrict__ cellStart, int i, const float4 *__restrict__ pos,
     const int4 *__restrict__ info, const int *__restrict__ nb, const int *__restrict__ bonds,
     const PairList<SC_LIST_PP> &L, const uint32_t *__restrict__ match, const int *__restrict__ matchN,
     const float4 *__restrict__ pnIn, const float4 *__restrict__ anIn, float4 *__restrict__ pnOut,
@@ -361,6 +369,8 @@ __device__ __forceinline__ void coordinate_noise_item(
         *anOut = an4;
         return;
     }
+    ScParams P = P0;
+    rep_apply<BATCH>(P, in.w);
     const int nbi = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
     const int *__restrict__ myBonds = bonds + (size_t)i * 24;
     float4 p4 = pos[i];
@@ -410,6 +420,7 @@ __device__ __forceinline__ void coordinate_noise_item(
 // Runs over the bonded work class (items with at least one bond), the new
 // noise of class position t going to pnTmp[t] / anTmp[t]; every other
 // item's noise is unchanged.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ classIdx,
     const int *__restrict__ classCount, const float4 *__restrict__ pos, const int4 *__restrict__ info,
@@ -418,7 +429,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_coordinate_noise(
     const float4 *__restrict__ anIn, float4 *__restrict__ pnTmp, float4 *__restrict__ anTmp, float frac) {
     const int n0 = classCount[0];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n0; t += gridDim.x * blockDim.x)
-        coordinate_noise_item(P, cellStart, classIdx[t], pos, info, nb, bonds, L, match, matchN, pnIn, anIn,
+        coordinate_noise_item<BATCH>(P, cellStart, classIdx[t], pos, info, nb, bonds, L, match, matchN, pnIn, anIn,
                               pnTmp + t, anTmp + t, frac);
 }
 
@@ -821,8 +832,8 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
 
 // One item of a work class (the items whose list overflowed, and bonded
 // items with a test bond, are left to k_relax_overflow).
-template <int MODE>
-__device__ __forceinline__ void relax_class_item(const ScParams &P, const RelaxArgs &A, int i) {
+template <int MODE, bool BATCH>
+__device__ __forceinline__ void relax_class_item(const ScParams &P0, const RelaxArgs &A, int i) {
     int4 in = A.info[i];
     float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
     if (!(in.z & SC_ACTIVE)) {
@@ -831,6 +842,8 @@ __device__ __forceinline__ void relax_class_item(const ScParams &P, const RelaxA
         A.avOut[i] = a4;
         return;
     }
+    ScParams P = P0;
+    rep_apply<BATCH>(P, in.w);
     if (A.L.cnt[i] > min(SC_LIST_PP, P.listLimit)) return;
     if (MODE == 0) {
         if (!(A.matchN[i] & SC_MATCH_INORDER)) relax_bonded_item(P, A, i, in, v4, r4, a4);
@@ -844,7 +857,7 @@ __device__ __forceinline__ void relax_class_item(const ScParams &P, const RelaxA
 // count (chain-bonded apart from rule-bonded) inside the block, so a warp's
 // lanes walk about as many bond terms of the same kind (items with more
 // bonds would otherwise hold back the rest of their warp).
-template <int MODE>
+template <int MODE, bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
     const int n = A.classCount[MODE];
     const int *__restrict__ idx = A.classIdx + (size_t)MODE * A.L.cap;
@@ -862,22 +875,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
                       (A.bonds[(size_t)i * 24] == SC_INTERACTION_TYPE_CHAIN ? SC_MAX_ACTIVE_INTERACTIONS + 1 : 0);
             int src, cs;
             count_rank<2 * SC_MAX_ACTIVE_INTERACTIONS + 1>(i >= 0, key, &src, &cs);
-            if (cs >= 0) relax_class_item<MODE>(P, A, s_item[src]);
+            if (cs >= 0) relax_class_item<MODE, BATCH>(P, A, s_item[src]);
             __syncthreads();  // the ranking's shared arrays are reused by the next round
         }
     } else {
         for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-            relax_class_item<MODE>(P, A, idx[t]);
+            relax_class_item<MODE, BATCH>(P, A, idx[t]);
     }
 }
 
 // Active items whose list overflowed: their neighbourhood is scanned.  A
 // separate kernel keeps the scan code out of k_relax's instruction stream.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_overflow(ScParams P, RelaxArgs A, const int *__restrict__ ovf,
                                                                const int *__restrict__ ovfCount) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
         const int i = ovf[t];
         int4 in = A.info[i];
+        rep_apply<BATCH>(P, in.w);
         if (in.z & SC_ACTIVE) relax_item<true, 0>(P, A, i, in, A.velIn[i], A.rotIn[i], A.avIn[i]);
     }
 }
