@@ -346,6 +346,39 @@ int64_t sc_reduce_frame_async(sc_sim *sim, sc_reduced_particle *particles,
 /* Blocks until frame `ticket` (and every earlier frame) is in host memory. */
 int sc_frame_wait(sc_sim *sim, int64_t ticket);
 
+/* ---- batched replicas (no counterpart in the reference) ----
+ * One sim that steps many independent replica cells together: every phase
+ * is one launch over the items of all replicas, the sort orders one key
+ * space in which each replica's cells follow the previous replica's (the
+ * replica in the key's high part), and each kernel works on an item with
+ * its replica's box, cells and noise key.  A replica evolves exactly as a
+ * sim of its own created with the same config, box, capacities and seed,
+ * bit for bit.  The config gives the shared physics (noise scales, ranges,
+ * cell size, sub-iterations, box kind, extension switches); its capacities
+ * and box are replaced by the replicas'.  Rules that polymerise are not
+ * accepted, and the sim-wide calls that need one box (sc_generate_*,
+ * sc_mark_positions, sc_observe, sc_pair_histogram, sc_checkpoint_*) return
+ * SC_E_INVALID on a batch; sc_step, sc_run_phase, sc_sync, sc_reduce_frame
+ * (records of all replicas in slot order) and sc_export_grid work as for
+ * any sim. */
+typedef struct sc_replica {
+    int32_t num_particles;            /* the replica's particle capacity */
+    int32_t num_metabolic_particles;  /* its metabolic capacity */
+    float sim_size;                   /* its box */
+    int32_t _pad;
+    uint64_t seed;                    /* Philox key of its noise */
+} sc_replica;
+int sc_create_batch(const sc_config *cfg, const sc_replica *replicas, int32_t n_replicas, const sc_type_info *types,
+                    int32_t n_types, const sc_rule *rules, int32_t n_rules, sc_sim **out);
+/* Loads the replicas' states: particles / metabolic hold replica 0's
+ * n[0] / nm[0] records, then replica 1's, and so on (the layout of
+ * sc_load_state per replica). */
+int sc_load_batch(sc_sim *sim, const sc_particle *particles, const int32_t *n, const sc_metabolic_particle *metabolic,
+                  const int32_t *nm, int32_t step);
+/* Replica r's records in slot order into buffers of its capacities (zero
+ * past its records): what sc_export_state gives for a sim of its own. */
+int sc_export_replica(sc_sim *sim, int32_t replica, sc_particle *particles, sc_metabolic_particle *metabolic);
+
 /* ---- allocation-free cell sort (no counterpart in the reference) ----
  * For callers that cannot let a library allocate device memory: a framework
  * that owns the GPU's memory as its own pool, or a loop that cannot absorb

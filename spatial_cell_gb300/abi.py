@@ -159,6 +159,17 @@ class Config(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
 
 
+class Replica(ctypes.Structure):
+    """sc_replica: one replica cell of a batched sim."""
+    _fields_ = [
+        ("num_particles", ctypes.c_int32),
+        ("num_metabolic_particles", ctypes.c_int32),
+        ("sim_size", ctypes.c_float),
+        ("_pad", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
 class Counters(ctypes.Structure):
     _fields_ = [
         ("n_active_particles", ctypes.c_int32),
@@ -184,6 +195,7 @@ class Observables(ctypes.Structure):
 
 assert ctypes.sizeof(Config) == 120
 assert ctypes.sizeof(Counters) == 32
+assert ctypes.sizeof(Replica) == 24
 
 # Reference defaults (spatial_cell_sim/config.json) and extension defaults.
 DEFAULT_CONFIG = dict(num_particles=65536, num_metabolic_particles=65536, steps=401, sim_size=400.0,

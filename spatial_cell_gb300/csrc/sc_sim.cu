@@ -186,6 +186,24 @@ __global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePt
 }
 
 __global__ void k_after_sort(ScCounters *c) { c->lastActive = c->nActive - 1; }
+
+// The replica of every slot of a batch just loaded: the loaded items are the
+// replicas' items one replica after another (offsets: nRep + 1 prefix
+// sums); slots past them get the replica id nRep, which names no replica.
+__global__ void k_set_reps(int4 *__restrict__ info, int cap, const int *__restrict__ offsets, int nRep) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    int lo = 0, hi = nRep;  // the last replica whose offset is <= i
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (offsets[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const int r = i < offsets[nRep] ? lo : nRep;
+    int4 in = info[i];
+    in.w = (in.w & 0xff) | (r << 8);
+    info[i] = in;
+}
 // Per sorted particle slot: 1 for an active lipid (the metabolic kernels'
 // candidate test); slots past the active ones are cleared.
 __global__ void k_mark_lipids(const int *__restrict__ nActivePtr, int cap, const int4 *__restrict__ info,
@@ -233,6 +251,9 @@ struct sc_sim {
     float4 *markP = nullptr, *markM = nullptr;
     int markCapP = 0, markCapM = 0;
     double *obs = nullptr;  // partials table, then 2 result rows
+    // batched sims (sc_create_batch): the replicas and their geometry
+    std::vector<sc_replica> reps;
+    std::vector<ScRep> repGeom;
 };
 
 namespace {
@@ -519,10 +540,51 @@ const char *sc_last_error(const sc_sim *sim) {
     return sc_host_last_error();
 }
 
+static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32_t n_replicas,
+                      const sc_type_info *types, int32_t n_types, const sc_rule *rules, int32_t n_rules, sc_sim **out);
+
 int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, const sc_rule *rules, int32_t n_rules,
               sc_sim **out) {
-    if (!cfg || !out) return set_err(nullptr, SC_E_INVALID, "null argument");
+    return create_sim(cfg, nullptr, 0, types, n_types, rules, n_rules, out);
+}
+
+int sc_create_batch(const sc_config *cfg, const sc_replica *replicas, int32_t n_replicas, const sc_type_info *types,
+                    int32_t n_types, const sc_rule *rules, int32_t n_rules, sc_sim **out) {
+    if (!cfg || !out || !replicas || n_replicas < 1) return set_err(nullptr, SC_E_INVALID, "bad batch arguments");
+    return create_sim(cfg, replicas, n_replicas, types, n_types, rules, n_rules, out);
+}
+
+static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32_t n_replicas,
+                      const sc_type_info *types, int32_t n_types, const sc_rule *rules, int32_t n_rules, sc_sim **out) {
+    if (!cfg_in || !out) return set_err(nullptr, SC_E_INVALID, "null argument");
     *out = nullptr;
+    // A batch: the replicas' capacities add up, the largest box stands for the
+    // sim-wide grid values; each replica's own grid is set up below.
+    sc_config batchCfg = *cfg_in;
+    const sc_config *cfg = cfg_in;
+    if (n_replicas > 0) {
+        int64_t np = 0, nmp = 0;
+        float box = 0.0f;
+        for (int r = 0; r < n_replicas; r++) {
+            const sc_replica &q = replicas[r];
+            if (q.num_particles < 0 || q.num_metabolic_particles < 0 || !(q.sim_size > 0.0f))
+                return set_err(nullptr, SC_E_INVALID, "replica " + std::to_string(r) + ": bad capacity or box");
+            if (cfg_in->periodic && floorf(q.sim_size / cfg_in->grid_cell_size) < 3.0f)
+                return set_err(nullptr, SC_E_INVALID, "replica " + std::to_string(r) + ": a periodic box needs at least 3 grid cells per axis");
+            np += q.num_particles;
+            nmp += q.num_metabolic_particles;
+            box = std::max(box, q.sim_size);
+        }
+        if (np > INT_MAX / 2 || nmp > INT_MAX / 2) return set_err(nullptr, SC_E_INVALID, "batch too large");
+        for (int i = 0; i < n_rules; i++)
+            if (rules && rules[i].polymerize >= 0)
+                return set_err(nullptr, SC_E_INVALID, "batched sims run no polymerising rules");
+        batchCfg.num_particles = (int32_t)np;
+        batchCfg.num_metabolic_particles = (int32_t)nmp;
+        batchCfg.sim_size = box;
+        batchCfg.tiles = 0;
+        cfg = &batchCfg;
+    }
     if (cfg->num_particles < 0 || cfg->num_metabolic_particles < 0)
         return set_err(nullptr, SC_E_INVALID, "negative capacity");
     if (cfg->num_metabolites < 1 || cfg->num_metabolites > SC_AOS_NUM_METABOLITES)
@@ -598,6 +660,43 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.metabLean = cfg->metabolic_pairs == 0;
     P.nUsed = (int)ceilf(cfg->sim_size / cfg->grid_cell_size);
     if (cfg->periodic) P.nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &P.cell);
+    P.nRep = 1;
+    if (n_replicas > 0) {
+        // Each replica's grid as a sim of its own would have it (config.cuh:65-74
+        // cells per axis, or the periodic box's equal cells), its cells at
+        // consecutive keys after the previous replica's; the sort orders the
+        // key bits the whole key space needs.
+        s->reps.assign(replicas, replicas + n_replicas);
+        uint64_t base = 0;
+        for (int r = 0; r < n_replicas; r++) {
+            sc_config rc = *cfg;
+            rc.sim_size = replicas[r].sim_size;
+            int32_t ng = 0, nb = 0;
+            if (sc_config_grid(&rc, &ng, &nb) != SC_OK) {
+                sc_destroy(s);
+                return set_err(nullptr, SC_E_INVALID, sc_host_last_error());
+            }
+            ScRep g;
+            g.simSize = rc.sim_size;
+            g.cell = rc.grid_cell_size;
+            g.ngrid = ng;
+            g.bits = nb;
+            g.nUsed = (int)ceilf(rc.sim_size / rc.grid_cell_size);
+            if (rc.periodic) g.nUsed = sc_periodic_cells(rc.sim_size, rc.grid_cell_size, &g.cell);
+            g.keyBase = (uint32_t)base;
+            g.seed = replicas[r].seed;
+            s->repGeom.push_back(g);
+            base += (uint64_t)ng * ng * ng;
+        }
+        if (base >= (1ull << 31)) {
+            sc_destroy(s);
+            return set_err(nullptr, SC_E_INVALID, "the batch's cells do not fit 31 key bits");
+        }
+        P.cells = (uint32_t)base;
+        P.keyBits = 1;
+        while ((1ull << P.keyBits) - 1 < base) P.keyBits++;
+        P.nRep = n_replicas;
+    }
     // Tile capacities of the metabolic sweeps from the mean occupancy of the
     // cells a tile spans, with room for fluctuations.  The tiled sweep is
     // selected with tiles = 1 (the per-item list sweep is faster at present);
@@ -675,6 +774,12 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
     P.prules = dPrules;
     P.types = dTypes;
     P.nTypes = n_types;
+    if (!s->repGeom.empty()) {
+        ScRep *dReps = nullptr;
+        if ((rc = dalloc(s, &dReps, s->repGeom.size()))) return bail(rc);
+        cudaMemcpyAsync(dReps, s->repGeom.data(), s->repGeom.size() * sizeof(ScRep), cudaMemcpyHostToDevice, s->st);
+        P.reps = dReps;
+    }
 
     ScBuffers &B = s->B;
     memset(&B, 0, sizeof B);
@@ -694,7 +799,7 @@ int sc_create(const sc_config *cfg, const sc_type_info *types, int32_t n_types, 
             (rc = dalloc(s, &B.valsM[b], Nm)))
             return bail(rc);
     }
-    const int passes = sc_sort_passes(bits);
+    const int passes = sc_sort_passes_for(P);
     if ((rc = dalloc(s, &B.mcLscs, Nm)) || (rc = dalloc(s, &B.mcSpoly, Nm)) || (rc = dalloc(s, &B.mcNb, Nm)) ||
         (rc = dalloc(s, &B.mcBonds, Nm * 24)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
@@ -979,6 +1084,96 @@ int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *me
     return check_launch(s);
 }
 
+int sc_load_batch(sc_sim *s, const sc_particle *particles, const int32_t *n, const sc_metabolic_particle *metabolic,
+                  const int32_t *nm, int32_t step) {
+    if (!s || !n || !nm) return set_err(s, SC_E_INVALID, "null argument");
+    if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
+    const int R = (int)s->reps.size();
+    std::vector<int> offP(R + 1, 0), offM(R + 1, 0);
+    for (int r = 0; r < R; r++) {
+        if (n[r] < 0 || nm[r] < 0 || n[r] > s->reps[r].num_particles || nm[r] > s->reps[r].num_metabolic_particles)
+            return set_err(s, SC_E_INVALID, "replica " + std::to_string(r) + ": state larger than its capacity");
+        offP[r + 1] = offP[r] + n[r];
+        offM[r + 1] = offM[r] + nm[r];
+    }
+    int rc = sc_load_state(s, particles, offP[R], metabolic, offM[R], step, 0);
+    if (rc) return rc;
+    int *dOff = nullptr;
+    if ((rc = dalloc(s, &dOff, 2 * ((size_t)R + 1)))) return rc;
+    SC_CK(s, cudaMemcpyAsync(dOff, offP.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    SC_CK(s, cudaMemcpyAsync(dOff + R + 1, offM.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    ScBuffers &B = s->B;
+    if (s->P.N > 0) k_set_reps<<<nb_of(s->P.N), SC_THREADS, 0, s->st>>>(B.p[0].info, s->P.N, dOff, R);
+    if (s->P.Nm > 0) k_set_reps<<<nb_of(s->P.Nm), SC_THREADS, 0, s->st>>>(B.m[0].info, s->P.Nm, dOff + R + 1, R);
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    cudaFreeAsync(dOff, s->st);
+    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)dOff));
+    return check_launch(s);
+}
+
+// The slots of replica r in slot order (from the info records' replica bits).
+static int replica_slots(sc_sim *s, const int4 *info, int cap, int r, std::vector<std::pair<int, int>> &runs) {
+    std::vector<int4> h((size_t)std::max(cap, 1));
+    if (cap > 0) SC_CK(s, cudaMemcpy(h.data(), info, (size_t)cap * sizeof(int4), cudaMemcpyDeviceToHost));
+    runs.clear();
+    for (int i = 0; i < cap; i++) {
+        if ((int)((unsigned)h[(size_t)i].w >> 8) != r) continue;
+        if (!runs.empty() && runs.back().first + runs.back().second == i) runs.back().second++;
+        else runs.push_back({i, 1});
+    }
+    return SC_OK;
+}
+
+int sc_export_replica(sc_sim *s, int32_t r, sc_particle *particles, sc_metabolic_particle *metabolic) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
+    if (r < 0 || r >= (int)s->reps.size()) return set_err(s, SC_E_INVALID, "no such replica");
+    cudaSetDevice(s->device);
+    const int N = s->P.N, Nm = s->P.Nm;
+    int rc = ensure_staging(s, std::max<size_t>(
+                                   std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
+                                   16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    std::vector<std::pair<int, int>> runs;
+    if (particles) {
+        const size_t cap = (size_t)s->reps[(size_t)r].num_particles;
+        memset(particles, 0, cap * sizeof(sc_particle));
+        if (N > 0) {
+            k_pack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActive, N, B.P());
+            SC_CK(s, cudaStreamSynchronize(s->st));
+            if ((rc = replica_slots(s, B.P().info, N, r, runs))) return rc;
+            size_t k = 0;
+            for (auto &run : runs) {
+                const size_t m = std::min((size_t)run.second, cap - std::min(cap, k));
+                if (m) SC_CK(s, cudaMemcpy(particles + k, s->staging + (size_t)run.first * sizeof(sc_particle),
+                                           m * sizeof(sc_particle), cudaMemcpyDeviceToHost));
+                k += m;
+            }
+        }
+    }
+    if (metabolic) {
+        const size_t cap = (size_t)s->reps[(size_t)r].num_metabolic_particles;
+        memset(metabolic, 0, cap * sizeof(sc_metabolic_particle));
+        if (Nm > 0) {
+            k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
+                                                                  B.mcLscs, B.mcSpoly, B.mcNb, B.mcBonds);
+            SC_CK(s, cudaStreamSynchronize(s->st));
+            if ((rc = replica_slots(s, B.M().info, Nm, r, runs))) return rc;
+            size_t k = 0;
+            for (auto &run : runs) {
+                const size_t m = std::min((size_t)run.second, cap - std::min(cap, k));
+                if (m) SC_CK(s, cudaMemcpy(metabolic + k, s->staging + (size_t)run.first * sizeof(sc_metabolic_particle),
+                                           m * sizeof(sc_metabolic_particle), cudaMemcpyDeviceToHost));
+                k += m;
+            }
+        }
+    }
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    release_staging(s);
+    return check_launch(s);
+}
+
 int sc_export_grid(sc_sim *s, int32_t which, uint32_t *ranges, uint32_t *perm) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     cudaSetDevice(s->device);
@@ -1025,6 +1220,7 @@ int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabo
 // buffer on the sim's stream), unpacks them, generates and unpacks nm
 // metabolic particles and sets the counters.
 static int generate_into(sc_sim *s, int n, int nm, uint64_t seed, const std::function<void(float)> &particles) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     const int N = s->P.N, Nm = s->P.Nm;
     if (nm > 0 && (int)s->types.size() <= SC_PARTICLE_TYPE_METABOLIC)
         return set_err(s, SC_E_INVALID, "the type table has no metabolic particle type (1000)");
@@ -1104,6 +1300,7 @@ int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups,
 }
 
 int sc_mark_positions(sc_sim *s) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
     cudaSetDevice(s->device);
@@ -1136,6 +1333,7 @@ int sc_mark_positions(sc_sim *s) {
 }
 
 int sc_observe(sc_sim *s, sc_observables *out) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
     cudaSetDevice(s->device);
@@ -1176,6 +1374,7 @@ int sc_observe(sc_sim *s, sc_observables *out) {
 }
 
 int sc_pair_histogram(sc_sim *s, int32_t type_a, int32_t type_b, float r_max, int32_t n_bins, uint64_t *counts) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s || !counts) return set_err(s, SC_E_INVALID, "null argument");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
     if (n_bins < 1 || n_bins > 4096) return set_err(s, SC_E_INVALID, "n_bins must be in 1..4096");
@@ -1200,6 +1399,7 @@ int sc_pair_histogram(sc_sim *s, int32_t type_a, int32_t type_b, float r_max, in
 }
 
 int sc_checkpoint_write(sc_sim *s, void *file) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s || !file) return set_err(s, SC_E_INVALID, "null argument");
     sc_counters c;
     int rc = sc_get_counters(s, &c);
@@ -1219,6 +1419,7 @@ int sc_checkpoint_write(sc_sim *s, void *file) {
 }
 
 int sc_checkpoint_read(sc_sim *s, void *file) {
+    if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s || !file) return set_err(s, SC_E_INVALID, "null argument");
     FILE *f = (FILE *)file;
     char magic[8];

@@ -1030,15 +1030,19 @@ __device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, 
 // A.x, A.y, A.z}; a region is sized by the warp's longest stored list.  An
 // overflowed item, or every item of a block the pool has no room for, is
 // listed in `ovf` for the scan.
-__device__ __forceinline__ void emit_m_pairs(const ScParams &P, bool valid, int c, const uint32_t *scratch,
+template <bool BATCH>
+__device__ __forceinline__ void emit_m_pairs(const ScParams &P0, bool valid, int c, const uint32_t *scratch,
+                                             const int4 *__restrict__ minfo,
                                              const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
                                              uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
                                              int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
                                              int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const PoolSlot<uint4> S =
-        pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+        pool_take<SC_LIST_M>(P0, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
     if (S.n == 0) return;
     const int i = S.i;
+    ScParams P = P0;
+    rep_apply<BATCH>(P, minfo[i].w);
     const float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
@@ -1073,8 +1077,8 @@ __device__ __forceinline__ void emit_m_pairs_lean(const ScParams &P, bool valid,
     for (int k = 0; k < S.n; k++) S.out[(size_t)k * 32] = scratch[sc_list_at(SC_LIST_M, S.i, k)];
 }
 
-template <bool LEAN>
-__global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32_t *__restrict__ cellStartM,
+template <bool LEAN, bool BATCH>
+__global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P0, const uint32_t *__restrict__ cellStartM,
                                                         const uint32_t *__restrict__ cellStartP,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
@@ -1087,12 +1091,17 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P, const uint32
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
-    if (valid && (minfo[i].z & SC_ACTIVE)) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
+    if (valid) {
+        const int4 mi = minfo[i];
+        ScParams P = P0;
+        rep_apply<BATCH>(P, mi.w);
+        if (mi.z & SC_ACTIVE) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
+    }
     if (LEAN)
-        emit_m_pairs_lean(P, valid, c, scratch, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+        emit_m_pairs_lean(P0, valid, c, scratch, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
     else
-        emit_m_pairs(P, valid, c, scratch, mpos, ppos_, reinterpret_cast<uint4 *>(pool), poolCap, poolUsed, warpOff,
-                     cnt, perm, cap, ovf, ovfCount);
+        emit_m_pairs<BATCH>(P0, valid, c, scratch, minfo, mpos, ppos_, reinterpret_cast<uint4 *>(pool), poolCap,
+                            poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
 }
 
 
@@ -1187,11 +1196,13 @@ __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab(ScParams P, Relax
 // periodic box is decided once per item (Imager), the collision distance per
 // neighbour kind (the lipids' and the metabolic items' radii are each one
 // value in practice, CollisionDistCache recomputes it when they are not).
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab_lean(ScParams P, RelaxMArgs A) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *A.nActivePtr) return;
     const int i = A.L.perm[g];
     if (i < 0) return;
+    if (BATCH) rep_apply<BATCH>(P, A.minfo[i].w);
     const float4 v4 = A.mvelIn[i];
     const bool act = P.mAllActive ? i < (int)A.cellStartM[P.cells] : (A.minfo[i].z & SC_ACTIVE) != 0;
     if (!act) {
@@ -1242,8 +1253,13 @@ __global__ void __launch_bounds__(SC_THREADS, 4) k_relax_metab_lean(ScParams P, 
 }
 
 // An item whose list overflowed: the reference's loops over the 27 cells.
-__device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const RelaxMArgs &A, int i) {
-    if (i < 0 || !(A.minfo[i].z & SC_ACTIVE)) return;
+template <bool BATCH>
+__device__ __forceinline__ void relax_metab_scan_item(const ScParams &P0, const RelaxMArgs &A, int i) {
+    if (i < 0) return;
+    const int4 mi = A.minfo[i];
+    if (!(mi.z & SC_ACTIVE)) return;
+    ScParams P = P0;
+    rep_apply<BATCH>(P, mi.w);
     float4 v4 = A.mvelIn[i];
     float4 p4 = A.mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -1278,11 +1294,12 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P, const R
 }
 
 // The items whose list overflowed (listed by k_build_m), grid-stride.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A,
                                                                      const int *__restrict__ ovf,
                                                                      const int *__restrict__ ovfCount) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x)
-        relax_metab_scan_item(P, A, ovf[t]);
+        relax_metab_scan_item<BATCH>(P, A, ovf[t]);
 }
 
 // ---- the same sweep on column-segment tiles (sc_tile.cuh) ---------------------
@@ -1587,9 +1604,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_lipid_select(const int *__restri
     if (lip) work[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint32_t *__restrict__ cellStartM,
+template <bool BATCH>
+__global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P0, const uint32_t *__restrict__ cellStartM,
                                                          const int *__restrict__ lipids,
                                                          const int *__restrict__ lipidCount,
+                                                         const int4 *__restrict__ pinfo,
                                                          const float4 *__restrict__ ppos_,
                                                          const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                          uint4 *__restrict__ pool, int poolCap,
@@ -1600,10 +1619,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < *lipidCount;
     int c = 0;
-    if (valid) build_lm_item(P, cellStartM, lipids[t], ppos_, mpos, minfo, scratch, c);
-    const PoolSlot<uint4> S = pool_take<SC_LIST_LM>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, nullptr,
-                                             nullptr, lipids);
+    if (valid) {
+        ScParams P = P0;
+        rep_apply<BATCH>(P, pinfo[lipids[t]].w);
+        build_lm_item(P, cellStartM, lipids[t], ppos_, mpos, minfo, scratch, c);
+    }
+    const PoolSlot<uint4> S = pool_take<SC_LIST_LM>(P0, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap,
+                                                    nullptr, nullptr, lipids);
     if (S.n == 0) return;
+    ScParams P = P0;
+    rep_apply<BATCH>(P, pinfo[S.i].w);
     const float4 p4 = ppos_[S.i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M);
@@ -1623,6 +1648,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P, const uint3
 // adds its precomputed geometry and current velocity with weight 2, in list
 // order; the pairs are taken four at a time (entries, then velocities, all
 // in flight together).  An overflowed lipid scans its neighbourhood.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     ScParams P, const uint32_t *__restrict__ cellStartM, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
@@ -1634,6 +1660,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     if (i < 0) return;
     int4 in = pinfo[i];
     if (!(in.z & SC_ACTIVE) || in.y != SC_PARTICLE_TYPE_LIPID) return;
+    rep_apply<BATCH>(P, in.w);
     float4 p4 = ppos_[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const float prad = p4.w;
@@ -1748,6 +1775,7 @@ __device__ __forceinline__ bool bind_draw(const ScParams &P, const sc_rule &r, i
     return !r.use_probability || sc_bind_uniform(P.seed, r.id, pid, tid, step) < r.probability;
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_complexify(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
     const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
@@ -1757,6 +1785,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_complexify(
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
     const int i = work[t];
     int4 in = info[i];
+    rep_apply<BATCH>(P, in.w);
     int pnb = nbIn[i];
     const int cs = P.pidx[2 * in.y], ce = P.pidx[2 * in.y + 1];
     float4 p4 = pos[i];
@@ -1874,6 +1903,7 @@ __device__ __forceinline__ unsigned long long claim_key(sc_f3 delta, int i) {
     return ((unsigned long long)sc_f2u(sc_normsq3(delta)) << 32) | (unsigned)i;
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_claim_offer(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
     const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
@@ -1882,6 +1912,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_claim_offer(
   const int step = prep ? -1 : *stepPtr;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *workCount; t += gridDim.x * blockDim.x) {
     const int i = work[t];
+    rep_apply<BATCH>(P, info[i].w);
     const ClaimItem a = claim_item(P, pos, rot, info, state, nbIn, bonds, i);
     if (a.nb >= SC_MAX_ACTIVE_INTERACTIONS) continue;
     const Imager IM(P, a.pos, SC_BINNED_P);
@@ -1898,6 +1929,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_claim_offer(
   }
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_claim_bind(
     ScParams P, const int *__restrict__ work, const int *__restrict__ workCount, const float4 *__restrict__ pos,
     const float4 *__restrict__ rot, const int4 *__restrict__ info, const int *__restrict__ state,
@@ -1911,6 +1943,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_claim_bind(
     const int j = (int)(unsigned)(key & 0xffffffffull);
     if (key != ~0ull && (int)(unsigned)(claim[j] & 0xffffffffull) == i) {
         const int lo = min(i, j), hi = max(i, j);
+        rep_apply<BATCH>(P, info[lo].w);
         const ClaimItem a = claim_item(P, pos, rot, info, state, nbIn, bonds, lo);
         const ClaimItem b = claim_item(P, pos, rot, info, state, nbIn, bonds, hi);
         const Imager IM(P, a.pos, SC_BINNED_P);
@@ -1929,6 +1962,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_claim_bind(
 }
 
 // ---- interactions.cuh:349-555 transitionInteractions -------------------------
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_transition(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
     const int *__restrict__ stepPtr, const float4 *__restrict__ pos, const float4 *__restrict__ rot,
@@ -1938,6 +1972,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
     if (i >= *nActivePtr) return;
     const int step = *stepPtr;
     int4 in = info[i];
+    rep_apply<BATCH>(P, in.w);
     int pnb = min(max(nbIn[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
     int pstate = stateIn[i];
     int b[SC_MAX_ACTIVE_INTERACTIONS * 3];
@@ -2228,6 +2263,7 @@ __device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *
     });
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32_t *__restrict__ cellStart,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
@@ -2236,11 +2272,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
-    if (valid && (info[i].z & SC_ACTIVE)) build_d_item(P, cellStart, i, pos, info, scratch, c);
+    if (valid) {
+        const int4 in = info[i];
+        ScParams Q = P;
+        rep_apply<BATCH>(Q, in.w);
+        if (in.z & SC_ACTIVE) build_d_item(Q, cellStart, i, pos, info, scratch, c);
+    }
     emit_count_ordered<SC_LIST_D>(valid, c, P.listLimit, cap, scratch, list, cnt, perm);
 }
 
-template <int SP>
+template <int SP, bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32_t *__restrict__ cellStart,
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
@@ -2251,6 +2292,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
     if (g >= *nActivePtr) return;
     const int i = L.perm[g];
     if (i < 0) return;
+    if (BATCH) rep_apply<BATCH>(P, info[i].w);
     float pm[SP];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -2337,6 +2379,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
 // ---- metabolites.cuh:18-88 removeInterferingMetabolicParticles -------------
 // Only the item's own flags change and no other thread reads metabolic
 // flags here: updated in place.
+template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
     ScParams P, const uint32_t *__restrict__ cellStartP, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ mpos, int4 *__restrict__ minfo, const float4 *__restrict__ ppos_,
@@ -2345,6 +2388,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_remove_interfering(
     if (i >= *nActivePtr) return;
     int4 in = minfo[i];
     if (!(in.z & SC_ACTIVE)) return;
+    rep_apply<BATCH>(P, in.w);
     float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_P);
@@ -2404,18 +2448,21 @@ __global__ void __launch_bounds__(SC_THREADS) k_reduce_metabolic(const int *__re
 // ---- launchers ------------------------------------------------------------------
 static inline int nblocks(int n) { return (n + SC_THREADS - 1) / SC_THREADS; }
 
+// The instantiation of a kernel for this launch: replica-aware in batched sims.
+#define SC_BATCHED(kern) (c.P.nRep > 1 ? kern<true> : kern<false>)
+
 void sc_phase_move_brownian(ScLaunchCtx &c, bool metabolic) {
     ScBuffers &B = *c.B;
     if (!metabolic) {
         PFields F = B.P();
         if (c.P.N <= 0) return;
-        k_move_brownian<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.dbg, F.posnoise,
+        SC_BATCHED(k_move_brownian)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.dbg, F.posnoise,
                                                                   F.angnoise, c.P, c.P.moveNoise, SC_STREAM_P_UNIFORM,
                                                                   SC_STREAM_P_NORMAL, &B.ctr->step);
     } else {
         MFields F = B.M();
         if (c.P.Nm <= 0) return;
-        k_move_brownian<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, F.info, F.pos, F.dbg, F.posnoise,
+        SC_BATCHED(k_move_brownian)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, F.info, F.pos, F.dbg, F.posnoise,
                                                                    F.angnoise, c.P, c.P.metabNoise,
                                                                    SC_STREAM_M_UNIFORM, SC_STREAM_M_NORMAL,
                                                                    &B.ctr->step);
@@ -2429,7 +2476,7 @@ static void ensure_pp(ScLaunchCtx &c) {
     PFields F = B.P();
     cudaMemsetAsync(B.ctr->ppClassCount, 0, sizeof(B.ctr->ppClassCount), c.st);
     cudaMemsetAsync(&B.ctr->ovfPP, 0, sizeof(int), c.st);
-    k_build_pp<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
+    SC_BATCHED(k_build_pp)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.nb,
                                                          F.bonds, B.listPP, B.cntPP, c.P.N, B.classPP,
                                                          B.ctr->ppClassCount, B.ovfPP, &B.ctr->ovfPP, B.matchPP,
                                                          B.matchN);
@@ -2454,7 +2501,7 @@ void sc_phase_coordinate_noise(ScLaunchCtx &c, float frac) {
     // values by class position until they are written back in place
     PFields F = B.P(), X = B.Pnext();
     const int g = std::min(nblocks(c.P.N), c.gridCap);
-    k_coordinate_noise<<<g, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.classPP, B.ctr->ppClassCount, F.pos, F.info,
+    SC_BATCHED(k_coordinate_noise)<<<g, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.classPP, B.ctr->ppClassCount, F.pos, F.info,
                                                     F.nb, F.bonds, pp_list(c), B.matchPP, B.matchN, F.posnoise,
                                                     F.angnoise, X.posnoise, X.angnoise, frac);
     k_noise_writeback<<<g, SC_THREADS, 0, c.st>>>(B.classPP, B.ctr->ppClassCount, X.posnoise, X.angnoise,
@@ -2497,16 +2544,17 @@ void sc_phase_relax(ScLaunchCtx &c) {
         cudaStreamWaitEvent(c.side[0], c.fork, 0);
         cudaStreamWaitEvent(c.side[1], c.fork, 0);
     }
-    k_relax<0><<<g, SC_THREADS, 0, c.st>>>(c.P, A);
-    k_relax<2><<<g, SC_THREADS, 0, fork ? c.side[0] : c.st>>>(c.P, A);
-    k_relax<1><<<g, SC_THREADS, 0, fork ? c.side[1] : c.st>>>(c.P, A);
+    const bool batch = c.P.nRep > 1;
+    (batch ? k_relax<0, true> : k_relax<0, false>)<<<g, SC_THREADS, 0, c.st>>>(c.P, A);
+    (batch ? k_relax<2, true> : k_relax<2, false>)<<<g, SC_THREADS, 0, fork ? c.side[0] : c.st>>>(c.P, A);
+    (batch ? k_relax<1, true> : k_relax<1, false>)<<<g, SC_THREADS, 0, fork ? c.side[1] : c.st>>>(c.P, A);
     if (fork) {
         cudaEventRecord(c.join[0], c.side[0]);
         cudaEventRecord(c.join[1], c.side[1]);
         cudaStreamWaitEvent(c.st, c.join[0], 0);
         cudaStreamWaitEvent(c.st, c.join[1], 0);
     }
-    k_relax_overflow<<<std::min(nblocks(c.P.N), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfPP, &B.ctr->ovfPP);
+    SC_BATCHED(k_relax_overflow)<<<std::min(nblocks(c.P.N), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfPP, &B.ctr->ovfPP);
     (*c.launches) += 3;
     B.cp[FP_VEL] ^= 1;
     B.cp[FP_ROT] ^= 1;
@@ -2538,7 +2586,9 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
                 B.cntM, B.ovfM, &B.ctr->ovfM);
         } else {
             cudaMemsetAsync(&B.ctr->poolM, 0, sizeof(B.ctr->poolM), c.st);
-            (c.P.metabLean ? k_build_m<true> : k_build_m<false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
+            (c.P.nRep > 1 ? (c.P.metabLean ? k_build_m<true, true> : k_build_m<false, true>)
+                          : (c.P.metabLean ? k_build_m<true, false> : k_build_m<false, false>))<<<
+                nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
                 c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info, B.listM,
                 (int)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
         }
@@ -2559,10 +2609,11 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
             B.cellStartM + c.P.cells, &B.ctr->nActiveM, M.vel, X.vel);
         (*c.launches) += 2;
     } else {
-        (c.P.metabLean ? k_relax_metab_lean : k_relax_metab)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
+        (c.P.metabLean ? (c.P.nRep > 1 ? k_relax_metab_lean<true> : k_relax_metab_lean<false>) : k_relax_metab)<<<
+            nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
         (*c.launches)++;
     }
-    k_relax_metab_overflow<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,
+    SC_BATCHED(k_relax_metab_overflow)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,
                                                                                              &B.ctr->ovfM);
     B.cm[FM_VEL] ^= 1;
     (*c.launches)++;
@@ -2578,8 +2629,9 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
         cudaMemsetAsync(&B.ctr->poolLM, 0, sizeof(B.ctr->poolLM), c.st);
         cudaMemsetAsync(&B.ctr->workCount, 0, sizeof(int), c.st);
         k_lipid_select<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, B.workP, &B.ctr->workCount);
-        k_build_lm<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
-            c.P, B.cellStartM, B.workP, &B.ctr->workCount, F.pos, M.pos, M.info, reinterpret_cast<uint4 *>(B.listLM),
+        SC_BATCHED(k_build_lm)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
+            c.P, B.cellStartM, B.workP, &B.ctr->workCount, F.info, F.pos, M.pos, M.info,
+            reinterpret_cast<uint4 *>(B.listLM),
             (int)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,
             c.P.N);
         (*c.launches)++;
@@ -2591,7 +2643,7 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
     L.cnt = B.cntLM;
     L.cap = c.P.N;
     L.perm = B.permLM;
-    k_relax_partners<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
+    SC_BATCHED(k_relax_partners)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActive, F.pos, F.info,
                                                                F.vel, L, reinterpret_cast<const uint4 *>(B.listLM),
                                                                B.warpOffLM, M.pos, M.info, M.vel);
     (*c.launches)++;
@@ -2601,13 +2653,13 @@ void sc_phase_apply_velocities(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N > 0) {
         PFields F = B.P();
-        k_apply_velocities<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.vel, F.rot,
+        SC_BATCHED(k_apply_velocities)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.pos, F.vel, F.rot,
                                                                      F.angvel, c.P, 0.45f);
         (*c.launches)++;
     }
     if (c.P.Nm > 0) {
         MFields M = B.M();
-        k_apply_velocities<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, M.info, M.pos, M.vel, M.rot,
+        SC_BATCHED(k_apply_velocities)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(&B.ctr->nActiveM, M.info, M.pos, M.vel, M.rot,
                                                                       M.angvel, c.P, 0.45f);
         (*c.launches)++;
     }
@@ -2622,14 +2674,14 @@ void sc_phase_complexify(ScLaunchCtx &c, bool prep) {
                                                                   B.workP, &B.ctr->workCount);
     const int blocks = std::min(nblocks(c.P.N), c.gridCap);
     if (!c.P.pairClaim) {
-        k_complexify<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
+        SC_BATCHED(k_complexify)<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
                                                       F.info, F.state, F.nb, X.nb, F.bonds, &B.ctr->step, prep);
         (*c.launches) += 2;
     } else {
         cudaMemsetAsync(B.claimP, 0xff, (size_t)c.P.N * sizeof(unsigned long long), c.st);
-        k_claim_offer<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
+        SC_BATCHED(k_claim_offer)<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, B.workP, &B.ctr->workCount, F.pos, F.rot,
                                                        F.info, F.state, F.nb, F.bonds, &B.ctr->step, prep, B.claimP);
-        k_claim_bind<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.workP, &B.ctr->workCount, F.pos, F.rot, F.info, F.state,
+        SC_BATCHED(k_claim_bind)<<<blocks, SC_THREADS, 0, c.st>>>(c.P, B.workP, &B.ctr->workCount, F.pos, F.rot, F.info, F.state,
                                                       F.nb, X.nb, F.bonds, &B.ctr->step, prep, B.claimP);
         (*c.launches) += 3;
     }
@@ -2640,7 +2692,7 @@ void sc_phase_transition(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     PFields F = B.P(), X = B.Pnext();
-    k_transition<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, &B.ctr->step, F.pos, F.rot,
+    SC_BATCHED(k_transition)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActive, &B.ctr->step, F.pos, F.rot,
                                                            F.info, F.state, X.state, F.nb, X.nb, F.bonds, X.bonds,
                                                            F.lscs, F.spoly);
     B.cp[FP_STATE] ^= 1;
@@ -2666,7 +2718,7 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     if (!B.validD) {
         // the metabolic relaxation list's buffer is the build scratch
         B.validM = false;
-        k_build_d<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+        SC_BATCHED(k_build_d)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
                                                              B.listD, B.listM, B.cntD, B.permD, c.P.Nm);
         (*c.launches)++;
         B.validD = true;
@@ -2678,15 +2730,15 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     L.perm = B.permD;
     switch (c.P.SP) {
         case 4:
-            k_diffuse<4><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+            (c.P.nRep > 1 ? k_diffuse<4, true> : k_diffuse<4, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
                                                                    L, M.met, X.met);
             break;
         case 8:
-            k_diffuse<8><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
+            (c.P.nRep > 1 ? k_diffuse<8, true> : k_diffuse<8, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
                                                                    L, M.met, X.met);
             break;
         default:
-            k_diffuse<12><<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
+            (c.P.nRep > 1 ? k_diffuse<12, true> : k_diffuse<12, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
                                                                     M.info, L, M.met, X.met);
             break;
     }
@@ -2699,7 +2751,7 @@ void sc_phase_remove_interfering(ScLaunchCtx &c) {
     if (c.P.Nm <= 0) return;
     MFields M = B.M();
     PFields F = B.P();
-    k_remove_interfering<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info,
+    SC_BATCHED(k_remove_interfering)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info,
                                                                     F.pos, F.info);
     (*c.launches)++;
 }

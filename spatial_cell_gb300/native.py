@@ -53,6 +53,10 @@ _SIGS = {
     "sc_frames_write_header": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config)]),
     "sc_frames_write_frame": (ctypes.c_int, [_P, ctypes.POINTER(abi.Config), _P, _P]),
     "sc_sort_cells_static": (ctypes.c_int, [ctypes.POINTER(abi.Config), _P, _P, ctypes.c_int32, _P, _P, _P]),
+    "sc_create_batch": (ctypes.c_int, [ctypes.POINTER(abi.Config), _P, ctypes.c_int32, _P, ctypes.c_int32, _P,
+                                       ctypes.c_int32, ctypes.POINTER(_P)]),
+    "sc_load_batch": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32]),
+    "sc_export_replica": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
 }
 
 # Every symbol include/spatialcell.h declares.
@@ -134,16 +138,28 @@ def grid(cfg):
 class Simulation:
     """One simulation on the current CUDA device (include/spatialcell.h)."""
 
-    def __init__(self, cfg, types, rules):
+    def __init__(self, cfg, types, rules, replicas=None):
         self.L = lib()
         self.cfg = cfg
         self.types = np.ascontiguousarray(types, dtype=abi.TYPE_INFO_DTYPE)
         self.rules = np.ascontiguousarray(rules, dtype=abi.RULE_DTYPE)
         h = ctypes.c_void_p()
-        _check(self.L.sc_create(ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules),
-                                len(self.rules), ctypes.byref(h)), None, "sc_create")
+        if replicas is None:
+            _check(self.L.sc_create(ctypes.byref(cfg), abi.ptr(self.types), len(self.types), abi.ptr(self.rules),
+                                    len(self.rules), ctypes.byref(h)), None, "sc_create")
+            self.n_grid, self.bits, self.cells = abi.grid_dims(cfg)
+        else:
+            self.replicas = (abi.Replica * len(replicas))(*replicas)
+            _check(self.L.sc_create_batch(ctypes.byref(cfg), self.replicas, len(replicas), abi.ptr(self.types),
+                                          len(self.types), abi.ptr(self.rules), len(self.rules), ctypes.byref(h)),
+                   None, "sc_create_batch")
+            # the batch's capacities and key space
+            self.cfg = abi.config_from_bytes(bytes(cfg))
+            self.cfg.num_particles = sum(r.num_particles for r in replicas)
+            self.cfg.num_metabolic_particles = sum(r.num_metabolic_particles for r in replicas)
+            self.cells = sum(abi.grid_dims(abi.make_config(sim_size=r.sim_size,
+                                                           grid_cell_size=cfg.grid_cell_size))[2] for r in replicas)
         self.h = h
-        self.n_grid, self.bits, self.cells = abi.grid_dims(cfg)
 
     def close(self):
         if getattr(self, "h", None):
@@ -166,6 +182,23 @@ class Simulation:
             next_particle_id = len(p)
         _check(self.L.sc_load_state(self.h, abi.ptr(p), len(p), abi.ptr(m), len(m), step, next_particle_id), self.h,
                "sc_load_state")
+
+    def load_batch(self, states, step=0):
+        """Loads a batched sim: states[r] = (particles, metabolic) of replica r."""
+        p = np.ascontiguousarray(np.concatenate([np.asarray(x[0], abi.PARTICLE_DTYPE) for x in states]))
+        m = np.ascontiguousarray(np.concatenate([np.asarray(x[1], abi.METABOLIC_DTYPE) for x in states]))
+        n = np.array([len(x[0]) for x in states], np.int32)
+        nm = np.array([len(x[1]) for x in states], np.int32)
+        _check(self.L.sc_load_batch(self.h, abi.ptr(p), abi.ptr(n), abi.ptr(m), abi.ptr(nm), step), self.h,
+               "sc_load_batch")
+
+    def export_replica(self, r):
+        """Replica r's records (sc_export_replica), arrays of its capacities."""
+        q = self.replicas[r]
+        p = np.zeros(q.num_particles, abi.PARTICLE_DTYPE)
+        m = np.zeros(q.num_metabolic_particles, abi.METABOLIC_DTYPE)
+        _check(self.L.sc_export_replica(self.h, r, abi.ptr(p), abi.ptr(m)), self.h, "sc_export_replica")
+        return p, m
 
     def load_state_ptr(self, p_ptr, n, m_ptr, nm, step=0, next_particle_id=0):
         """Loads from raw host pointers (e.g. pinned buffers)."""

@@ -358,3 +358,13 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, p
                           relaxation_steps=6, metabolite_diffusion_steps=3, steps=10, periodic=periodic,
                           walls=walls)
     return cfg, types, rules, p, m, n
+
+
+def batch_of(replica_states):
+    """The batched-sim form of replica cells (as batch_replicas gives them):
+    the shared config (replica 0's; the others differ only in capacities,
+    box and seed) and one abi.Replica per cell."""
+    cfg0 = replica_states[0][0]
+    reps = [abi.Replica(c.num_particles, c.num_metabolic_particles, c.sim_size, 0, c.seed)
+            for c, *_ in replica_states]
+    return cfg0, reps
