@@ -265,54 +265,79 @@ def cpu_sample(args, reps=1, warmup=0):
 
 
 def batched_sample(args, native, torch):
-    """Many independent replica cells (the batched workload's size and mix
-    distribution, a sample of its 512 replicas): every replica steps on its own
-    stream as a captured graph, all in flight together, against the same
-    replicas stepped one at a time.  Wall-clock with the device synchronised
-    on both sides; particle-steps/s of all replicas."""
+    """The batched workload: args.batch_replicas replica cells (particles
+    log-uniform in [2048, 262144] from seed 3, metabolic x2, each periodic
+    cube at the small workload's density, mix ~ Dirichlet(2,2,1,1)) stepped
+    as ONE batched sim -- every phase one launch over all replicas, the
+    replica in the high part of the sort key, each step a captured graph --
+    against a sample of the same replicas stepped one at a time as sims of
+    their own.  Scenes are generated on the device.  The grid cell size is
+    the autotuner's pick on a sub-batch.  Device-resident timing with CUDA
+    events on the sim's stream."""
     from spatial_cell_gb300 import autotune
-    reps = scenes.batch_replicas(args.batch_replicas)
-    # the tuner picks cell size and tile use on a median-size cell; work
-    # classes stay on one stream per cell (many cells fill the device)
-    mid = sorted(reps, key=lambda r: r[0].num_particles)[len(reps) // 2][0]
-    best, times = autotune.tune(mid, fork=(0,))
-    sims = []
-    for cfg, types, rules, p, m in reps:
-        cfg = autotune.apply(cfg, best)
-        s = native.Simulation(cfg, types, rules)
-        s.load_state(p, m)
-        s.prepare()
-        s.step(1)  # warm-up: captures the step graphs
-        sims.append(s)
-    items = sum(c.num_particles + c.num_metabolic_particles for c, *_ in reps)
-    for s in sims:
-        s.sync()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.batch_steps):
-        for s in sims:
-            s.step(1)
-    for s in sims:
-        s.sync()
-    batched_s = time.perf_counter() - t0
-    alone_s = 0.0
-    for s in sims:
-        t0 = time.perf_counter()
-        s.step(args.batch_steps)
-        s.sync()
-        alone_s += time.perf_counter() - t0
-    for s in sims:
-        s.close()
+    specs = scenes.batch_specs(args.batch_replicas)
+    kinds = (scenes.LIPID, scenes.DUMMY, scenes.TYPE_A, scenes.TYPE_B)
+    types, rules = scenes.baseline_types(), scenes.workload_rules()
+
+    def make_batch(sp, cell):
+        cfg, reps = scenes.batch_sim_args(sp, grid_cell_size=cell)
+        b = native.Simulation(cfg, types, rules, replicas=reps)
+        b.generate_batch([x[0] for x in sp], [x[1] for x in sp], kinds, [x[3] for x in sp], [x[4] for x in sp])
+        b.prepare()
+        return b
+
+    def timed_steps(sim, k):
+        stream = torch.cuda.ExternalStream(sim.stream_handle())
+        sim.step(1)  # captures the step graph
+        sim.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(k)
+        e1.record(stream)
+        e1.synchronize()
+        sim.sync()
+        return e0.elapsed_time(e1) / 1e3
+
+    # the autotuner's cell size, timed on every 16th replica as one batch
+    sub = specs[::16] or specs
+    sub_items = sum(n + nm for n, nm, *_ in sub)
+    times = {}
+    for cell in autotune.batch_cells(scenes.measured_config("plain_small")):
+        b = make_batch(sub, cell)
+        times[cell] = timed_steps(b, 2) / 2
+        b.close()
+    cell = min(times, key=lambda c: (times[c], c))
+    items = sum(n + nm for n, nm, *_ in specs)
+    b = make_batch(specs, cell)
+    batched_s = timed_steps(b, args.batch_steps)
+    finite = all(np.isfinite(b.export_replica(r)[0]["pos"]).all() for r in (0, len(specs) // 2, len(specs) - 1))
+    b.close()
     batched = items * args.batch_steps / batched_s
-    alone = items * args.batch_steps / alone_s
-    return {"replicas": len(reps), "particles_and_metabolic": items, "steps": args.batch_steps,
-            "value": batched, "unit": UNIT, "one_at_a_time": alone, "speedup": batched / alone,
+    # one at a time: a sample of the replicas (every 8th), each a sim of its own
+    alone_items, alone_s = 0, 0.0
+    k = max(2, args.batch_steps // 10)
+    for n, nm, box, mix, sd in specs[::8]:
+        c = scenes.measured_config("plain_small", num_particles=n, num_metabolic_particles=nm, sim_size=box, seed=sd,
+                                   grid_cell_size=cell)
+        s1 = native.Simulation(c, types, rules)
+        s1.generate_uniform(n, nm, kinds, mix, sd)
+        s1.prepare()
+        alone_s += timed_steps(s1, k)
+        alone_items += (n + nm) * k
+        s1.close()
+    alone = alone_items / alone_s
+    return {"replicas": len(specs), "particles": sum(x[0] for x in specs),
+            "metabolic_particles": sum(x[1] for x in specs), "steps": args.batch_steps, "value": batched,
+            "unit": UNIT, "ms_per_step": 1e3 * batched_s / args.batch_steps, "state_finite": finite,
+            "one_at_a_time": alone, "one_at_a_time_sample": f"{len(specs[::8])} replicas (every 8th), {k} steps each",
+            "speedup": batched / alone,
+            "form": "one batched sim: one launch per phase over all replicas, replica in the high key bits, "
+                    "graph-captured step",
             "sizes": "particles log-uniform in [2048, 262144] (seed 3), metabolic x2, cubes at 65,536 per "
-                     "(200 nm)^3, mix Dirichlet(2,2,1,1), periodic",
-            "autotuned": {"cell_nm": best[0], "tiles": best[2], "tuned_on_particles": mid.num_particles,
-                          "candidates_ms_per_step": {f"cell {c:g} tiles {t}": round(v * 1e3, 3)
-                                                     for (c, f, t), v in sorted(times.items())}},
-            "timing": "wall clock, device synchronised before and after"}
+                     "(200 nm)^3, mix Dirichlet(2,2,1,1), periodic, pair claim, A + B at p = 0.1",
+            "autotuned": {"cell_nm": cell, "tuned_on": f"{len(sub)} replicas ({sub_items} items) as one batch",
+                          "candidates_ms_per_step": {f"cell {c:g}": round(v * 1e3, 3) for c, v in sorted(times.items())}},
+            "timing": "CUDA events on the batch's stream, after a warm-up step"}
 
 
 def serving_sample(args, capacity):
@@ -661,9 +686,9 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.25,
                     help="volume fraction of the workload the CPU oracle steps (its timed sample)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--batch-replicas", type=int, default=64,
+    ap.add_argument("--batch-replicas", type=int, default=512,
                     help="replica cells in the batched sample (0: skip it)")
-    ap.add_argument("--batch-steps", type=int, default=4)
+    ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving sample (0: skip it)")
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")

@@ -375,6 +375,11 @@ int sc_create_batch(const sc_config *cfg, const sc_replica *replicas, int32_t n_
  * sc_load_state per replica). */
 int sc_load_batch(sc_sim *sim, const sc_particle *particles, const int32_t *n, const sc_metabolic_particle *metabolic,
                   const int32_t *nm, int32_t step);
+/* Fills every replica on the device: replica r gets the scene
+ * sc_generate_uniform(n[r], nm[r], kinds, fractions + r * nkinds, nkinds,
+ * seeds[r]) writes for a sim of its own with the replica's box. */
+int sc_generate_batch(sc_sim *sim, const int32_t *n, const int32_t *nm, const int32_t *kinds, const float *fractions,
+                      int32_t nkinds, const uint64_t *seeds);
 /* Replica r's records in slot order into buffers of its capacities (zero
  * past its records): what sc_export_state gives for a sim of its own. */
 int sc_export_replica(sc_sim *sim, int32_t replica, sc_particle *particles, sc_metabolic_particle *metabolic);

@@ -73,3 +73,10 @@ def apply(cfg, choice):
     d["class_streams"] = 3 if choice[1] else 1
     d["tiles"] = int(choice[2])
     return abi.make_config(**d)
+
+
+def batch_cells(cfg, cells=(6.0, 7.0, 8.0)):
+    """Grid cell sizes to try for a batch of replicas with cfg's physics (the
+    smallest replica's box is checked by sc_create_batch)."""
+    lo = max(cfg.max_interaction_distance, cfg.max_diffusion_distance)
+    return [float(c) for c in cells if c >= lo]

@@ -1084,6 +1084,8 @@ int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *me
     return check_launch(s);
 }
 
+static int set_batch_reps(sc_sim *s, const std::vector<int> &offP, const std::vector<int> &offM);
+
 int sc_load_batch(sc_sim *s, const sc_particle *particles, const int32_t *n, const sc_metabolic_particle *metabolic,
                   const int32_t *nm, int32_t step) {
     if (!s || !n || !nm) return set_err(s, SC_E_INVALID, "null argument");
@@ -1098,6 +1100,14 @@ int sc_load_batch(sc_sim *s, const sc_particle *particles, const int32_t *n, con
     }
     int rc = sc_load_state(s, particles, offP[R], metabolic, offM[R], step, 0);
     if (rc) return rc;
+    return set_batch_reps(s, offP, offM);
+}
+
+// The replica ids of a batch just loaded or generated, from the replicas'
+// item counts (offsets: prefix sums).
+static int set_batch_reps(sc_sim *s, const std::vector<int> &offP, const std::vector<int> &offM) {
+    const int R = (int)s->reps.size();
+    int rc;
     int *dOff = nullptr;
     if ((rc = dalloc(s, &dOff, 2 * ((size_t)R + 1)))) return rc;
     SC_CK(s, cudaMemcpyAsync(dOff, offP.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
@@ -1276,6 +1286,70 @@ int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, 
     return generate_into(s, n, nm, seed, [&](float box) {
         k_gen_particles<<<nb_of(n), SC_THREADS, 0, s->st>>>(s->staging, n, box, mix, seed);
     });
+}
+
+int sc_generate_batch(sc_sim *s, const int32_t *n, const int32_t *nm, const int32_t *kinds, const float *fractions,
+                      int32_t nkinds, const uint64_t *seeds) {
+    if (!s || !n || !nm || !seeds) return set_err(s, SC_E_INVALID, "null argument");
+    if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
+    cudaSetDevice(s->device);
+    const int R = (int)s->reps.size();
+    std::vector<int> offP(R + 1, 0), offM(R + 1, 0);
+    std::vector<sc_gen_mix> mix((size_t)R);
+    for (int r = 0; r < R; r++) {
+        if (n[r] < 0 || nm[r] < 0 || n[r] > s->reps[r].num_particles || nm[r] > s->reps[r].num_metabolic_particles)
+            return set_err(s, SC_E_INVALID, "replica " + std::to_string(r) + ": scene larger than its capacity");
+        memset(&mix[r], 0, sizeof mix[r]);
+        if (n[r] > 0 && (!kinds || !fractions ||
+                         sc_gen_make_mix(&mix[r], kinds, fractions + (size_t)r * nkinds, nkinds, s->types.data(),
+                                         (int)s->types.size())))
+            return set_err(s, SC_E_INVALID, "the particle mix needs 1 to 4 kinds of the type table, weights >= 0");
+        offP[r + 1] = offP[r] + n[r];
+        offM[r + 1] = offM[r] + nm[r];
+    }
+    if (offM[R] > 0 && (int)s->types.size() <= SC_PARTICLE_TYPE_METABOLIC)
+        return set_err(s, SC_E_INVALID, "the type table has no metabolic particle type (1000)");
+    const int N = s->P.N, Nm = s->P.Nm;
+    size_t bytes = std::max((size_t)offP[R] * sizeof(sc_particle), (size_t)offM[R] * sizeof(sc_metabolic_particle));
+    int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    B.invalidateLists();
+    s->P.binned = 0;
+    s->P.mAllActive = 0;
+    s->P.lipidValid = 0;
+    for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
+    for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
+    // each replica's records as sc_generate_uniform writes them for a sim of
+    // its own (ids from 0, its box, its mix and seed), one replica after another
+    if (N > 0) {
+        for (int r = 0; r < R; r++)
+            if (n[r] > 0)
+                k_gen_particles<<<nb_of(n[r]), SC_THREADS, 0, s->st>>>(
+                    s->staging + (size_t)offP[r] * sizeof(sc_particle), n[r], s->reps[r].sim_size, mix[r], seeds[r]);
+        k_unpack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, offP[R], N, B.p[0]);
+    }
+    if (Nm > 0) {
+        const sc_type_info &mt = s->types[SC_PARTICLE_TYPE_METABOLIC];
+        for (int r = 0; r < R; r++)
+            if (nm[r] > 0)
+                k_gen_metabolic<<<nb_of(nm[r]), SC_THREADS, 0, s->st>>>(
+                    s->staging + (size_t)offM[r] * sizeof(sc_metabolic_particle), nm[r], s->reps[r].sim_size,
+                    s->cfg.num_metabolites, mt.radius, mt.hydrophobic, seeds[r]);
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, offM[R], Nm, s->P.SP, B.m[0], B.mcLscs,
+                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+    }
+    ScCounters c;
+    memset(&c, 0, sizeof c);
+    c.nActive = offP[R];
+    c.lastActive = offP[R] - 1;
+    c.nActiveM = offM[R];
+    SC_CK(s, cudaMemcpyAsync(B.ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    if ((rc = check_launch(s))) return rc;
+    release_staging(s);
+    s->loaded = true;
+    return set_batch_reps(s, offP, offM);
 }
 
 int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed) {

@@ -57,6 +57,7 @@ _SIGS = {
                                        ctypes.c_int32, ctypes.POINTER(_P)]),
     "sc_load_batch": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32]),
     "sc_export_replica": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "sc_generate_batch": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32, _P]),
 }
 
 # Every symbol include/spatialcell.h declares.
@@ -191,6 +192,18 @@ class Simulation:
         nm = np.array([len(x[1]) for x in states], np.int32)
         _check(self.L.sc_load_batch(self.h, abi.ptr(p), abi.ptr(n), abi.ptr(m), abi.ptr(nm), step), self.h,
                "sc_load_batch")
+
+    def generate_batch(self, n, nm, kinds, fractions, seeds):
+        """Fills a batched sim on the device (sc_generate_batch): replica r gets
+        n[r] particles of the kinds with weights fractions[r] and nm[r]
+        metabolic particles, seeded by seeds[r]."""
+        n = np.ascontiguousarray(n, np.int32)
+        nm = np.ascontiguousarray(nm, np.int32)
+        k = np.ascontiguousarray(kinds, np.int32)
+        f = np.ascontiguousarray(fractions, np.float32).reshape(len(n), len(k))
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        _check(self.L.sc_generate_batch(self.h, abi.ptr(n), abi.ptr(nm), abi.ptr(k), abi.ptr(f), len(k), abi.ptr(sd)),
+               self.h, "sc_generate_batch")
 
     def export_replica(self, r):
         """Replica r's records (sc_export_replica), arrays of its capacities."""

@@ -151,6 +151,28 @@ def workload_config(name, **overrides):
     return abi.make_config(**kw)
 
 
+def batch_specs(count, seed=3, n_lo=2048, n_hi=262144):
+    """The replica cells of the batched workload without their states:
+    (particles, metabolic, box nm, mix, seed) per replica, as batch_replicas
+    draws them (states then come from sc_generate_batch on the device)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(count):
+        n = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        box = float(200.0 * (n / 65536.0) ** (1.0 / 3.0))
+        mix = rng.dirichlet([2.0, 2.0, 1.0, 1.0])
+        out.append((n, 2 * n, box, mix, seed * 1000 + r))
+    return out
+
+
+def batch_sim_args(specs, **overrides):
+    """Config and replicas (abi.Replica) of a batch of replica specs."""
+    cfg = measured_config("plain_small", num_particles=specs[0][0], num_metabolic_particles=specs[0][1],
+                          sim_size=specs[0][2], seed=specs[0][4], **overrides)
+    reps = [abi.Replica(n, nm, box, 0, sd) for n, nm, box, _, sd in specs]
+    return cfg, reps
+
+
 def batch_replicas(count, seed=3, n_lo=2048, n_hi=262144):
     """Replica cells of the batched workload: particle counts log-uniform in
     [n_lo, n_hi], twice as many metabolic items, each periodic cube scaled to

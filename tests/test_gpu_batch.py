@@ -84,3 +84,28 @@ def test_batch_rejects_a_replica_too_small_for_its_periodic_box(product):
     replicas[1].sim_size = 2.0 * cfg.grid_cell_size
     with pytest.raises(product.ScError):
         product.Simulation(cfg, reps[0][1], reps[0][2], replicas=replicas)
+
+
+@pytest.mark.gpu
+def test_generated_batch_equals_generated_solo_sims(product):
+    """sc_generate_batch gives every replica the scene sc_generate_uniform
+    gives a sim of its own; two steps later they still agree bit for bit."""
+    specs = scenes.batch_specs(6, seed=21, n_lo=500, n_hi=4000)
+    cfg, replicas = scenes.batch_sim_args(specs)
+    types, rules = scenes.baseline_types(), scenes.workload_rules()
+    kinds = (scenes.LIPID, scenes.DUMMY, scenes.TYPE_A, scenes.TYPE_B)
+    batch = product.Simulation(cfg, types, rules, replicas=replicas)
+    batch.generate_batch([x[0] for x in specs], [x[1] for x in specs], kinds, [x[3] for x in specs],
+                         [x[4] for x in specs])
+    batch.prepare()
+    batch.step(2)
+    for r, (n, nm, box, mix, sd) in enumerate(specs):
+        c = scenes.measured_config("plain_small", num_particles=n, num_metabolic_particles=nm, sim_size=box, seed=sd)
+        solo = product.Simulation(c, types, rules)
+        solo.generate_uniform(n, nm, kinds, mix, sd)
+        solo.prepare()
+        solo.step(2)
+        assert_same_state(batch.export_replica(r), solo.export_state(), species=c.num_metabolites,
+                          what=f"generated replica {r}")
+        solo.close()
+    batch.close()
