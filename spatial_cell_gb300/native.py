@@ -186,10 +186,17 @@ class Simulation:
 
     def load_batch(self, states, step=0):
         """Loads a batched sim: states[r] = (particles, metabolic) of replica r."""
-        p = np.ascontiguousarray(np.concatenate([np.asarray(x[0], abi.PARTICLE_DTYPE) for x in states]))
-        m = np.ascontiguousarray(np.concatenate([np.asarray(x[1], abi.METABOLIC_DTYPE) for x in states]))
         n = np.array([len(x[0]) for x in states], np.int32)
         nm = np.array([len(x[1]) for x in states], np.int32)
+        # filled slice by slice: np.concatenate would drop the records' padded layout
+        p = np.zeros(int(n.sum()), abi.PARTICLE_DTYPE)
+        m = np.zeros(int(nm.sum()), abi.METABOLIC_DTYPE)
+        o = om = 0
+        for (pp, mm), k, km in zip(states, n, nm):
+            p[o:o + k] = pp
+            m[om:om + km] = mm
+            o += k
+            om += km
         _check(self.L.sc_load_batch(self.h, abi.ptr(p), abi.ptr(n), abi.ptr(m), abi.ptr(nm), step), self.h,
                "sc_load_batch")
 
