@@ -4,6 +4,8 @@
                                       # the reference tree is present
 
 * oracle/_build/libscport.so  <- oracle/scport.cpp (g++, OpenMP)
+* oracle/_build/libscport64.so <- oracle/scport64.cpp: the same restatement
+                                 in double precision (the FP64 host oracle)
 * oracle/_ref/libscref.so     <- oracle/ref_harness.cpp + the reference's
                                  spatial_cell_sim/src/*.cuh read in place,
                                  with oracle/shim first on the include path
@@ -62,6 +64,23 @@ def build_port(force=False):
         return out
     os.makedirs(os.path.dirname(out), exist_ok=True)
     _run(["g++", "-std=c++17", "-fPIC", "-shared", "-fopenmp", *FP_FLAGS, "-I", CSRC, "-I", INCLUDE,
+          srcs[0], "-o", out])
+    return out
+
+
+def port64_path():
+    return os.path.join(HERE, "_build", "libscport64.so")
+
+
+def build_port64(force=False):
+    """The FP64 build of the CPU restatement (oracle/scport64.cpp)."""
+    out = port64_path()
+    srcs = [os.path.join(HERE, "scport64.cpp"), os.path.join(HERE, "scport.cpp"), os.path.join(HERE, "scmath64.h"),
+            os.path.join(CSRC, "scmath.h"), os.path.join(CSRC, "sc_gen.h"), os.path.join(INCLUDE, "spatialcell.h")]
+    if not force and _newer(out, srcs):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    _run(["g++", "-std=c++17", "-fPIC", "-shared", "-fopenmp", *FP_FLAGS, "-I", CSRC, "-I", INCLUDE, "-I", HERE,
           srcs[0], "-o", out])
     return out
 
@@ -133,6 +152,7 @@ def build_ref_device(force=False):
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_port(force=force))
+    print(build_port64(force=force))
     print(build_ref(force=force))
     print(build_ref_cubin(force=force))
     print(build_ref_device(force=force))

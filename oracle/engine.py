@@ -1,7 +1,8 @@
 """ctypes drivers of the oracle libraries (TEST INFRASTRUCTURE ONLY).
 
 ``OracleEngine("port")`` drives oracle/_build/libscport.so (the CPU
-restatement); ``OracleEngine("ref")`` drives oracle/_ref/libscref.so (the
+restatement), ``OracleEngine("port64")`` its double-precision build
+oracle/_build/libscport64.so (the FP64 host oracle); ``OracleEngine("ref")`` drives oracle/_ref/libscref.so (the
 reference's own kernels compiled for the host); ``OracleEngine("ref_device")``
 drives oracle/_build/librefdev.so, the reference's own kernels compiled for
 sm_103a (oracle/_ref/ref_step.cubin) run on the GPU in main.cu's launch
@@ -40,6 +41,8 @@ def load(kind):
         return _LIBS[kind]
     if kind == "port":
         path, prefix = build.build_port(), "scp_"
+    elif kind == "port64":
+        path, prefix = build.build_port64(), "scp_"
     elif kind == "ref":
         path, prefix = build.build_ref(), "oref_"
         if path is None:
@@ -67,7 +70,7 @@ def load(kind):
         fns["last_error"] = lib.refdev_last_error
         fns["nonfinite"] = lib.refdev_nonfinite
         fns["guards"] = lib.refdev_guards
-    if kind == "port":
+    if kind in ("port", "port64"):
         lib.scp_set_threads.argtypes = [ctypes.c_int]
         lib.scp_max_threads.restype = ctypes.c_int
         fns["set_threads"] = lib.scp_set_threads

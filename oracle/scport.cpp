@@ -32,6 +32,53 @@
 #include "spatialcell.h"
 #include "sc_gen.h"
 
+// The state's own single-precision scalar (the ABI layouts stay float in
+// both builds below).
+typedef float sc_single;
+
+#if defined(SC_PORT_FP64)
+// The FP64 build (oracle/scport64.cpp): every floating-point quantity of the
+// step is a double -- state, temporaries, the reference's double-precision
+// expressions as they are -- with oracle/scmath64.h's vector / quaternion
+// helpers and the C library's double elementary functions.  The noise
+// draws, the rules and the load / export records stay the reference's
+// single-precision values (converted at the boundary).
+#include <math.h>
+#include "scmath64.h"
+#define sc_f2 sc_d2
+#define sc_f3 sc_d3
+#define sc_f4 sc_d4
+#define sc_make_f3 sc_make_d3
+#define sc_make_f4 sc_make_d4
+#define sc_up sc_d_up
+#define sc_right sc_d_right
+#define sc_forward sc_d_forward
+#define sc_zero3 sc_d_zero3
+#define sc_qid sc_d_qid
+#define sc_normsq3 sc_d_normsq3
+#define sc_normsq4 sc_d_normsq4
+#define sc_norm3 sc_d_norm3
+#define sc_safe_cross sc_d_safe_cross
+#define sc_qmul sc_d_qmul
+#define sc_angle3 sc_d_angle3
+#define sc_quat sc_d_quat
+#define sc_quat_from_to sc_d_quat_from_to
+#define sc_qinv sc_d_qinv
+#define sc_slerp sc_d_slerp
+#define sc_random_rotation sc_d_random_rotation
+#define sc_rotate sc_d_rotate
+#define sc_image3 sc_d_image3
+#define sc_wrap3 sc_d_wrap3
+#define sc_reflect3 sc_d_reflect3
+#define sc_grid_idx sc_d_grid_idx
+#define sc_powf pow
+#define float double
+#define fabsf fabs
+#define fminf fmin
+#define fmaxf fmax
+#define sqrtf sqrt
+#endif
+
 #if defined(_OPENMP)
 #include <omp.h>
 #define SC_OMP_FOR _Pragma("omp parallel for schedule(dynamic, 256)")
@@ -65,10 +112,72 @@ struct PP {
 struct PM : PP {
     float m[SC_AOS_NUM_METABOLITES];
 };
+#if !defined(SC_PORT_FP64)
 static_assert(sizeof(PP) == 256 && offsetof(PP, pos) == 28 && offsetof(PP, rot) == 48, "Particle layout");
 static_assert(offsetof(PP, angVel) == 96 && offsetof(PP, nb) == 128 && offsetof(PP, dbg) == 240, "Particle layout");
 static_assert(sizeof(PM) == 304 && offsetof(PM, m) == 256, "MetabolicParticle layout");
 static_assert(sizeof(PP) == sizeof(sc_particle) && sizeof(PM) == sizeof(sc_metabolic_particle), "ABI layout");
+
+// State records in and out: the reference's layout byte for byte.
+void put_particles(PP *dst, const sc_particle *src, int n) { memcpy((void *)dst, src, (size_t)n * sizeof(PP)); }
+void put_metabolic(PM *dst, const sc_metabolic_particle *src, int n) { memcpy((void *)dst, src, (size_t)n * sizeof(PM)); }
+void get_particles(sc_particle *dst, const PP *src, int n) { memcpy(dst, (const void *)src, (size_t)n * sizeof(PP)); }
+void get_metabolic(sc_metabolic_particle *dst, const PM *src, int n) { memcpy(dst, (const void *)src, (size_t)n * sizeof(PM)); }
+#else
+// State records in and out: every field converted between the reference's
+// single-precision layout and this build's doubles.
+void put_particle(PP &d, const sc_particle &r) {
+    d.id = r.id; d.type = r.type; d.flags = r.flags; d.state = r.state; d.lscs = r.last_state_change_step;
+    d.radius = r.radius; d.hydro = r.hydrophobic;
+    d.pos = sc_make_d3(r.pos[0], r.pos[1], r.pos[2]);
+    d.rot = sc_make_d4(r.rot[0], r.rot[1], r.rot[2], r.rot[3]);
+    d.vel = sc_make_d3(r.velocity[0], r.velocity[1], r.velocity[2]);
+    d.posNoise = sc_make_d3(r.pos_noise[0], r.pos_noise[1], r.pos_noise[2]);
+    d.angVel = sc_make_d4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2], r.angular_velocity[3]);
+    d.angNoise = sc_make_d4(r.angular_noise[0], r.angular_noise[1], r.angular_noise[2], r.angular_noise[3]);
+    d.nb = r.n_active_interactions;
+    memcpy(d.bonds, r.interactions, sizeof d.bonds);
+    d.spoly = r.scheduled_polymerization;
+    d.dbg = sc_make_d4(r.debug_vector[0], r.debug_vector[1], r.debug_vector[2], r.debug_vector[3]);
+}
+void get_particle(sc_particle &r, const PP &d) {
+    memset(&r, 0, sizeof r);
+    r.id = d.id; r.type = d.type; r.flags = d.flags; r.state = d.state; r.last_state_change_step = d.lscs;
+    r.radius = (sc_single)d.radius; r.hydrophobic = d.hydro;
+    const sc_single v[] = {(sc_single)d.pos.x, (sc_single)d.pos.y, (sc_single)d.pos.z, (sc_single)d.rot.x,
+                           (sc_single)d.rot.y, (sc_single)d.rot.z, (sc_single)d.rot.w, (sc_single)d.vel.x,
+                           (sc_single)d.vel.y, (sc_single)d.vel.z, (sc_single)d.posNoise.x, (sc_single)d.posNoise.y,
+                           (sc_single)d.posNoise.z, (sc_single)d.angVel.x, (sc_single)d.angVel.y,
+                           (sc_single)d.angVel.z, (sc_single)d.angVel.w, (sc_single)d.angNoise.x,
+                           (sc_single)d.angNoise.y, (sc_single)d.angNoise.z, (sc_single)d.angNoise.w,
+                           (sc_single)d.dbg.x, (sc_single)d.dbg.y, (sc_single)d.dbg.z, (sc_single)d.dbg.w};
+    memcpy(r.pos, v, 3 * sizeof(sc_single));
+    memcpy(r.rot, v + 3, 4 * sizeof(sc_single));
+    memcpy(r.velocity, v + 7, 3 * sizeof(sc_single));
+    memcpy(r.pos_noise, v + 10, 3 * sizeof(sc_single));
+    memcpy(r.angular_velocity, v + 13, 4 * sizeof(sc_single));
+    memcpy(r.angular_noise, v + 17, 4 * sizeof(sc_single));
+    memcpy(r.debug_vector, v + 21, 4 * sizeof(sc_single));
+    r.n_active_interactions = d.nb;
+    memcpy(r.interactions, d.bonds, sizeof d.bonds);
+    r.scheduled_polymerization = d.spoly;
+}
+void put_particles(PP *dst, const sc_particle *src, int n) { for (int i = 0; i < n; i++) put_particle(dst[i], src[i]); }
+void put_metabolic(PM *dst, const sc_metabolic_particle *src, int n) {
+    for (int i = 0; i < n; i++) {
+        put_particle(dst[i], src[i].p);
+        for (int k = 0; k < SC_AOS_NUM_METABOLITES; k++) dst[i].m[k] = src[i].metabolites[k];
+    }
+}
+void get_particles(sc_particle *dst, const PP *src, int n) { for (int i = 0; i < n; i++) get_particle(dst[i], src[i]); }
+void get_metabolic(sc_metabolic_particle *dst, const PM *src, int n) {
+    for (int i = 0; i < n; i++) {
+        memset(&dst[i], 0, sizeof dst[i]);
+        get_particle(dst[i].p, src[i]);
+        for (int k = 0; k < SC_AOS_NUM_METABOLITES; k++) dst[i].metabolites[k] = (sc_single)src[i].m[k];
+    }
+}
+#endif
 
 // Particle(...) constructor of types.cuh:192-221
 PP make_particle(int id, int type, float radius, int8_t hydro, sc_f3 pos, sc_f4 rot) {
@@ -915,6 +1024,7 @@ void reduce_one(const T &p, R &r) {
 
 extern "C" {
 
+#if !defined(SC_PORT_FP64)
 // ---- scmath.h entry points for the CPU tests ---------------------------------
 // fn: 0 sin, 1 cos, 2 acos, 3 log, 4 exp, 5 pow(x, y)
 void scp_math_eval(int fn, const float *x, const float *y, float *out, int n) {
@@ -1005,6 +1115,8 @@ void scp_compare_forms(int kind, const float *a, const float *b, uint8_t *bad, i
     }
 }
 
+#endif  // !SC_PORT_FP64
+
 void scp_set_threads(int n) {
 #if defined(_OPENMP)
     if (n > 0) omp_set_num_threads(n);
@@ -1035,7 +1147,11 @@ scp_sim *scp_create(const sc_config *cfg, const sc_type_info *types, int n_types
     s->periodic = cfg->periodic != 0;
     s->nUsed = ng;
     s->cellSize = cfg->grid_cell_size;
-    if (s->periodic) s->nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &s->cellSize);
+    if (s->periodic) {
+        sc_single width = 0;
+        s->nUsed = sc_periodic_cells(cfg->sim_size, cfg->grid_cell_size, &width);
+        s->cellSize = width;
+    }
     if (s->periodic && s->nUsed < 3) { delete s; return nullptr; }
     s->cells = (size_t)p2 * p2 * p2;
     s->N = cfg->num_particles;
@@ -1090,8 +1206,8 @@ int scp_load_state(scp_sim *s, const sc_particle *p, int n, const sc_metabolic_p
     if (n < 0 || nm < 0 || n > s->N || nm > s->Nm) return SC_E_INVALID;
     if (s->N) memset((void *)s->p.data(), 0, s->p.size() * sizeof(PP));
     if (s->Nm) memset((void *)s->m.data(), 0, s->m.size() * sizeof(PM));
-    if (n) memcpy((void *)s->p.data(), p, (size_t)n * sizeof(PP));
-    if (nm) memcpy((void *)s->m.data(), m, (size_t)nm * sizeof(PM));
+    if (n) put_particles(s->p.data(), p, n);
+    if (nm) put_metabolic(s->m.data(), m, nm);
     s->nActive = n; s->lastActive = n - 1; s->nextId = next_id; s->nActiveM = nm; s->step = step;
     return SC_OK;
 }
@@ -1173,8 +1289,8 @@ int scp_step(scp_sim *s, int n_steps) {
 }
 
 int scp_export_state(scp_sim *s, sc_particle *p, sc_metabolic_particle *m) {
-    if (p && s->N) memcpy(p, s->p.data(), (size_t)s->N * sizeof(PP));
-    if (m && s->Nm) memcpy(m, s->m.data(), (size_t)s->Nm * sizeof(PM));
+    if (p && s->N) get_particles(p, s->p.data(), s->N);
+    if (m && s->Nm) get_metabolic(m, s->m.data(), s->Nm);
     return SC_OK;
 }
 
