@@ -340,26 +340,48 @@ def batched_sample(args, native, torch):
             "timing": "CUDA events on the batch's stream, after a warm-up step"}
 
 
-def serving_sample(args, capacity):
-    """The request loop on a scaled-down request stream: Poisson arrivals at
-    80 % of the measured batched capacity, particle counts log-uniform in
-    [4096, 131072], horizons uniform in [10, 60] steps, mix ~ Dirichlet(1,1,1,1),
-    a 160 GB budget; against the same stream served one request at a time."""
+def serving_sample(args):
+    """The request loop (spatial_cell_gb300/serving.py) on a scaled-down
+    stream of the serving workload: particles log-uniform in [4096, 1048576],
+    metabolic x2, horizons uniform in [100, serve_horizon] steps, mix ~
+    Dirichlet(1,1,1,1), the small workload's density and physics, a 160 GB
+    budget.  Three runs: (1) saturated -- serve_saturated requests arriving
+    at once, enough that the budget binds -- giving the server's capacity;
+    (2) serve_requests requests arriving as a Poisson stream at 80 % of that
+    capacity, each streaming a frame to the host every 25 steps, giving
+    p50 / p99 latency and throughput; (3) the same stream served one request
+    at a time.  Wall clock."""
     from spatial_cell_gb300 import serving
-    probe = serving.poisson_requests(args.serve_requests, 1.0, n_lo=4096, n_hi=131072, h_lo=10, h_hi=60)
-    mean_work = sum(3 * r.n * r.horizon for r in probe) / len(probe)
+    hi = args.serve_horizon
+    sat = serving.saturated(serving.poisson_requests(args.serve_saturated, 1.0, seed=5, h_lo=100, h_hi=hi))
+    server = serving.Server(budget_bytes=160 << 30)
+    t0 = time.perf_counter()
+    res = server.run(sat)
+    sat_s = time.perf_counter() - t0
+    work = sum((r.n + r.nm) * r.horizon for r in sat)
+    capacity = work / sat_s
+    peak_bytes = sum(r.bytes for r in sat)
+    probe = serving.poisson_requests(args.serve_requests, 1.0, h_lo=100, h_hi=hi)
+    mean_work = sum((r.n + r.nm) * r.horizon for r in probe) / len(probe)
     rate = 0.8 * capacity / mean_work
-    reqs = serving.poisson_requests(args.serve_requests, rate, n_lo=4096, n_hi=131072, h_lo=10, h_hi=60)
-    res = serving.Server(budget_bytes=160 << 30).run(reqs)
+    reqs = serving.poisson_requests(args.serve_requests, rate, h_lo=100, h_hi=hi)
+    live = serving.Server(budget_bytes=160 << 30, frame_every=25)
+    res = live.run(reqs)
     p50, p99 = serving.percentiles(res)
-    one = serving.Server(budget_bytes=max(r.bytes for r in reqs)).run(reqs)
+    # room for one request at a time
+    one = serving.Server(budget_bytes=max(r.bytes for r in reqs), frame_every=25).run(reqs)
     q50, q99 = serving.percentiles(one)
     return {"requests": len(reqs), "arrival_rate_per_s": rate, "p50_latency_s": p50, "p99_latency_s": p99,
             "value": serving.throughput(res, reqs), "unit": UNIT,
+            "frames_streamed": live.frames, "frame_bytes_streamed": live.frame_bytes,
             "one_at_a_time": {"value": serving.throughput(one, reqs), "p50_latency_s": q50, "p99_latency_s": q99},
-            "stream": "Poisson at 80% of the batched capacity; particles log-uniform [4096, 131072], horizon "
-                      "uniform [10, 60] steps, metabolic x2, mix Dirichlet(1,1,1,1), 160 GB budget "
-                      "(scaled down from 10,000 requests of up to 1M particles and 5,000 steps)"}
+            "saturated": {"requests": len(sat), "value": capacity, "unit": UNIT, "seconds": sat_s,
+                          "requests_bytes_total": peak_bytes, "budget_bytes": 160 << 30},
+            "stream": f"particles log-uniform [4096, 1048576], horizon uniform [100, {hi}] steps, metabolic x2, "
+                      f"mix Dirichlet(1,1,1,1), 160 GB budget; latency run Poisson at 80% of the saturated "
+                      f"capacity with a frame streamed every 25 steps (scaled down from 10,000 requests of "
+                      f"horizons up to 5,000 steps)",
+            "timing": "wall clock"}
 
 
 def vesicle_sample(args, native, torch):
@@ -627,8 +649,7 @@ def run_ours(args):
                        "ends when the last frame has landed"}
     sim.close()
     batched = batched_sample(args, native, torch) if args.batch_replicas > 0 and world == 1 else None
-    served = (serving_sample(args, batched["value"] if batched else value)
-              if args.serve_requests > 0 and world == 1 else None)
+    served = serving_sample(args) if args.serve_requests > 0 and world == 1 else None
     vesicle = vesicle_sample(args, native, torch) if args.vesicle_scale > 0 and world == 1 else None
     ref_cuda = reference_cuda_sample(args, native, torch) if args.ref_steps > 0 and world == 1 else None
 
@@ -689,7 +710,11 @@ def main():
     ap.add_argument("--batch-replicas", type=int, default=512,
                     help="replica cells in the batched sample (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=50)
-    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving sample (0: skip it)")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the serving sample's latency runs (0: skip the serving sample)")
+    ap.add_argument("--serve-saturated", type=int, default=240,
+                    help="requests of the serving sample's saturated run (enough that the 160 GB budget binds)")
+    ap.add_argument("--serve-horizon", type=int, default=150, help="longest request horizon (steps)")
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
     ap.add_argument("--vesicle-steps", type=int, default=6)

@@ -203,9 +203,9 @@ typedef struct sc_config {
     int32_t tiles;            /* metabolic sweeps: 0 per-item pair lists, 1 shared-memory tiles */
     int32_t pair_list_limit;  /* -1: pair lists at full capacity; n >= 0: at most n entries per
                                  list (the items beyond take the neighbourhood-scan paths) */
-    int32_t pool_per_item;    /* -1: the metabolic pair pool starts sized by the list capacity;
-                                 n >= 0: it starts at n entries per metabolic item (it grows to
-                                 its demand at the next synchronisation either way) */
+    int32_t pool_per_item;    /* -1: the metabolic pair pool is sized by the scene's demand at
+                                 sc_prepare; n >= 0: it starts at n entries per metabolic item
+                                 (it grows to its demand at the next synchronisation either way) */
     /* complexify extension: 0 the reference's per-item scan (every passing
        rule appends a bond on the scanning item's side); 1 deterministic pair
        claim: every item offers itself to each neighbour that passes a rule's
@@ -329,6 +329,18 @@ int sc_get_counters(sc_sim *sim, sc_counters *out);
 /* The sim's CUDA stream (a cudaStream_t), for callers that order their own
  * work or timing events after the sim's. */
 void *sc_get_stream(sc_sim *sim);
+/* Completion notices (no counterpart in the reference; for loops that
+ * drive many sims at once without polling them).  With a key set (>= 0),
+ * every sc_step call of the sim queues the key once the work it enqueued has
+ * finished on the device; sc_wait_notices blocks until at least one key is
+ * queued or timeout_ms has passed (< 0: no limit, 0: does not wait), takes up
+ * to cap keys in the order they were queued, and returns how many it took.
+ * The queue is shared by every sim of the process. */
+int sc_set_notify(sc_sim *sim, int64_t key);
+int32_t sc_wait_notices(int64_t *keys, int32_t cap, int32_t timeout_ms);
+/* Device memory the sim holds now, in bytes (no counterpart in the
+ * reference; for admission against a memory budget). */
+int sc_device_bytes(const sc_sim *sim, int64_t *bytes);
 /* The frames.dat payload of the current state (reduceParticles on the
  * counters' ranges, zero beyond), into capacity-sized host buffers. */
 int sc_reduce_frame(sc_sim *sim, sc_reduced_particle *particles,

@@ -8,6 +8,8 @@
 #include <algorithm>
 #include <functional>
 #include <map>
+#include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <cmath>
 #include <string>
@@ -243,6 +245,8 @@ struct sc_sim {
     long long launches = 0;
     std::string err;
     std::vector<void *> allocs;
+    std::map<void *, size_t> allocBytes;    // bytes of each allocation in allocs
+    int64_t notifyKey = -1;                 // queued when each sc_step's work finishes (sc_set_notify)
     std::vector<sc_type_info> types;        // host copy of the type table
     uint8_t *staging = nullptr;
     size_t stagingBytes = 0;
@@ -267,24 +271,53 @@ int set_err(sc_sim *s, int code, const std::string &m) {
 #define SC_CK(s, call)                                                                                    \
     do {                                                                                                  \
         cudaError_t e_ = (call);                                                                          \
-        if (e_ != cudaSuccess)                                                                            \
+        if (e_ != cudaSuccess) {                                                                          \
+            cudaGetLastError(); /* reported here: not again by the next launch check */                   \
             return set_err((s), e_ == cudaErrorMemoryAllocation ? SC_E_OOM : SC_E_CUDA,                   \
                            std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+        }                                                                                                 \
     } while (0)
+
+// Initial metabolic pair pool entries per item (the pool grows to demand).
+const int kPoolStart = 12;
 
 // Device memory comes from the device's stream-ordered pool on the sim's
 // stream: creating or destroying a sim does not synchronise the device, so
 // sims can come and go while others run (the request loop relies on it).
+// Completion notices (sc_set_notify / sc_wait_notices): a host function
+// enqueued on a sim's stream after its steps queues the sim's key when the
+// device reaches it; waiters block on a condition variable instead of
+// polling the streams.  The host function calls no CUDA function.
+std::mutex g_noticeMu;
+std::condition_variable g_noticeCv;
+std::deque<int64_t> g_notices;
+
+void CUDART_CB notice_cb(void *arg) {
+    {
+        std::lock_guard<std::mutex> lk(g_noticeMu);
+        g_notices.push_back((int64_t)(intptr_t)arg);
+    }
+    g_noticeCv.notify_all();
+}
+
+// A device allocation the sim no longer owns (freed by the caller).
+void forget_alloc(sc_sim *s, void *p) {
+    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), p));
+    s->allocBytes.erase(p);
+}
+
 template <class T>
 int dalloc(sc_sim *s, T **p, size_t count) {
     size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
     cudaError_t e = cudaMallocAsync((void **)p, bytes, s->st);
     if (e != cudaSuccess) {
         *p = nullptr;
+        cudaGetLastError();  // reported here: not again by the next launch check
         return set_err(s, e == cudaErrorMemoryAllocation ? SC_E_OOM : SC_E_CUDA,
                        "cudaMallocAsync of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
     }
     s->allocs.push_back((void *)*p);
+    s->allocBytes[(void *)*p] = bytes;
     return SC_OK;
 }
 
@@ -309,6 +342,16 @@ ScLaunchCtx ctx(sc_sim *s) {
     c.join[0] = s->join[0];
     c.join[1] = s->join[1];
     return c;
+}
+
+// Entry of a call on a sim: its device current, and the runtime's last-error
+// slot cleared.  That slot is per thread and shared with every other CUDA
+// user in the process; an error left there by someone else's failed call (an
+// allocation refused for lack of room) is not one of this sim's launches, and
+// every call of this library checks its own results as it makes them.
+void enter(const sc_sim *s) {
+    cudaSetDevice(s->device);
+    cudaGetLastError();
 }
 
 int check_launch(sc_sim *s) {
@@ -508,7 +551,7 @@ int ensure_staging(sc_sim *s, size_t bytes) {
     if (s->stagingBytes >= bytes) return SC_OK;
     if (s->staging) {
         cudaFreeAsync(s->staging, s->st);
-        s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->staging));
+        forget_alloc(s, (void *)s->staging);
         s->staging = nullptr;
         s->stagingBytes = 0;
     }
@@ -522,10 +565,23 @@ int ensure_staging(sc_sim *s, size_t bytes) {
 // it goes back to the device's pool (stream-ordered, no synchronisation)
 // after each load, generation and export, which leaves a resident sim
 // 304 bytes per metabolic particle lighter.
+// The frame staging slots (reduced records, two per item set), allocated on
+// the first frame: a sim that never reduces a frame holds none.
+int ensure_frame_slots(sc_sim *s) {
+    ScBuffers &B = s->B;
+    if (B.redP) return SC_OK;
+    const size_t N = (size_t)s->P.N, Nm = (size_t)s->P.Nm;
+    int rc;
+    if ((rc = dalloc(s, &B.redP, N)) || (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.redP2, N)) ||
+        (rc = dalloc(s, &B.redM2, Nm)))
+        return rc;
+    return SC_OK;
+}
+
 void release_staging(sc_sim *s) {
     if (!s->staging) return;
     cudaFreeAsync(s->staging, s->st);
-    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->staging));
+    forget_alloc(s, (void *)s->staging);
     s->staging = nullptr;
     s->stagingBytes = 0;
 }
@@ -800,16 +856,22 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
             return bail(rc);
     }
     const int passes = sc_sort_passes_for(P);
+    // The metabolic pair pool starts at kPoolStart entries per item (the
+    // tiled sweep's 16-bit lists take the full list capacity) and sc_prepare
+    // grows it to the scene's demand: a pool sized for the worst case would
+    // hold most of a sim's memory.
+    const int poolEntryWords = P.metabLean ? 1 : 4;
+    size_t poolWords = sc_list_words(SC_LIST_M, (int)Nm);
+    if (P.tileCapM == 0) poolWords = std::min(poolWords, sc_list_words(kPoolStart * poolEntryWords, (int)Nm));
     if ((rc = dalloc(s, &B.mcLscs, Nm)) || (rc = dalloc(s, &B.mcSpoly, Nm)) || (rc = dalloc(s, &B.mcNb, Nm)) ||
         (rc = dalloc(s, &B.mcBonds, Nm * 24)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
-        (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.redP, N)) ||
-        (rc = dalloc(s, &B.redM, Nm)) || (rc = dalloc(s, &B.redP2, N)) || (rc = dalloc(s, &B.redM2, Nm)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
+        (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
         (rc = dalloc(s, &B.cntPP, N)) ||
         (rc = dalloc(s, &B.classPP, (size_t)SC_RELAX_CLASSES * N)) ||
         (rc = dalloc(s, &B.matchPP, (size_t)SC_MAX_ACTIVE_INTERACTIONS * N)) || (rc = dalloc(s, &B.matchN, N)) ||
-        (rc = dalloc(s, &B.listM, sc_list_words(SC_LIST_M, (int)Nm))) ||
+        (rc = dalloc(s, &B.listM, poolWords)) ||
         (rc = dalloc(s, &B.cntM, Nm)) || (rc = dalloc(s, &B.listLM, sc_list_words(SC_LIST_LM, (int)N))) ||
         (rc = dalloc(s, &B.cntLM, N)) || (rc = dalloc(s, &B.listD, sc_list_words(SC_LIST_DBUF, (int)Nm))) ||
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
@@ -825,8 +887,8 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
         return bail(rc);
     }
     B.invalidateLists();
-    B.poolEntryWords = P.metabLean ? 1 : 4;
-    B.poolCapM = std::min<size_t>(sc_list_words(SC_LIST_M, (int)Nm) / B.poolEntryWords, (size_t)INT_MAX - 1024);
+    B.poolEntryWords = poolEntryWords;
+    B.poolCapM = std::min<size_t>(poolWords / B.poolEntryWords, (size_t)INT_MAX - 1024);
     // pool_per_item = n >= 0 starts the metabolic pair pool at n entries per item
     if (cfg->pool_per_item >= 0)
         B.poolCapM = std::min(B.poolCapM, (size_t)cfg->pool_per_item * (size_t)std::max<int64_t>(Nm, 1));
@@ -843,7 +905,7 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
 
 void sc_destroy(sc_sim *s) {
     if (!s) return;
-    cudaSetDevice(s->device);
+    enter(s);
     if (s->copySt) {
         cudaStreamSynchronize(s->copySt);
         cudaStreamDestroy(s->copySt);
@@ -867,7 +929,7 @@ void sc_destroy(sc_sim *s) {
 int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_metabolic_particle *metabolic,
                   int32_t nm, int32_t step, int32_t next_particle_id) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     const int N = s->P.N, Nm = s->P.Nm;
     if (n < 0 || nm < 0 || n > N || nm > Nm || (n > 0 && !particles) || (nm > 0 && !metabolic))
         return set_err(s, SC_E_INVALID, "state larger than the capacity or missing");
@@ -911,21 +973,32 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     return SC_OK;
 }
 
+static int grow_pools(sc_sim *s);
+
 int sc_prepare(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
-    cudaSetDevice(s->device);
+    enter(s);
     int rc;
     if ((rc = run_phase(s, SC_PHASE_SORT_PARTICLES, 0)) || (rc = run_phase(s, SC_PHASE_SORT_METABOLIC, 0)) ||
         (rc = run_phase(s, SC_PHASE_REMOVE_INTERFERING, 0)) || (rc = run_phase(s, SC_PHASE_COMPLEXIFY, -1)))
         return rc;
-    return SC_OK;
+    // the metabolic pair pool sized for this scene: its list built once,
+    // its demand read back, the pool grown to it (1.25x); a pool whose
+    // starting size the config fixes (pool_per_item >= 0) is left to grow at
+    // the next synchronisation
+    if (s->cfg.pool_per_item >= 0) return SC_OK;
+    ScLaunchCtx c = ctx(s);
+    sc_phase_build_m(c);
+    if ((rc = check_launch(s))) return rc;
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    return grow_pools(s);
 }
 
 int sc_run_phase(sc_sim *s, int32_t phase, int32_t arg) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
-    cudaSetDevice(s->device);
+    enter(s);
     return run_phase(s, phase, arg);
 }
 
@@ -933,12 +1006,35 @@ int sc_step(sc_sim *s, int32_t n_steps) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
     if (n_steps < 0) return set_err(s, SC_E_INVALID, "negative step count");
-    cudaSetDevice(s->device);
+    enter(s);
     for (int k = 0; k < n_steps; k++) {
         int rc = s->useGraphs ? step_graph(s) : step_direct(s);
         if (rc) return rc;
     }
+    if (s->notifyKey >= 0) SC_CK(s, cudaLaunchHostFunc(s->st, notice_cb, (void *)(intptr_t)s->notifyKey));
     return SC_OK;
+}
+
+int sc_set_notify(sc_sim *s, int64_t key) {
+    if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
+    s->notifyKey = key < 0 ? -1 : key;
+    return SC_OK;
+}
+
+int32_t sc_wait_notices(int64_t *keys, int32_t cap, int32_t timeout_ms) {
+    if (!keys || cap < 1) return set_err(nullptr, SC_E_INVALID, "no room for notices");
+    std::unique_lock<std::mutex> lk(g_noticeMu);
+    if (g_notices.empty() && timeout_ms != 0) {
+        auto ready = [] { return !g_notices.empty(); };
+        if (timeout_ms < 0) g_noticeCv.wait(lk, ready);
+        else g_noticeCv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
+    }
+    int32_t n = 0;
+    while (n < cap && !g_notices.empty()) {
+        keys[n++] = g_notices.front();
+        g_notices.pop_front();
+    }
+    return n;
 }
 
 
@@ -962,7 +1058,7 @@ static int grow_pools(sc_sim *s) {
         s->err.clear();
         return SC_OK;
     }
-    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)B.listM));
+    forget_alloc(s, (void *)B.listM);
     SC_CK(s, cudaFreeAsync(B.listM, s->st));
     B.listM = grown;
     B.poolCapM = cap;
@@ -974,7 +1070,7 @@ static int grow_pools(sc_sim *s) {
 
 int sc_sync(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     SC_CK(s, cudaStreamSynchronize(s->st));
     SC_CK(s, cudaStreamSynchronize(s->copySt));
     int derr = 0;
@@ -985,7 +1081,7 @@ int sc_sync(sc_sim *s) {
 
 int sc_pair_counts(sc_sim *s, int64_t out[4]) {
     if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
-    cudaSetDevice(s->device);
+    enter(s);
     const ScBuffers &B = s->B;
     const int *cnt[4] = {B.cntPP, B.cntM, B.cntLM, B.cntD};
     const bool valid[4] = {B.validPP, B.validM, B.validLM, B.validD};
@@ -1007,7 +1103,7 @@ int sc_pair_counts(sc_sim *s, int64_t out[4]) {
 
 int sc_list_overflows(sc_sim *s, int64_t out[4]) {
     if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
-    cudaSetDevice(s->device);
+    enter(s);
     const ScBuffers &B = s->B;
     const int *cnt[4] = {B.cntPP, B.cntM, B.cntLM, B.cntD};
     const bool valid[4] = {B.validPP, B.validM, B.validLM, B.validD};
@@ -1033,7 +1129,7 @@ int sc_list_overflows(sc_sim *s, int64_t out[4]) {
 
 int sc_idle(sc_sim *s) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     for (cudaStream_t st : {s->st, s->copySt}) {
         cudaError_t e = cudaStreamQuery(st);
         if (e == cudaErrorNotReady) return 0;
@@ -1059,9 +1155,17 @@ int sc_get_counters(sc_sim *s, sc_counters *out) {
 
 void *sc_get_stream(sc_sim *s) { return s ? (void *)s->st : nullptr; }
 
+int sc_device_bytes(const sc_sim *s, int64_t *bytes) {
+    if (!s || !bytes) return set_err(nullptr, SC_E_INVALID, "null argument");
+    int64_t t = 0;
+    for (const auto &kv : s->allocBytes) t += (int64_t)kv.second;
+    *bytes = t;
+    return SC_OK;
+}
+
 int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     const int N = s->P.N, Nm = s->P.Nm;
     int rc = ensure_staging(s, std::max<size_t>(
                                    std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
@@ -1117,7 +1221,7 @@ static int set_batch_reps(sc_sim *s, const std::vector<int> &offP, const std::ve
     if (s->P.Nm > 0) k_set_reps<<<nb_of(s->P.Nm), SC_THREADS, 0, s->st>>>(B.m[0].info, s->P.Nm, dOff + R + 1, R);
     SC_CK(s, cudaStreamSynchronize(s->st));
     cudaFreeAsync(dOff, s->st);
-    s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)dOff));
+    forget_alloc(s, (void *)dOff);
     return check_launch(s);
 }
 
@@ -1138,7 +1242,7 @@ int sc_export_replica(sc_sim *s, int32_t r, sc_particle *particles, sc_metabolic
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
     if (r < 0 || r >= (int)s->reps.size()) return set_err(s, SC_E_INVALID, "no such replica");
-    cudaSetDevice(s->device);
+    enter(s);
     const int N = s->P.N, Nm = s->P.Nm;
     int rc = ensure_staging(s, std::max<size_t>(
                                    std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
@@ -1186,7 +1290,7 @@ int sc_export_replica(sc_sim *s, int32_t r, sc_particle *particles, sc_metabolic
 
 int sc_export_grid(sc_sim *s, int32_t which, uint32_t *ranges, uint32_t *perm) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     SC_CK(s, cudaStreamSynchronize(s->st));
     const uint32_t cells = s->P.cells;
     const int cap = which ? s->P.Nm : s->P.N;
@@ -1208,12 +1312,14 @@ int sc_export_grid(sc_sim *s, int32_t which, uint32_t *ranges, uint32_t *perm) {
 
 int sc_reduce_frame(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
+    int rc = ensure_frame_slots(s);
+    if (rc) return rc;
     ScLaunchCtx c = ctx(s);
     // the synchronous form uses slot 0 once the frames in flight have landed
     if (s->frames > 0) SC_CK(s, cudaStreamSynchronize(s->copySt));
     sc_phase_reduce(c, 0);
-    int rc = check_launch(s);
+    rc = check_launch(s);
     if (rc) return rc;
     if (particles && s->P.N > 0)
         SC_CK(s, cudaMemcpyAsync(particles, s->B.redP, (size_t)s->P.N * sizeof(sc_reduced_particle),
@@ -1276,7 +1382,7 @@ static int generate_into(sc_sim *s, int n, int nm, uint64_t seed, const std::fun
 int sc_generate_uniform(sc_sim *s, int32_t n, int32_t nm, const int32_t *kinds, const float *fractions,
                         int32_t nkinds, uint64_t seed) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     if (n < 0 || nm < 0 || n > s->P.N || nm > s->P.Nm) return set_err(s, SC_E_INVALID, "scene larger than the capacity");
     sc_gen_mix mix;
     memset(&mix, 0, sizeof mix);
@@ -1292,7 +1398,7 @@ int sc_generate_batch(sc_sim *s, const int32_t *n, const int32_t *nm, const int3
                       int32_t nkinds, const uint64_t *seeds) {
     if (!s || !n || !nm || !seeds) return set_err(s, SC_E_INVALID, "null argument");
     if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
-    cudaSetDevice(s->device);
+    enter(s);
     const int R = (int)s->reps.size();
     std::vector<int> offP(R + 1, 0), offM(R + 1, 0);
     std::vector<sc_gen_mix> mix((size_t)R);
@@ -1354,7 +1460,7 @@ int sc_generate_batch(sc_sim *s, const int32_t *n, const int32_t *nm, const int3
 
 int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     if (n_groups < 0 || (n_groups > 0 && !groups) || nm < 0 || nm > s->P.Nm)
         return set_err(s, SC_E_INVALID, "bad group list or metabolic count");
     std::vector<sc_gen_group> gg((size_t)std::max(n_groups, 1));
@@ -1377,14 +1483,14 @@ int sc_mark_positions(sc_sim *s) {
     if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
-    cudaSetDevice(s->device);
+    enter(s);
     ScCounters c;
     SC_CK(s, cudaStreamSynchronize(s->st));
     SC_CK(s, cudaMemcpy(&c, s->B.ctr, sizeof c, cudaMemcpyDeviceToHost));
     const int capP = std::max(std::max(s->P.N, c.nextId), 1), capM = std::max(s->P.Nm, 1);
     if (capP > s->markCapP) {
         if (s->markP) {
-            s->allocs.erase(std::find(s->allocs.begin(), s->allocs.end(), (void *)s->markP));
+            forget_alloc(s, (void *)s->markP);
             cudaFreeAsync(s->markP, s->st);
             s->markP = nullptr;
         }
@@ -1410,7 +1516,7 @@ int sc_observe(sc_sim *s, sc_observables *out) {
     if (s && !s->reps.empty()) return set_err(s, SC_E_INVALID, "not available on a batched sim");
     if (!s || !out) return set_err(s, SC_E_INVALID, "null argument");
     if (!s->loaded) return set_err(s, SC_E_STATE, "no state loaded");
-    cudaSetDevice(s->device);
+    enter(s);
     const int cols = sc_observe_cols(), rows = sc_observe_rows();
     if (!s->obs) {
         int rc = dalloc(s, &s->obs, (size_t)(rows + 2) * cols);
@@ -1454,7 +1560,7 @@ int sc_pair_histogram(sc_sim *s, int32_t type_a, int32_t type_b, float r_max, in
     if (n_bins < 1 || n_bins > 4096) return set_err(s, SC_E_INVALID, "n_bins must be in 1..4096");
     if (!(r_max > 0.0f) || r_max > s->cfg.grid_cell_size)
         return set_err(s, SC_E_INVALID, "r_max must be in (0, grid cell size]");
-    cudaSetDevice(s->device);
+    enter(s);
     int rc;
     if (!(s->P.binned & SC_BINNED_P) && (rc = run_phase(s, SC_PHASE_SORT_PARTICLES, 0))) return rc;
     ScBuffers &B = s->B;
@@ -1513,13 +1619,15 @@ int sc_checkpoint_read(sc_sim *s, void *file) {
 
 int64_t sc_reduce_frame_async(sc_sim *s, sc_reduced_particle *particles, sc_reduced_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
-    cudaSetDevice(s->device);
+    enter(s);
     const int slot = (int)(s->frames & 1);
+    int rc = ensure_frame_slots(s);
+    if (rc) return rc;
     // the slot's previous frame must have left the device before it is rewritten
     if (s->frames >= 2) SC_CK(s, cudaStreamWaitEvent(s->st, s->copied[slot], 0));
     ScLaunchCtx c = ctx(s);
     sc_phase_reduce(c, slot);
-    int rc = check_launch(s);
+    rc = check_launch(s);
     if (rc) return rc;
     SC_CK(s, cudaEventRecord(s->reduced[slot], s->st));
     SC_CK(s, cudaStreamWaitEvent(s->copySt, s->reduced[slot], 0));
@@ -1537,7 +1645,7 @@ int64_t sc_reduce_frame_async(sc_sim *s, sc_reduced_particle *particles, sc_redu
 int sc_frame_wait(sc_sim *s, int64_t ticket) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (ticket < 0 || ticket >= s->frames) return set_err(s, SC_E_INVALID, "no such frame");
-    cudaSetDevice(s->device);
+    enter(s);
     // The slot's event records this frame's copy or a later one on the same
     // in-order copy stream; either way this frame has landed when it fires.
     SC_CK(s, cudaEventSynchronize(s->copied[ticket & 1]));

@@ -2570,10 +2570,12 @@ void sc_tile_init() {
 }
 size_t sc_tile_bytes(int capM, int capP, int perSlot) { return SC_TILE_HDR_BYTES + (size_t)(capM + capP) * perSlot; }
 
-void sc_phase_relax_metab(ScLaunchCtx &c) {
+// The metabolic relaxation's pair list (and pool) for the current
+// positions, unless it is already built.
+void sc_phase_build_m(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.Nm <= 0) return;
-    MFields M = B.M(), X = B.Mnext();
+    MFields M = B.M();
     PFields F = B.P();
     const bool tiles = c.P.tileCapM > 0;
     if (!B.validM) {
@@ -2595,6 +2597,15 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
         (*c.launches)++;
         B.validM = true;
     }
+}
+
+void sc_phase_relax_metab(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.Nm <= 0) return;
+    MFields M = B.M(), X = B.Mnext();
+    PFields F = B.P();
+    const bool tiles = c.P.tileCapM > 0;
+    sc_phase_build_m(c);
     PairList<SC_LIST_M> L;
     L.list = B.listM;
     L.cnt = B.cntM;

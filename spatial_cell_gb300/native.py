@@ -42,6 +42,9 @@ _SIGS = {
     "sc_reduce_frame_async": (ctypes.c_int64, [_P, _P, _P]),
     "sc_frame_wait": (ctypes.c_int, [_P, ctypes.c_int64]),
     "sc_get_stream": (ctypes.c_void_p, [_P]),
+    "sc_device_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    "sc_set_notify": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "sc_wait_notices": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32]),
     "sc_generate_uniform": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P, ctypes.c_int32,
                                            ctypes.c_uint64]),
     "sc_generate_scene": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64]),
@@ -128,6 +131,16 @@ def load_rules_json(path):
     out = np.zeros(n.value, abi.RULE_DTYPE)
     _check(lib().sc_rules_load_json(path.encode(), abi.ptr(out), n.value, ctypes.byref(n)), None, "sc_rules_load_json")
     return out
+
+
+def wait_notices(cap=1024, timeout_ms=-1):
+    """Keys of sims whose stepping finished (sc_wait_notices), in order;
+    blocks up to timeout_ms (the GIL is released while it waits)."""
+    buf = (ctypes.c_int64 * cap)()
+    n = lib().sc_wait_notices(buf, cap, timeout_ms)
+    if n < 0:
+        _check(n, None, "sc_wait_notices")
+    return [int(buf[k]) for k in range(n)]
 
 
 def grid(cfg):
@@ -304,6 +317,16 @@ class Simulation:
         perm = np.zeros(max(cap, 1), np.uint32)
         _check(self.L.sc_export_grid(self.h, which, abi.ptr(r), abi.ptr(perm)), self.h, "sc_export_grid")
         return r, perm[:cap]
+
+    def set_notify(self, key):
+        """Queue `key` each time this sim's sc_step work finishes (see wait_notices)."""
+        _check(self.L.sc_set_notify(self.h, key), self.h, "sc_set_notify")
+
+    def device_bytes(self):
+        """Device memory the sim holds now (sc_device_bytes)."""
+        b = ctypes.c_int64(0)
+        _check(self.L.sc_device_bytes(self.h, ctypes.byref(b)), self.h, "sc_device_bytes")
+        return b.value
 
     def stream_handle(self):
         """The sim's cudaStream_t as an integer."""
