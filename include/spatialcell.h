@@ -222,6 +222,14 @@ typedef struct sc_config {
        entry (the neighbour), the term evaluated again in each sub-iteration
        (a quarter of the pool's memory, about twice the sweep's time) */
     int32_t metabolic_pairs;
+    /* 1: after polymerize, each particle takes the state (and its last
+       state-change step) of a bonded partner whose state changed later, over
+       the bonds whose rule sets propagateState -- the reference's
+       propagateState kernel (interactions.cuh:743-822), which its step
+       leaves commented out (main.cu:618-631); 0 (default): the reference's
+       step, without it */
+    int32_t propagate_state;
+    int32_t _reserved;
 } sc_config;
 
 /* Counters of a sim (the reference's nActiveParticles, lastActiveParticle,
@@ -253,7 +261,8 @@ enum sc_phase {
     SC_PHASE_POLYMERIZE = 12,         /* polymerize, interactions.cuh:558-740 */
     SC_PHASE_DIFFUSE = 13,            /* diffuseMetabolites, metabolites.cuh:352-431 */
     SC_PHASE_REMOVE_INTERFERING = 14, /* removeInterferingMetabolicParticles, metabolites.cuh:18-88 */
-    SC_PHASE_END_STEP = 15            /* step counter += 1 */
+    SC_PHASE_END_STEP = 15,           /* step counter += 1 */
+    SC_PHASE_PROPAGATE_STATE = 16     /* propagateState, interactions.cuh:743-822 (sc_config.propagate_state) */
 };
 
 typedef struct sc_sim sc_sim;

@@ -351,6 +351,16 @@ int oref_run_phase(oref_sim *s, int phase, int arg) {
             });
             break;
         }
+        case SC_PHASE_PROPAGATE_STATE: {  // the launch main.cu:618-631 leaves commented out
+            int n = s->nActive;
+            memset(s->pNext, 0, (size_t)s->N * sizeof(Particle));
+            Particle *c = s->pCur, *x = s->pNext;
+            launch(n, [&] {
+                propagateState(step, s->rngP, c, x, n, s->rangesP, s->flatRules, s->partnerIndex, s->partnerRules);
+            });
+            std::swap(s->pCur, s->pNext);
+            break;
+        }
         case SC_PHASE_DIFFUSE: {  // main.cu:637-649
             int nm = s->nActiveM;
             memset(s->mNext, 0, (size_t)s->Nm * sizeof(MetabolicParticle));

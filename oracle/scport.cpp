@@ -949,6 +949,47 @@ void polymerize(scp_sim &s) {
     }
 }
 
+// ---- interactions.cuh:743-822 propagateState ---------------------------------
+// (main.cu:618-631 leaves its launch commented out: it runs here, after
+// polymerize, only with sc_config.propagate_state.)  Each active particle
+// below the post-polymerize count walks its 27 cells in order and, for every
+// active neighbour inside the interaction cube that is the partner of one of
+// its rule bonds (type >= 10) whose rule propagates state, takes the
+// neighbour's state when the neighbour's last state change is later than its
+// own (as updated so far).  Neighbours are read from the state before the pass.
+void propagate_state(scp_sim &s) {
+    const int n = s.nActive;
+    const float lim = s.cfg.max_interaction_distance;
+    const std::vector<PP> &cur = s.p;
+    SC_OMP_FOR
+    for (int i = 0; i < n; i++) {
+        PP p = cur[i];
+        if (p.flags & kActive) {
+            s.scan(s.rangesP, p.pos, [&](int j) {
+                if (j == i) return;
+                const PP &tp = cur[j];
+                if (!(tp.flags & kActive)) return;
+                sc_f3 delta = s.img(tp.pos, p.pos) - p.pos;
+                if (outside_cube(delta, lim)) return;
+                // (a count past the 8 slots, which polymerize can leave, reads
+                // the 8 slots: the reference would read past the array)
+                for (int k = 0; k < std::min(p.nb, SC_MAX_ACTIVE_INTERACTIONS); k++) {
+                    const sc_interaction &it = p.bonds[k];
+                    if (it.type < 10 || it.partner_id != tp.id) continue;
+                    if (!s.rule(it.type).propagate_state) continue;
+                    if (tp.lscs > p.lscs) {
+                        p.lscs = tp.lscs;
+                        p.state = tp.state;
+                    }
+                }
+            });
+        }
+        s.pn[i] = p;
+    }
+    clear_tail(s.pn, n);
+    s.p.swap(s.pn);
+}
+
 // ---- metabolites.cuh:352-431 diffuseMetabolites ------------------------------
 void diffuse(scp_sim &s) {
     const int n = s.nActiveM;
@@ -1250,6 +1291,7 @@ int scp_run_phase(scp_sim *s, int phase, int arg) {
         case SC_PHASE_DIFFUSE: diffuse(*s); break;
         case SC_PHASE_REMOVE_INTERFERING: remove_interfering(*s); break;
         case SC_PHASE_END_STEP: s->step++; break;
+        case SC_PHASE_PROPAGATE_STATE: propagate_state(*s); break;
         default: return SC_E_INVALID;
     }
     return SC_OK;
@@ -1282,6 +1324,7 @@ int scp_step(scp_sim *s, int n_steps) {
         scp_run_phase(s, SC_PHASE_COMPLEXIFY, s->step);
         scp_run_phase(s, SC_PHASE_TRANSITION, 0);
         scp_run_phase(s, SC_PHASE_POLYMERIZE, 0);
+        if (s->cfg.propagate_state) scp_run_phase(s, SC_PHASE_PROPAGATE_STATE, 0);
         for (int j = 0; j < s->cfg.metabolite_diffusion_steps; j++) scp_run_phase(s, SC_PHASE_DIFFUSE, j);
         scp_run_phase(s, SC_PHASE_END_STEP, 0);
     }

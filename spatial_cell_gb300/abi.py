@@ -119,6 +119,7 @@ PHASE_POLYMERIZE = 12
 PHASE_DIFFUSE = 13
 PHASE_REMOVE_INTERFERING = 14
 PHASE_END_STEP = 15
+PHASE_PROPAGATE_STATE = 16
 
 
 class Config(ctypes.Structure):
@@ -153,6 +154,8 @@ class Config(ctypes.Structure):
         ("pair_claim", ctypes.c_int32),
         ("rule_probabilities", ctypes.c_int32),
         ("metabolic_pairs", ctypes.c_int32),
+        ("propagate_state", ctypes.c_int32),
+        ("_reserved", ctypes.c_int32),
     ]
 
     def as_dict(self):
@@ -193,7 +196,7 @@ class Observables(ctypes.Structure):
     ]
 
 
-assert ctypes.sizeof(Config) == 120
+assert ctypes.sizeof(Config) == 128
 assert ctypes.sizeof(Counters) == 32
 assert ctypes.sizeof(Replica) == 24
 
@@ -205,7 +208,7 @@ DEFAULT_CONFIG = dict(num_particles=65536, num_metabolic_particles=65536, steps=
                       relaxation_steps=32, metabolite_diffusion_steps=8, persist_every_nth_frame=1,
                       report_every_nth_frame=10, num_metabolites=10, periodic=0, walls=0, seed=42, graphs=1,
                       class_streams=0, tiles=0, pair_list_limit=-1, pool_per_item=-1, pair_claim=0,
-                      rule_probabilities=0, metabolic_pairs=1)
+                      rule_probabilities=0, metabolic_pairs=1, propagate_state=0)
 
 
 def make_config(**kw):

@@ -55,8 +55,10 @@
                         // membrane ~110)
 #define SC_LIST_LM 48   // lipid <- metabolic collisions
 #define SC_LIST_D 96    // metabolic diffusion partners
-// The diffusion list's buffer is also the metabolic list's build scratch.
-#define SC_LIST_DBUF (SC_LIST_M > SC_LIST_D ? SC_LIST_M : SC_LIST_D)
+// The diffusion list's buffer holds the count-ordered diffusion list and,
+// after it, the diffusion list's build scratch; the whole buffer is also the
+// build scratch of the metabolic list (whose pool is sized by demand).
+#define SC_LIST_DBUF (SC_LIST_M > 2 * SC_LIST_D ? SC_LIST_M : 2 * SC_LIST_D)
 #define SC_PP_POLAR 0x80000000u
 #define SC_PP_PARTNER 0x40000000u
 #define SC_PP_COLLIDE 0x20000000u
@@ -79,7 +81,9 @@ struct ScCounters {
     int nextId;       // nextParticleId (main.cu:246)
     int nActiveM;     // nActiveMetabolicParticles (main.cu:253)
     int error;        // first device-side error code
-    int polyCount;    // scheduled polymerisations collected this step
+    int polyCount;    // scheduled polymerisations listed this step (k_poly_offsets)
+    int polyCreates;  // of those, the ones whose rule creates a monomer
+    int polyConflict; // 1: two listed items touch the same particle (k_poly_plan)
     int step;         // the step loop counter (main.cu:347)
     int tileCounter[4];
     int ppClassCount[4];  // items per relax work class (k_build_pp)

@@ -111,6 +111,7 @@ extern "C" void sc_config_defaults(sc_config *c) {
     c->pair_claim = 0;
     c->rule_probabilities = 0;
     c->metabolic_pairs = 1;
+    c->propagate_state = 0;
 }
 
 extern "C" int sc_config_load_json(const char *path, sc_config *c) {
@@ -143,6 +144,7 @@ extern "C" int sc_config_load_json(const char *path, sc_config *c) {
     I("walls", &c->walls);
     I("pairClaim", &c->pair_claim);
     I("ruleProbabilities", &c->rule_probabilities);
+    I("propagateState", &c->propagate_state);
     if (const scjson::Value *m = v.find("seed")) c->seed = (uint64_t)(m->type == scjson::Value::Int ? m->i : (long long)m->as_double());
     return SC_OK;
 }

@@ -60,8 +60,11 @@ struct ScBuffers {
     bool validPP, validM, validLM, validD;
     void invalidateLists() { validPP = validM = validLM = validD = false; }
     // polymerisation list
-    int *polyList;
-    int polyCap;
+    // polymerize: the scheduled items in index order, per slot the rank of
+    // its new monomer and its previous monomer, per item a claim count, per
+    // block of items its two counts and their offsets
+    int *polyList, *polyRank, *polyPmi, *polyClaim;
+    int2 *polyBlk;
     ScCounters *ctr;
     // frames
     sc_reduced_particle *redP, *redP2;                // frame staging, two slots
@@ -162,6 +165,7 @@ void sc_phase_apply_velocities(ScLaunchCtx &c);
 void sc_phase_complexify(ScLaunchCtx &c, bool prep);
 void sc_phase_transition(ScLaunchCtx &c);
 void sc_phase_polymerize(ScLaunchCtx &c);
+void sc_phase_propagate_state(ScLaunchCtx &c);
 void sc_phase_diffuse(ScLaunchCtx &c);
 void sc_phase_remove_interfering(ScLaunchCtx &c);
 void sc_phase_reduce(ScLaunchCtx &c, int slot);

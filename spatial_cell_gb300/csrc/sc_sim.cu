@@ -457,6 +457,7 @@ int run_phase(sc_sim *s, int phase, int arg) {
         case SC_PHASE_COMPLEXIFY: sc_phase_complexify(c, arg == -1); break;
         case SC_PHASE_TRANSITION: sc_phase_transition(c); break;
         case SC_PHASE_POLYMERIZE: sc_phase_polymerize(c); break;
+        case SC_PHASE_PROPAGATE_STATE: sc_phase_propagate_state(c); break;
         case SC_PHASE_DIFFUSE: sc_phase_diffuse(c); break;
         case SC_PHASE_REMOVE_INTERFERING: sc_phase_remove_interfering(c); break;
         case SC_PHASE_END_STEP:
@@ -489,6 +490,7 @@ int step_direct(sc_sim *s) {
         run_phase(s, SC_PHASE_COMPLEXIFY, 0);
         run_phase(s, SC_PHASE_TRANSITION, 0);
         run_phase(s, SC_PHASE_POLYMERIZE, 0);
+        if (c.propagate_state) run_phase(s, SC_PHASE_PROPAGATE_STATE, 0);
         for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
         return run_phase(s, SC_PHASE_END_STEP, 0);
     }
@@ -867,7 +869,8 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
         (rc = dalloc(s, &B.mcBonds, Nm * 24)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
-        (rc = dalloc(s, &B.polyList, 4096)) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
+        (rc = dalloc(s, &B.polyList, N)) || (rc = dalloc(s, &B.polyRank, N)) || (rc = dalloc(s, &B.polyPmi, N)) ||
+        (rc = dalloc(s, &B.polyClaim, N)) || (rc = dalloc(s, &B.polyBlk, 2 * ((size_t)N / SC_THREADS + 1))) || (rc = dalloc(s, &B.ctr, 1)) || (rc = dalloc(s, &B.listPP, sc_list_words(SC_LIST_PP, (int)N))) ||
         (rc = dalloc(s, &B.cntPP, N)) ||
         (rc = dalloc(s, &B.classPP, (size_t)SC_RELAX_CLASSES * N)) ||
         (rc = dalloc(s, &B.matchPP, (size_t)SC_MAX_ACTIVE_INTERACTIONS * N)) || (rc = dalloc(s, &B.matchN, N)) ||
@@ -892,9 +895,9 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
     // pool_per_item = n >= 0 starts the metabolic pair pool at n entries per item
     if (cfg->pool_per_item >= 0)
         B.poolCapM = std::min(B.poolCapM, (size_t)cfg->pool_per_item * (size_t)std::max<int64_t>(Nm, 1));
-    B.polyCap = 4096;
     P.lipidP = B.lipidP;
     cudaMemsetAsync(B.ctr, 0, sizeof(ScCounters), s->st);
+    cudaMemsetAsync(B.polyClaim, 0, std::max<size_t>(N, 1) * sizeof(int), s->st);
     cudaMemsetAsync(B.cellStartP, 0, ((size_t)P.cells + 1) * 4, s->st);
     cudaMemsetAsync(B.cellStartM, 0, ((size_t)P.cells + 1) * 4, s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);

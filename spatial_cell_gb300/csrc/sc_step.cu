@@ -2073,40 +2073,74 @@ __global__ void __launch_bounds__(SC_THREADS) k_transition(
 // ---- interactions.cuh:558-740 polymerize --------------------------------------
 // The reference runs it in place with atomicAdd slot / id allocation and
 // cross-slot writes, so its outcome depends on thread scheduling.  Here the
-// scheduled items are collected and one thread performs them in slot order,
-// which is the order a one-thread-at-a-time execution of the reference gives.
-__global__ void __launch_bounds__(SC_THREADS) k_poly_collect(const int *__restrict__ nActivePtr,
-                                                             const int4 *__restrict__ info,
-                                                             const int *__restrict__ spoly, int *list, int cap,
-                                                             ScCounters *ctr) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nActivePtr) return;
-    if (!(info[i].z & SC_ACTIVE) || spoly[i] < 0) return;
-    int k = atomicAdd(&ctr->polyCount, 1);
-    if (k < cap) list[k] = i;
+// outcome is the one a one-item-at-a-time execution in slot (index) order
+// gives, computed in parallel:
+//  * k_poly_count / k_poly_offsets / k_poly_plan list the scheduled items in
+//    index order (an ordered compaction), with the rank of each one's new
+//    monomer among the items whose rule creates one: in slot order the k-th
+//    creating item takes index lastActive + 1 + k and id nextId + k (when
+//    the index is below the capacity), so neither needs a serial counter;
+//  * an item's processing reads and writes its own bonds and those of its
+//    previous monomer (pmi, found by id among the binned particles, whose
+//    ids no processing changes) and writes its new monomer's slot.  When no
+//    listed item's previous monomer is itself listed or shared with another
+//    item, the footprints are disjoint and every item runs at once
+//    (k_poly_apply); otherwise one thread runs them all in slot order
+//    (k_poly_finish), as before.
+__device__ __forceinline__ bool poly_scheduled(const PFields &F, int n0, int i) {
+    return i < n0 && (F.info[i].z & SC_ACTIVE) && F.spoly[i] >= 0;
+}
+__device__ __forceinline__ bool poly_creates(const ScParams &P, const PFields &F, int i) {
+    const sc_rule &poly = rule_at(P, F.spoly[i]);
+    const bool first = poly.first_partner_type == F.info[i].y;
+    return (first ? poly.second_partner_type : poly.first_partner_type) >= 0;
+}
+// First bond of the rule's group (the active polymerisation bond), -1 if none.
+__device__ __forceinline__ int poly_api(const sc_rule &poly, const int *pb, int pnb) {
+    for (int k = 0; k < pnb; k++)
+        if (pb[3 * k + 1] == poly.group) return k;
+    return -1;
+}
+// The binned particle whose id is `target` (the last one in scan order).
+__device__ __forceinline__ int poly_find(const ScParams &P, const uint32_t *cellStart, const PFields &F, int i,
+                                         int target) {
+    float4 p4 = F.pos[i];
+    int pmi = -1;
+    scan27(P, cellStart, sc_make_f3(p4.x, p4.y, p4.z), [&](int j) {
+        if (j == i) return;
+        int4 tin = F.info[j];
+        if (!(tin.z & SC_ACTIVE)) return;
+        if (tin.x == target) pmi = j;
+    });
+    return pmi;
 }
 
-__device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFields &F, ScCounters *ctr, int i,
-                         int step) {
+// Removes the first bond of `group` from item m's bonds (shifting the rest).
+__device__ __forceinline__ int poly_drop_group(int *mb, int mnb, int group) {
+    for (int k = 0; k < mnb; k++) {
+        if (mb[3 * k + 1] == group) {
+            for (int l = k; l < mnb - 1; l++) {
+                mb[3 * l] = mb[3 * l + 3]; mb[3 * l + 1] = mb[3 * l + 4]; mb[3 * l + 2] = mb[3 * l + 5];
+            }
+            return mnb - 1;
+        }
+    }
+    return mnb;
+}
+
+// One scheduled item: `pmi` its previous monomer (-2: find it now), its new
+// monomer at newIdx with id newId (used when newIdx < N).
+__device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFields &F, int i, int step, int pmi,
+                         int newIdx, int newId) {
     int4 in = F.info[i];
     const sc_rule &poly = rule_at(P, F.spoly[i]);
     const int pid = in.x, ptype = in.y;
     int *pb = F.bonds + (size_t)i * 24;
     int pnb = min(max(F.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
-    int api = -1, pmi = -1;
-    for (int k = 0; k < pnb; k++)
-        if (pb[3 * k + 1] == poly.group) { api = k; break; }
+    const int api = poly_api(poly, pb, pnb);
+    if (pmi == -2) pmi = api >= 0 ? poly_find(P, cellStart, F, i, pb[3 * api + 2]) : -1;
     float4 p4 = F.pos[i];
     const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
-    if (api >= 0) {
-        int target = pb[3 * api + 2];
-        scan27(P, cellStart, ppos, [&](int j) {
-            if (j == i) return;
-            int4 tin = F.info[j];
-            if (!(tin.z & SC_ACTIVE)) return;
-            if (tin.x == target) pmi = j;
-        });
-    }
     const bool first = poly.first_partner_type == ptype;
     const int newType = first ? poly.second_partner_type : poly.first_partner_type;
     const int newState = first ? poly.second_partner_state : poly.first_partner_state;
@@ -2115,9 +2149,7 @@ __device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFi
         float nr = 0.0f;
         int nh = 0;
         if (newType < P.nTypes) { nr = P.types[newType].radius; nh = P.types[newType].hydrophobic; }
-        int newIdx = ++ctr->lastActive;
         if (newIdx < P.N) {
-            int newId = ctr->nextId++;
             sc_f3 rp = rule_pos(poly);
             sc_f4 ro = rule_ori(poly);
             sc_f4 prot = ld4(F.rot, i);
@@ -2142,16 +2174,7 @@ __device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFi
             nnb = 1;
             if (pmi >= 0) {
                 int *mb = F.bonds + (size_t)pmi * 24;
-                int mnb = min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS);
-                for (int k = 0; k < mnb; k++) {
-                    if (mb[3 * k + 1] == poly.group) {
-                        for (int l = k; l < mnb - 1; l++) {
-                            mb[3 * l] = mb[3 * l + 3]; mb[3 * l + 1] = mb[3 * l + 4]; mb[3 * l + 2] = mb[3 * l + 5];
-                        }
-                        mnb--;
-                        break;
-                    }
-                }
+                int mnb = poly_drop_group(mb, min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS), poly.group);
                 if (mnb < SC_MAX_ACTIVE_INTERACTIONS) {
                     mb[3 * mnb] = SC_INTERACTION_TYPE_CHAIN; mb[3 * mnb + 1] = SC_INTERACTION_GROUP_FORWARD;
                     mb[3 * mnb + 2] = newId;
@@ -2170,24 +2193,13 @@ __device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFi
             }
             for (int k = 3 * nnb; k < 24; k++) nbp[k] = 0;
             F.nb[newIdx] = nnb;
-            ctr->nActive++;
         }
     } else {
         // End of the chain; the reference's out-of-bounds stores without a
         // previous monomer / active bond (interactions.cuh:728, 731-734) are skipped.
         if (pmi >= 0) {
             int *mb = F.bonds + (size_t)pmi * 24;
-            int mnb = min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS);
-            for (int k = 0; k < mnb; k++) {
-                if (mb[3 * k + 1] == poly.group) {
-                    for (int l = k; l < mnb - 1; l++) {
-                        mb[3 * l] = mb[3 * l + 3]; mb[3 * l + 1] = mb[3 * l + 4]; mb[3 * l + 2] = mb[3 * l + 5];
-                    }
-                    mnb--;
-                    break;
-                }
-            }
-            F.nb[pmi] = mnb;
+            F.nb[pmi] = poly_drop_group(mb, min(max(F.nb[pmi], 0), SC_MAX_ACTIVE_INTERACTIONS), poly.group);
         }
         if (api >= 0) {
             for (int l = api; l < pnb - 1; l++) {
@@ -2200,44 +2212,184 @@ __device__ void poly_one(const ScParams &P, const uint32_t *cellStart, const PFi
     F.spoly[i] = -1;
 }
 
-// One CTA: sorts the collected slots (odd-even transposition in shared
-// memory), then thread 0 performs them in slot order.  If more were scheduled
-// than the list holds, the CTA walks all slots in order instead.
-#define SC_POLY_LIST_CAP 4096
-__global__ void __launch_bounds__(1024) k_polymerize(ScParams P, const uint32_t *__restrict__ cellStart, PFields F,
-                                                     ScCounters *ctr, const int *list) {
-    const int step = ctr->step;
-    __shared__ int s[SC_POLY_LIST_CAP];
-    __shared__ int s_n0;
+// Per block of SC_THREADS items: (scheduled, creating) counts.
+__global__ void __launch_bounds__(SC_THREADS) k_poly_count(ScParams P, PFields F, const ScCounters *ctr,
+                                                           int2 *blk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n0 = ctr->nActive;
+    const bool s = poly_scheduled(F, n0, i);
+    const bool c = s && poly_creates(P, F, i);
+    const int ns = __syncthreads_count(s), nc = __syncthreads_count(c);
+    if (threadIdx.x == 0) blk[blockIdx.x] = make_int2(ns, nc);
+}
+
+// Exclusive offsets of the block counts (one CTA), the totals, and the
+// conflict flag cleared.
+#define SC_POLY_SCAN_THREADS 1024
+__global__ void __launch_bounds__(SC_POLY_SCAN_THREADS) k_poly_offsets(const int2 *__restrict__ blk, int2 *off,
+                                                                       int nblk, ScCounters *ctr) {
+    __shared__ int2 s_w[SC_POLY_SCAN_THREADS / 32];
+    __shared__ int2 s_carry;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) s_carry = make_int2(0, 0);
+    __syncthreads();
+    for (int b0 = 0; b0 < nblk; b0 += SC_POLY_SCAN_THREADS) {
+        const int b = b0 + t;
+        const int2 v = b < nblk ? blk[b] : make_int2(0, 0);
+        int2 x = v;  // inclusive warp scan
+        for (int d = 1; d < 32; d *= 2) {
+            const int ax = __shfl_up_sync(0xffffffffu, x.x, d), ay = __shfl_up_sync(0xffffffffu, x.y, d);
+            if (lane >= d) { x.x += ax; x.y += ay; }
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int2 w = s_w[lane];
+            for (int d = 1; d < 32; d *= 2) {
+                const int ax = __shfl_up_sync(0xffffffffu, w.x, d), ay = __shfl_up_sync(0xffffffffu, w.y, d);
+                if (lane >= d) { w.x += ax; w.y += ay; }
+            }
+            s_w[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const int2 before = warp ? s_w[warp - 1] : make_int2(0, 0);
+        const int2 carry = s_carry;
+        if (b < nblk) off[b] = make_int2(carry.x + before.x + x.x - v.x, carry.y + before.y + x.y - v.y);
+        __syncthreads();
+        if (t == 0) s_carry = make_int2(carry.x + s_w[31].x, carry.y + s_w[31].y);
+        __syncthreads();
+    }
+    if (t == 0) {
+        ctr->polyCount = s_carry.x;
+        ctr->polyCreates = s_carry.y;
+        ctr->polyConflict = 0;
+    }
+}
+
+// Lists the scheduled items in index order with their monomer ranks, finds
+// each one's previous monomer, and flags a conflict when a previous monomer
+// is itself scheduled or claimed by two items.
+__global__ void __launch_bounds__(SC_THREADS) k_poly_plan(ScParams P, const uint32_t *__restrict__ cellStart, PFields F,
+                                                          ScCounters *ctr, const int2 *__restrict__ off, int *list,
+                                                          int *rank, int *pmiOut, int *claim) {
+    __shared__ int2 s_w[SC_THREADS / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int n0 = ctr->nActive;
+    const bool s = poly_scheduled(F, n0, i);
+    const bool c = s && poly_creates(P, F, i);
+    const unsigned bs = __ballot_sync(0xffffffffu, s), bc = __ballot_sync(0xffffffffu, c);
+    const unsigned below = (1u << lane) - 1u;
+    if (lane == 0) s_w[warp] = make_int2(__popc(bs), __popc(bc));
+    __syncthreads();
+    if (!s) return;
+    int2 o = off[blockIdx.x];
+    for (int w = 0; w < warp; w++) { o.x += s_w[w].x; o.y += s_w[w].y; }
+    const int slot = o.x + __popc(bs & below);
+    list[slot] = i;
+    rank[slot] = c ? o.y + __popc(bc & below) : -1;
+    const sc_rule &poly = rule_at(P, F.spoly[i]);
+    const int *pb = F.bonds + (size_t)i * 24;
+    const int api = poly_api(poly, pb, min(max(F.nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS));
+    const int pmi = api >= 0 ? poly_find(P, cellStart, F, i, pb[3 * api + 2]) : -1;
+    pmiOut[slot] = pmi;
+    if (pmi >= 0 && (poly_scheduled(F, n0, pmi) || atomicAdd(&claim[pmi], 1) != 0)) ctr->polyConflict = 1;
+}
+
+// Without a conflict every listed item runs at once; either way the claims
+// are cleared for the next step.
+__global__ void __launch_bounds__(SC_THREADS) k_poly_apply(ScParams P, const uint32_t *__restrict__ cellStart, PFields F,
+                                                           const ScCounters *ctr, const int *__restrict__ list,
+                                                           const int *__restrict__ rank, const int *__restrict__ pmiIn,
+                                                           int *claim) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= ctr->polyCount) return;
+    const int pmi = pmiIn[slot];
+    if (pmi >= 0) claim[pmi] = 0;
+    if (ctr->polyConflict) return;
+    const int r = rank[slot];
+    poly_one(P, cellStart, F, list[slot], ctr->step, pmi, r >= 0 ? ctr->lastActive + 1 + r : P.N,
+             r >= 0 ? ctr->nextId + r : -1);
+}
+
+// The serial path of a conflicting list, then the counters: lastActive
+// advances by every creating item (the reference increments it before its
+// capacity test), nextId and nActive by those that fit.
+__global__ void k_poly_finish(ScParams P, const uint32_t *__restrict__ cellStart, PFields F, ScCounters *ctr,
+                              const int *__restrict__ list, const int *__restrict__ rank) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int count = ctr->polyCount;
     if (count == 0) return;
-    if (threadIdx.x == 0) s_n0 = ctr->nActive;
-    __syncthreads();
-    const int n0 = s_n0;
-    if (count <= SC_POLY_LIST_CAP) {
-        for (int k = threadIdx.x; k < count; k += blockDim.x) s[k] = list[k];
-        __syncthreads();
-        for (int phase = 0; phase < count; phase++) {
-            for (int k = 2 * threadIdx.x + (phase & 1); k + 1 < count; k += 2 * blockDim.x) {
-                int a = s[k], b = s[k + 1];
-                if (a > b) { s[k] = b; s[k + 1] = a; }
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < count; k++) {
-                int i = s[k];
-                if (i < n0 && (F.info[i].z & SC_ACTIVE) && F.spoly[i] >= 0) poly_one(P, cellStart, F, ctr, i, step);
-            }
-        }
-    } else {
-        if (threadIdx.x == 0) {
-            for (int i = 0; i < n0; i++)
-                if ((F.info[i].z & SC_ACTIVE) && F.spoly[i] >= 0) poly_one(P, cellStart, F, ctr, i, step);
+    const int last0 = ctr->lastActive, next0 = ctr->nextId;
+    if (ctr->polyConflict) {
+        for (int k = 0; k < count; k++) {
+            const int r = rank[k];
+            poly_one(P, cellStart, F, list[k], ctr->step, -2, r >= 0 ? last0 + 1 + r : P.N, r >= 0 ? next0 + r : -1);
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) ctr->polyCount = 0;
+    const int R = ctr->polyCreates;
+    const int made = max(0, min(R, P.N - 1 - last0));
+    ctr->lastActive = last0 + R;
+    ctr->nextId = next0 + made;
+    ctr->nActive += made;
+    ctr->polyCount = 0;
+}
+
+// ---- interactions.cuh:743-822 propagateState (sc_config.propagate_state) -----
+// The reference's kernel, whose launch its step leaves commented out
+// (main.cu:618-631); it runs after polymerize when the config asks for it.
+// Each active particle below the count after polymerize walks its 27 cells in
+// order and, for every active neighbour inside the interaction cube that is
+// the partner of one of its rule bonds (type >= 10) whose rule sets
+// propagateState, takes the neighbour's state and last state-change step when
+// that step is later than its own as updated so far.  Neighbours are read
+// from the state before the pass (state and lscs are double-buffered).  A
+// particle without such a bond keeps its state and scans nothing.
+template <bool BATCH>
+__global__ void __launch_bounds__(SC_THREADS) k_propagate_state(
+    ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ nActivePtr,
+    const float4 *__restrict__ pos, const int4 *__restrict__ info, const int *__restrict__ stateIn,
+    int *__restrict__ stateOut, const int *__restrict__ lscsIn, int *__restrict__ lscsOut, const int *__restrict__ nb,
+    const int *__restrict__ bonds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nActivePtr) return;
+    const int4 in = info[i];
+    int st = stateIn[i], ls = lscsIn[i];
+    const int pnb = min(max(nb[i], 0), SC_MAX_ACTIVE_INTERACTIONS);
+    int partner[SC_MAX_ACTIVE_INTERACTIONS];
+    unsigned prop = 0u;  // bit k: bond k propagates
+#pragma unroll
+    for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+        const int t = k < pnb ? bonds[(size_t)i * 24 + 3 * k] : 0;
+        partner[k] = k < pnb ? bonds[(size_t)i * 24 + 3 * k + 2] : 0;
+        if (k < pnb && t >= 10 && rule_at(P, t).propagate_state) prop |= 1u << k;
+    }
+    if ((in.z & SC_ACTIVE) && prop) {
+        rep_apply<BATCH>(P, in.w);
+        const float4 p4 = pos[i];
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_P);
+        scan27(P, cellStart, pp, [&](int j) {
+            if (j == i) return;
+            const int4 tin = info[j];
+            if (!(tin.z & SC_ACTIVE)) return;
+            const float4 t4 = pos[j];
+            const sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, P.maxInt)) return;
+#pragma unroll
+            for (int k = 0; k < SC_MAX_ACTIVE_INTERACTIONS; k++) {
+                if (((prop >> k) & 1u) && partner[k] == tin.x) {
+                    const int tl = lscsIn[j];
+                    if (tl > ls) {
+                        ls = tl;
+                        st = stateIn[j];
+                    }
+                }
+            }
+        });
+    }
+    stateOut[i] = st;
+    lscsOut[i] = ls;
 }
 
 // ---- metabolites.cuh:352-431 diffuseMetabolites ------------------------------
@@ -2716,10 +2868,26 @@ void sc_phase_polymerize(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     PFields F = B.P();
-    k_poly_collect<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(&B.ctr->nActive, F.info, F.spoly, B.polyList, B.polyCap,
-                                                             B.ctr);
-    k_polymerize<<<1, 1024, 0, c.st>>>(c.P, B.cellStartP, F, B.ctr, B.polyList);
-    (*c.launches) += 2;
+    const int nb = nblocks(c.P.N);
+    k_poly_count<<<nb, SC_THREADS, 0, c.st>>>(c.P, F, B.ctr, B.polyBlk);
+    k_poly_offsets<<<1, SC_POLY_SCAN_THREADS, 0, c.st>>>(B.polyBlk, B.polyBlk + nb, nb, B.ctr);
+    k_poly_plan<<<nb, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, F, B.ctr, B.polyBlk + nb, B.polyList, B.polyRank,
+                                             B.polyPmi, B.polyClaim);
+    k_poly_apply<<<nb, SC_THREADS, 0, c.st>>>(c.P, B.cellStartP, F, B.ctr, B.polyList, B.polyRank, B.polyPmi,
+                                              B.polyClaim);
+    k_poly_finish<<<1, 32, 0, c.st>>>(c.P, B.cellStartP, F, B.ctr, B.polyList, B.polyRank);
+    (*c.launches) += 5;
+}
+
+void sc_phase_propagate_state(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    PFields F = B.P(), X = B.Pnext();
+    SC_BATCHED(k_propagate_state)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
+        c.P, B.cellStartP, &B.ctr->nActive, F.pos, F.info, F.state, X.state, F.lscs, X.lscs, F.nb, F.bonds);
+    B.cp[FP_STATE] ^= 1;
+    B.cp[FP_LSCS] ^= 1;
+    (*c.launches)++;
 }
 
 void sc_phase_diffuse(ScLaunchCtx &c) {
@@ -2727,10 +2895,10 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     if (c.P.Nm <= 0) return;
     MFields M = B.M(), X = B.Mnext();
     if (!B.validD) {
-        // the metabolic relaxation list's buffer is the build scratch
-        B.validM = false;
+        // the build scratch follows the list in the same buffer
         SC_BATCHED(k_build_d)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                             B.listD, B.listM, B.cntD, B.permD, c.P.Nm);
+                                                             B.listD, B.listD + sc_list_words(SC_LIST_D, c.P.Nm),
+                                                             B.cntD, B.permD, c.P.Nm);
         (*c.launches)++;
         B.validD = true;
     }

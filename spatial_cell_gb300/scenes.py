@@ -382,6 +382,93 @@ def test_scene(seed, n=1500, nm=3000, box=48.0, species=10, capacity_slack=64, p
     return cfg, types, rules, p, m, n
 
 
+def polymer_scene(seed, pairs, scheduled_monomers=0, shared=0, capacity_slack=None, box=None):
+    """Controllers, each bonded (rule 1022, group 1020, both directions) to a
+    monomer 1.5-3 nm away and scheduled to polymerise by rule 1022, which
+    creates a new monomer.  `scheduled_monomers` monomers are scheduled too
+    (their previous monomer -- the controller -- is then itself scheduled);
+    `shared` monomers are bonded to a second controller as well (two
+    scheduled items share a previous monomer).  Capacity: the particles plus
+    `capacity_slack` (default: room for every new monomer).  Returns
+    (config, types, rules, particles, metabolic, next_particle_id)."""
+    rng = np.random.default_rng(seed)
+    types, rules = test_types(), test_rules()
+    n = 2 * pairs
+    box = float(box or 3.0 * (n ** (1.0 / 3.0)) + 12.0)
+    p = blank_particles(n)
+    p["id"] = np.arange(n, dtype=np.int32)
+    ctrl, mono = np.arange(0, n, 2), np.arange(1, n, 2)
+    p["type"][ctrl], p["type"][mono] = CTRL, MONO
+    p["radius"] = types["radius"][p["type"]]
+    p["rot"] = random_quaternions(rng, n)
+    p["pos"][ctrl] = (rng.random((pairs, 3)) * (box - 8.0) + 4.0).astype(np.float32)
+    off = rng.normal(size=(pairs, 3))
+    off *= (rng.uniform(1.5, 3.0, pairs) / np.linalg.norm(off, axis=1))[:, None]
+    p["pos"][mono] = (p["pos"][ctrl] + off).astype(np.float32)
+    for c, m in zip(ctrl, mono):
+        p[c]["interactions"][0] = (1022, 1020, p[m]["id"])
+        p[m]["interactions"][0] = (1022, 1020, p[c]["id"])
+    p["n_active_interactions"] = 1
+    p["scheduled_polymerization"] = -1
+    p["scheduled_polymerization"][ctrl] = 1022
+    if scheduled_monomers:
+        p["scheduled_polymerization"][rng.choice(mono, scheduled_monomers, replace=False)] = 1022
+    if shared:
+        # controller k + 1 also bonds controller k's monomer, placed between them
+        for k in rng.choice(pairs - 1, shared, replace=False):
+            c2, m = ctrl[k + 1], mono[k]
+            p[c2]["pos"] = p[m]["pos"] + np.float32(1.0)
+            p[c2]["interactions"][0] = (1022, 1020, p[m]["id"])
+            j = p[m]["n_active_interactions"]
+            if j < abi.MAX_ACTIVE_INTERACTIONS:
+                p[m]["interactions"][j] = (1022, 1020, p[c2]["id"])
+                p[m]["n_active_interactions"] = j + 1
+    p["pos"] = p["pos"].clip(0, box)
+    slack = pairs + scheduled_monomers + 16 if capacity_slack is None else capacity_slack
+    m = uniform_metabolic(rng, 64, box, types, 8)
+    cfg = abi.make_config(num_particles=n + slack, num_metabolic_particles=64, sim_size=box, grid_cell_size=6.0,
+                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8,
+                          seed=2000 + seed, noise_coordination_steps=4, relaxation_steps=6,
+                          metabolite_diffusion_steps=3, steps=10)
+    return cfg, types, rules, p, m, n
+
+
+def propagation_scene(seed, chains=300, length=6, n_free=600):
+    """Chains of particles bonded to their neighbours by rule bonds -- rule
+    1001 (which propagates state) on even chains, rule 1010 (which does not)
+    on odd ones -- with random states and last state-change steps, among free
+    particles, in a box the chains fill; config with propagate_state on.
+    Returns (config, types, rules, particles, metabolic, next_particle_id)."""
+    rng = np.random.default_rng(seed)
+    types, rules = test_types(), test_rules()
+    rules["propagate_state"] = 0
+    rules["propagate_state"][rules["id"] == 1001] = 1
+    n = chains * length + n_free
+    box = float(2.2 * n ** (1.0 / 3.0) + 10.0)
+    p = blank_particles(n)
+    p["id"] = np.arange(n, dtype=np.int32)
+    p["type"] = rng.choice([TYPE_A, TYPE_B, DUMMY], size=n)
+    p["radius"] = types["radius"][p["type"]]
+    p["rot"] = random_quaternions(rng, n)
+    p["pos"] = (rng.random((n, 3)) * (box - 10.0) + 5.0).astype(np.float32)
+    for c in range(chains):
+        s0 = c * length
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        for k in range(length):
+            p[s0 + k]["pos"] = (p[s0]["pos"] + d * 1.8 * k).astype(np.float32)
+        _link_serially(p, s0, s0 + length, itype=1001 if c % 2 == 0 else 1010)
+    p["pos"] = p["pos"].clip(0, box)
+    p["state"] = rng.integers(0, 4, n)
+    p["last_state_change_step"] = rng.integers(-1, 60, n)
+    m = uniform_metabolic(rng, 256, box, types, 8)
+    cfg = abi.make_config(num_particles=n + 32, num_metabolic_particles=256 + 16, sim_size=box, grid_cell_size=6.0,
+                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8,
+                          seed=3000 + seed, noise_coordination_steps=4, relaxation_steps=6,
+                          metabolite_diffusion_steps=3, steps=10, propagate_state=1)
+    return cfg, types, rules, p, m, n
+
+
 def batch_of(replica_states):
     """The batched-sim form of replica cells (as batch_replicas gives them):
     the shared config (replica 0's; the others differ only in capacities,

@@ -63,6 +63,8 @@ def step_phases(cfg):
             ph += [(abi.PHASE_RELAX_METAB, j), (abi.PHASE_RELAX_PARTNERS, j)]
     ph += [(abi.PHASE_APPLY_VELOCITIES, 0), (abi.PHASE_COMPLEXIFY, 0), (abi.PHASE_TRANSITION, 0),
            (abi.PHASE_POLYMERIZE, 0)]
+    if getattr(cfg, "propagate_state", 0):
+        ph += [(abi.PHASE_PROPAGATE_STATE, 0)]
     ph += [(abi.PHASE_DIFFUSE, j) for j in range(cfg.metabolite_diffusion_steps)]
     ph += [(abi.PHASE_END_STEP, 0)]
     return ph

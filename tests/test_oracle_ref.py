@@ -215,3 +215,23 @@ def test_edge_states_byte_identical(case):
         port.step(1)
         ref.step(1)
         _bytes_equal(port, ref, f"{case}: after step {k + 1}")
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_propagate_state_byte_identical(seed):
+    """propagateState (interactions.cuh:743-822), which the reference's step
+    leaves commented out: the port's pass equals the reference kernel's, as
+    one phase after a sort and inside whole steps with the switch on."""
+    cfg, port, ref = _pair(scenes.propagation_scene(seed))
+    for ph in (abi.PHASE_SORT_PARTICLES, abi.PHASE_SORT_METABOLIC, abi.PHASE_PROPAGATE_STATE):
+        port.run_phase(ph, 0)
+        ref.run_phase(ph, 0)
+        _bytes_equal(port, ref, f"after phase {ph}")
+    before = scenes.propagation_scene(seed)[3]
+    after = port.export_state()[0]
+    assert (after["state"][: len(before)] != before["state"]).sum() > 50, "the pass changed too few states"
+    for k in range(2):
+        for ph, arg in step_phases(cfg):
+            port.run_phase(ph, arg)
+            ref.run_phase(ph, arg)
+        _bytes_equal(port, ref, f"after step {k + 1}")
