@@ -223,32 +223,31 @@ __global__ void __launch_bounds__(SC_THREADS) k_gather_particles(const uint32_t 
     for (int k = 0; k < nw; k++) o[k] = b[k];
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_gather_metabolic(const uint32_t *__restrict__ perm, int n, int sp4,
-                                                                 MFields src, MFields dst) {
+// One step of the metabolic gather: optionally the two double-buffered
+// fields (vel, met) into their other buffers, one single-buffer 16-byte field
+// and one single-buffer int field into their spares (null: not gathered).
+__global__ void __launch_bounds__(SC_THREADS) k_gather_mfield(const uint32_t *__restrict__ perm, int n, int sp4,
+                                                              const float4 *__restrict__ vel, float4 *__restrict__ vel2,
+                                                              const float4 *__restrict__ met, float4 *__restrict__ met2,
+                                                              const float4 *__restrict__ a, float4 *__restrict__ a2,
+                                                              const int *__restrict__ c, int *__restrict__ c2) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int s = (int)perm[i];
-    const float4 pos = src.pos[s], vel = src.vel[s], rot = src.rot[s], angvel = src.angvel[s];
-    const float4 posnoise = src.posnoise[s], angnoise = src.angnoise[s], dbg = src.dbg[s];
-    const int4 info = src.info[s];
-    const int state = src.state[s], orig = src.orig[s];
-    float4 met[3];  // up to 12 species
+    const int s = (int)perm[i];
+    float4 v = make_float4(0, 0, 0, 0), x = make_float4(0, 0, 0, 0), mt[3];
+    int y = 0;
+    if (vel) v = vel[s];
+    if (a) x = a[s];
+    if (c) y = c[s];
 #pragma unroll
     for (int k = 0; k < 3; k++)
-        if (k < sp4) met[k] = src.met[(size_t)s * sp4 + k];
-    dst.pos[i] = pos;
-    dst.vel[i] = vel;
-    dst.rot[i] = rot;
-    dst.angvel[i] = angvel;
-    dst.posnoise[i] = posnoise;
-    dst.angnoise[i] = angnoise;
-    dst.dbg[i] = dbg;
-    dst.info[i] = info;
-    dst.state[i] = state;
-    dst.orig[i] = orig;
+        if (met && k < sp4) mt[k] = met[(size_t)s * sp4 + k];
+    if (vel) vel2[i] = v;
+    if (a) a2[i] = x;
+    if (c) c2[i] = y;
 #pragma unroll
     for (int k = 0; k < 3; k++)
-        if (k < sp4) dst.met[(size_t)i * sp4 + k] = met[k];
+        if (met && k < sp4) met2[(size_t)i * sp4 + k] = mt[k];
 }
 
 // ---- host-side launchers -----------------------------------------------------
@@ -303,9 +302,34 @@ void sc_launch_gather_particles(cudaStream_t st, const uint32_t *perm, int n, co
     (*launches)++;
 }
 
-void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, const MFields &src,
-                                const MFields &dst, long long *launches) {
-    if (n <= 0) return;
-    k_gather_metabolic<<<(n + SC_THREADS - 1) / SC_THREADS, SC_THREADS, 0, st>>>(perm, n, sp4, src, dst);
-    (*launches)++;
+// The metabolic gather through the spares (ScBuffers::mChain4 / mChain1):
+// from parity 0 field k moves from chain entry k + 1 to entry k, fields in
+// ascending order; from parity 1 from entry k to k + 1, in descending order
+// (each launch writes the buffer the previous one read).  vel and met go to
+// their other buffers in the first launch.  Flips the parity and the two
+// double-buffered fields.
+void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, ScBuffers &B,
+                                long long *launches) {
+    if (n > 0) {
+        const MFields src = B.M(), dst = B.Mnext();
+        const int par = B.mParity;
+        for (int t = 0; t < ScBuffers::kM4; t++) {
+            const int k = par ? ScBuffers::kM4 - 1 - t : t;
+            const float4 *a = par ? B.mChain4[k] : B.mChain4[k + 1];
+            float4 *a2 = par ? B.mChain4[k + 1] : B.mChain4[k];
+            const int *c = nullptr;
+            int *c2 = nullptr;
+            if (t < ScBuffers::kM1) {
+                const int q = par ? ScBuffers::kM1 - 1 - t : t;
+                c = par ? B.mChain1[q] : B.mChain1[q + 1];
+                c2 = par ? B.mChain1[q + 1] : B.mChain1[q];
+            }
+            k_gather_mfield<<<(n + SC_THREADS - 1) / SC_THREADS, SC_THREADS, 0, st>>>(
+                perm, n, sp4, t == 0 ? src.vel : nullptr, dst.vel, t == 0 ? src.met : nullptr, dst.met, a, a2, c, c2);
+            (*launches)++;
+        }
+    }
+    B.setMParity(1 - B.mParity);
+    B.cm[FM_VEL] ^= 1;
+    B.cm[FM_MET] ^= 1;
 }

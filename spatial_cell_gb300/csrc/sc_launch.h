@@ -33,6 +33,12 @@ struct ScBuffers {
     int cm[FM_COUNT];   // current buffer of each metabolic field
     // metabolic fields no step kernel touches, in load order (indexed by orig)
     int *mcLscs, *mcSpoly, *mcNb, *mcBonds;
+    // Loads whose metabolic records all hold no interactions and one value of
+    // each of the other two fields keep those two values instead (mcUniform;
+    // the four arrays above are then unallocated until a load needs them).
+    bool mcUniform;
+    int mcLscs0, mcSpoly0;
+    int *mcFlag;   // device word of k_mc_scan
     // binning: keys / slot values ping-pong per item set, the buffer of the
     // last pass holding the sorted keys and the permutation
     uint32_t *keysP[2], *valsP[2], *keysM[2], *valsM[2], *hist, *lookback;
@@ -108,7 +114,36 @@ struct ScBuffers {
         return f;
     }
     void flipAllP() { for (int k = 0; k < FP_COUNT; k++) cp[k] ^= 1; }
-    void flipAllM() { for (int k = 0; k < FM_COUNT; k++) cm[k] ^= 1; }
+
+    // Metabolic fields no step kernel double-buffers (every one but vel and
+    // met) have one buffer each plus one spare per element size.  A sort
+    // gathers them one field at a time into the spare, which then takes the
+    // field's place: chain k of mChain4 / mChain1 (k >= 1) is field k - 1's
+    // buffer at parity 0 and field k's at parity 1, chain entry 0 the spare
+    // at parity 0; sorts alternate the parity, so buffers return every two.
+    static constexpr int kM4 = 7, kM1 = 2;  // pos rot angvel posnoise angnoise dbg info | state orig
+    float4 *mChain4[kM4 + 1];
+    int *mChain1[kM1 + 1];
+    int mParity;
+    float4 **mField4(int k) {
+        switch (k) {
+            case 0: return &m[0].pos;
+            case 1: return &m[0].rot;
+            case 2: return &m[0].angvel;
+            case 3: return &m[0].posnoise;
+            case 4: return &m[0].angnoise;
+            case 5: return &m[0].dbg;
+            default: return reinterpret_cast<float4 **>(&m[0].info);
+        }
+    }
+    int **mField1(int k) { return k == 0 ? &m[0].state : &m[0].orig; }
+    void setMParity(int par) {
+        mParity = par;
+        for (int k = 0; k < kM4; k++) *mField4(k) = mChain4[k + 1 - par];
+        for (int k = 0; k < kM1; k++) *mField1(k) = mChain1[k + 1 - par];
+    }
+    float4 *mSpare4() const { return mChain4[mParity ? kM4 : 0]; }
+    int *mSpare1() const { return mChain1[mParity ? kM1 : 0]; }
 };
 
 // sc_grid.cu
@@ -121,8 +156,8 @@ void sc_launch_cell_start(cudaStream_t st, const uint32_t *keys, int n, uint32_t
                           long long *launches);
 void sc_launch_gather_particles(cudaStream_t st, const uint32_t *perm, int n, const PFields &src, const PFields &dst,
                                 long long *launches);
-void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, const MFields &src,
-                                const MFields &dst, long long *launches);
+void sc_launch_gather_metabolic(cudaStream_t st, const uint32_t *perm, int n, int sp4, ScBuffers &B,
+                                long long *launches);
 
 // sc_observe.cu: FP64 observables.  The observe launcher reduces one item set
 // into out[sc_observe_cols()] through a partials table of

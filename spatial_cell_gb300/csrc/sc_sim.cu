@@ -109,28 +109,42 @@ __global__ void k_unpack_metabolic(const uint8_t *__restrict__ aos, int n, int c
         F.pos[i] = F.vel[i] = F.rot[i] = F.angvel[i] = F.posnoise[i] = F.angnoise[i] = F.dbg[i] = make_float4(0, 0, 0, 0);
         F.info[i] = make_int4(0, 0, 0, 0);
         F.state[i] = 0;
-        cLscs[i] = cSpoly[i] = cNb[i] = 0;
-        for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = 0;
+        if (cLscs) {
+            cLscs[i] = cSpoly[i] = cNb[i] = 0;
+            for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = 0;
+        }
         for (int q = 0; q < SP / 4; q++) F.met[(size_t)i * (SP / 4) + q] = make_float4(0, 0, 0, 0);
         return;
     }
     const uint8_t *r = aos + (size_t)i * 304;
     F.info[i] = make_int4(rdi(r, 0), rdi(r, 4), rdi(r, 8), rdb(r, 24));
     F.state[i] = rdb(r, 12);
-    cLscs[i] = rdi(r, 16);
     F.pos[i] = make_float4(rdf(r, 28), rdf(r, 32), rdf(r, 36), rdf(r, 20));
     F.rot[i] = rd4(r, 48);
     F.vel[i] = make_float4(rdf(r, 64), rdf(r, 68), rdf(r, 72), 0.0f);
     F.posnoise[i] = make_float4(rdf(r, 76), rdf(r, 80), rdf(r, 84), 0.0f);
     F.angvel[i] = rd4(r, 96);
     F.angnoise[i] = rd4(r, 112);
-    int nb = rdi(r, 128);
-    cNb[i] = nb;
-    for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = k < 3 * min(max(nb, 0), 8) ? rdi(r, 132 + 4 * k) : 0;
-    cSpoly[i] = rdi(r, 228);
+    if (cLscs) {
+        cLscs[i] = rdi(r, 16);
+        int nb = rdi(r, 128);
+        cNb[i] = nb;
+        for (int k = 0; k < 24; k++) cBonds[(size_t)i * 24 + k] = k < 3 * min(max(nb, 0), 8) ? rdi(r, 132 + 4 * k) : 0;
+        cSpoly[i] = rdi(r, 228);
+    }
     F.dbg[i] = rd4(r, 240);
     float *met = (float *)(F.met) + (size_t)i * SP;
     for (int k = 0; k < SP; k++) met[k] = k < SC_AOS_NUM_METABOLITES ? rdf(r, 256 + 4 * k) : 0.0f;
+}
+
+// Whether staged metabolic records differ from record 0 in the fields no step
+// kernel touches (interaction count, last state-change step, scheduled
+// polymerisation): any record with interactions or another value sets *mixed.
+__global__ void k_mc_scan(const uint8_t *__restrict__ aos, int n, int *mixed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t *r = aos + (size_t)i * 304;
+    if (rdi(r, 128) != 0 || rdi(r, 16) != rdi(aos, 16) || rdi(r, 228) != rdi(aos, 228)) *mixed = 1;
 }
 
 __device__ __forceinline__ void wr4(uint8_t *r, int off, float4 v) { *(float4 *)(r + off) = v; }
@@ -171,7 +185,8 @@ __global__ void k_pack_particles(uint8_t *__restrict__ aos, const int *nActivePt
 }
 
 __global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePtr, int cap, int SP, MFields F,
-                                 const int *cLscs, const int *cSpoly, const int *cNb, const int *cBonds) {
+                                 const int *cLscs, const int *cSpoly, const int *cNb, const int *cBonds, int lscs0,
+                                 int spoly0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap) return;
     uint8_t *r = aos + (size_t)i * 304;
@@ -180,8 +195,12 @@ __global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePt
         return;
     }
     int o = F.orig[i];
-    pack_common(r, F.info[i], F.state[i], cLscs[o], F.pos[i], F.rot[i], F.vel[i], F.posnoise[i], F.angvel[i],
-                F.angnoise[i], cNb[o], cBonds + (size_t)o * 24, cSpoly[o], F.dbg[i]);
+    if (cLscs)
+        pack_common(r, F.info[i], F.state[i], cLscs[o], F.pos[i], F.rot[i], F.vel[i], F.posnoise[i], F.angvel[i],
+                    F.angnoise[i], cNb[o], cBonds + (size_t)o * 24, cSpoly[o], F.dbg[i]);
+    else
+        pack_common(r, F.info[i], F.state[i], lscs0, F.pos[i], F.rot[i], F.vel[i], F.posnoise[i], F.angvel[i],
+                    F.angnoise[i], 0, nullptr, spoly0, F.dbg[i]);
     for (int k = 256; k < 304; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
     const float *met = (const float *)(F.met) + (size_t)i * SP;
     for (int k = 0; k < SC_AOS_NUM_METABOLITES && k < SP; k++) wrf(r, 256 + 4 * k, met[k]);
@@ -381,8 +400,7 @@ void sort_metabolic(sc_sim *s) {
     int cur = sc_launch_sort(s->st, F.pos, F.info, Nm, s->P, B.keysM, B.valsM, B.hist, B.lookback, B.ctr, &s->launches);
     B.sortCurM = cur;
     sc_launch_cell_start(s->st, B.keysM[cur], Nm, s->P.cells, B.cellStartM, &s->launches);
-    sc_launch_gather_metabolic(s->st, B.valsM[cur], Nm, s->P.SP / 4, B.M(), B.Mnext(), &s->launches);
-    B.flipAllM();
+    sc_launch_gather_metabolic(s->st, B.valsM[cur], Nm, s->P.SP / 4, B, &s->launches);
 }
 
 // Which pair lists a phase invalidates (it changes positions, flags, types,
@@ -418,7 +436,7 @@ std::vector<int> host_state(const sc_sim *s) {
     std::vector<int> v(B.cp, B.cp + FP_COUNT);
     v.insert(v.end(), B.cm, B.cm + FM_COUNT);
     v.insert(v.end(), {B.sortCurP, B.sortCurM, (int)B.validPP, (int)B.validM, (int)B.validLM, (int)B.validD,
-                       s->P.binned, s->P.mAllActive, s->P.lipidValid});
+                       s->P.binned, s->P.mAllActive, s->P.lipidValid, B.mParity});
     return v;
 }
 void set_host_state(sc_sim *s, const std::vector<int> &v) {
@@ -435,6 +453,7 @@ void set_host_state(sc_sim *s, const std::vector<int> &v) {
     s->P.binned = v[k++];
     s->P.mAllActive = v[k++];
     s->P.lipidValid = v[k++];
+    B.setMParity(v[k++]);
 }
 
 int run_phase(sc_sim *s, int phase, int arg) {
@@ -849,14 +868,17 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
             (rc = dalloc(s, &f.angvel, N)) || (rc = dalloc(s, &f.posnoise, N)) || (rc = dalloc(s, &f.angnoise, N)) ||
             (rc = dalloc(s, &f.dbg, N)) || (rc = dalloc(s, &f.info, N)) || (rc = dalloc(s, &f.state, N)) ||
             (rc = dalloc(s, &f.lscs, N)) || (rc = dalloc(s, &f.spoly, N)) || (rc = dalloc(s, &f.nb, N)) ||
-            (rc = dalloc(s, &f.bonds, N * 24)) || (rc = dalloc(s, &m.pos, Nm)) || (rc = dalloc(s, &m.vel, Nm)) ||
-            (rc = dalloc(s, &m.rot, Nm)) || (rc = dalloc(s, &m.angvel, Nm)) || (rc = dalloc(s, &m.posnoise, Nm)) ||
-            (rc = dalloc(s, &m.angnoise, Nm)) || (rc = dalloc(s, &m.dbg, Nm)) || (rc = dalloc(s, &m.info, Nm)) ||
-            (rc = dalloc(s, &m.state, Nm)) || (rc = dalloc(s, &m.met, Nm * Q)) || (rc = dalloc(s, &m.orig, Nm)) ||
+            (rc = dalloc(s, &f.bonds, N * 24)) || (rc = dalloc(s, &m.vel, Nm)) || (rc = dalloc(s, &m.met, Nm * Q)) ||
             (rc = dalloc(s, &B.keysP[b], N)) || (rc = dalloc(s, &B.valsP[b], N)) || (rc = dalloc(s, &B.keysM[b], Nm)) ||
             (rc = dalloc(s, &B.valsM[b], Nm)))
             return bail(rc);
     }
+    // the metabolic fields with one buffer each, and their spares
+    for (int k = 0; k <= ScBuffers::kM4; k++)
+        if ((rc = dalloc(s, &B.mChain4[k], Nm))) return bail(rc);
+    for (int k = 0; k <= ScBuffers::kM1; k++)
+        if ((rc = dalloc(s, &B.mChain1[k], Nm))) return bail(rc);
+    B.setMParity(0);
     const int passes = sc_sort_passes_for(P);
     // The metabolic pair pool starts at kPoolStart entries per item (the
     // tiled sweep's 16-bit lists take the full list capacity) and sc_prepare
@@ -865,8 +887,7 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
     const int poolEntryWords = P.metabLean ? 1 : 4;
     size_t poolWords = sc_list_words(SC_LIST_M, (int)Nm);
     if (P.tileCapM == 0) poolWords = std::min(poolWords, sc_list_words(kPoolStart * poolEntryWords, (int)Nm));
-    if ((rc = dalloc(s, &B.mcLscs, Nm)) || (rc = dalloc(s, &B.mcSpoly, Nm)) || (rc = dalloc(s, &B.mcNb, Nm)) ||
-        (rc = dalloc(s, &B.mcBonds, Nm * 24)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
+    if ((rc = dalloc(s, &B.mcFlag, 1)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
         (rc = dalloc(s, &B.polyList, N)) || (rc = dalloc(s, &B.polyRank, N)) || (rc = dalloc(s, &B.polyPmi, N)) ||
@@ -929,6 +950,45 @@ void sc_destroy(sc_sim *s) {
     delete s;
 }
 
+// The per-item copies of the metabolic fields no step kernel touches, or
+// nulls when the loaded records share one value of each (B.mcUniform).
+#define MC_MIRRORS(B)                                                                                      \
+    ((B).mcUniform ? nullptr : (B).mcLscs), ((B).mcUniform ? nullptr : (B).mcSpoly),                     \
+        ((B).mcUniform ? nullptr : (B).mcNb), ((B).mcUniform ? nullptr : (B).mcBonds)
+
+// Decides, for the nm metabolic records now staged, whether the sim keeps
+// per-item copies of the fields no step kernel touches (allocated the first
+// time a load needs them) or the two values every record shares.
+static int mc_prepare(sc_sim *s, int nm) {
+    ScBuffers &B = s->B;
+    int h[3] = {0, 0, 0};  // record 0's last state-change step and scheduled polymerisation; mixed
+    if (nm > 0) {
+        SC_CK(s, cudaMemsetAsync(B.mcFlag, 0, sizeof(int), s->st));
+        k_mc_scan<<<nb_of(nm), SC_THREADS, 0, s->st>>>(s->staging, nm, B.mcFlag);
+        SC_CK(s, cudaMemcpyAsync(&h[0], s->staging + 16, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+        SC_CK(s, cudaMemcpyAsync(&h[1], s->staging + 228, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+        SC_CK(s, cudaMemcpyAsync(&h[2], B.mcFlag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+        SC_CK(s, cudaStreamSynchronize(s->st));
+        int rc = check_launch(s);
+        if (rc) return rc;
+    }
+    if (!h[2]) {
+        B.mcUniform = true;
+        B.mcLscs0 = h[0];
+        B.mcSpoly0 = h[1];
+        return SC_OK;
+    }
+    if (!B.mcLscs) {
+        const size_t Nm = (size_t)s->P.Nm;
+        int rc;
+        if ((rc = dalloc(s, &B.mcLscs, Nm)) || (rc = dalloc(s, &B.mcSpoly, Nm)) || (rc = dalloc(s, &B.mcNb, Nm)) ||
+            (rc = dalloc(s, &B.mcBonds, Nm * 24)))
+            return rc;
+    }
+    B.mcUniform = false;
+    return SC_OK;
+}
+
 int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_metabolic_particle *metabolic,
                   int32_t nm, int32_t step, int32_t next_particle_id) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
@@ -957,8 +1017,8 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
         if (nm)
             SC_CK(s, cudaMemcpyAsync(s->staging, metabolic, (size_t)nm * sizeof(sc_metabolic_particle),
                                      cudaMemcpyHostToDevice, s->st));
-        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], B.mcLscs,
-                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+        if ((rc = mc_prepare(s, nm))) return rc;
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], MC_MIRRORS(B));
     }
     ScCounters c;
     memset(&c, 0, sizeof c);
@@ -1182,7 +1242,7 @@ int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *me
     if (metabolic && Nm > 0) {
         SC_CK(s, cudaStreamSynchronize(s->st));
         k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
-                                                              B.mcLscs, B.mcSpoly, B.mcNb, B.mcBonds);
+                                                              MC_MIRRORS(B), B.mcLscs0, B.mcSpoly0);
         SC_CK(s, cudaMemcpyAsync(metabolic, s->staging, (size_t)Nm * sizeof(sc_metabolic_particle),
                                  cudaMemcpyDeviceToHost, s->st));
     }
@@ -1274,7 +1334,7 @@ int sc_export_replica(sc_sim *s, int32_t r, sc_particle *particles, sc_metabolic
         memset(metabolic, 0, cap * sizeof(sc_metabolic_particle));
         if (Nm > 0) {
             k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
-                                                                  B.mcLscs, B.mcSpoly, B.mcNb, B.mcBonds);
+                                                                  MC_MIRRORS(B), B.mcLscs0, B.mcSpoly0);
             SC_CK(s, cudaStreamSynchronize(s->st));
             if ((rc = replica_slots(s, B.M().info, Nm, r, runs))) return rc;
             size_t k = 0;
@@ -1364,8 +1424,8 @@ static int generate_into(sc_sim *s, int n, int nm, uint64_t seed, const std::fun
             k_gen_metabolic<<<nb_of(nm), SC_THREADS, 0, s->st>>>(s->staging, nm, box, s->cfg.num_metabolites,
                                                                  mt.radius, mt.hydrophobic, seed);
         }
-        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], B.mcLscs,
-                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+        if ((rc = mc_prepare(s, nm))) return rc;
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], MC_MIRRORS(B));
     }
     ScCounters c;
     memset(&c, 0, sizeof c);
@@ -1445,8 +1505,8 @@ int sc_generate_batch(sc_sim *s, const int32_t *n, const int32_t *nm, const int3
                 k_gen_metabolic<<<nb_of(nm[r]), SC_THREADS, 0, s->st>>>(
                     s->staging + (size_t)offM[r] * sizeof(sc_metabolic_particle), nm[r], s->reps[r].sim_size,
                     s->cfg.num_metabolites, mt.radius, mt.hydrophobic, seeds[r]);
-        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, offM[R], Nm, s->P.SP, B.m[0], B.mcLscs,
-                                                                B.mcSpoly, B.mcNb, B.mcBonds);
+        if ((rc = mc_prepare(s, offM[R]))) return rc;
+        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, offM[R], Nm, s->P.SP, B.m[0], MC_MIRRORS(B));
     }
     ScCounters c;
     memset(&c, 0, sizeof c);

@@ -221,3 +221,31 @@ def test_metabolic_pool_grows_and_results_do_not_change(product, pairs):
     for e in (gpu, cpu):
         e.step(2)
     _same(cfg, gpu, cpu, "2 more steps")
+
+
+@pytest.mark.parametrize("kind", ["uniform", "mixed"])
+def test_metabolic_fields_no_kernel_touches(product, kind):
+    """The metabolic records' interaction slots, last state-change step and
+    scheduled polymerisation pass through steps unchanged: one shared value
+    of each (kept as two numbers), or per-record values (kept per item)."""
+    cfg, types, rules, p, m, nid = scenes.test_scene(8, n=600, nm=1400, box=36.0)
+    rng = np.random.default_rng(8)
+    if kind == "uniform":
+        m["last_state_change_step"] = 7
+        m["scheduled_polymerization"] = 3
+    else:
+        m["last_state_change_step"] = rng.integers(-1, 50, len(m))
+        m["scheduled_polymerization"] = rng.integers(-1, 4, len(m))
+        k = rng.integers(0, 9, len(m))
+        m["n_active_interactions"] = k
+        m["interactions"] = rng.integers(0, 1000, m["interactions"].shape)
+    cfg_, gpu, cpu = _engines(product, (cfg, types, rules, p, m, nid))
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(2)
+    _same(cfg, gpu, cpu, f"{kind} metabolic record fields, 2 steps")
+    got = gpu.export_state()[1]
+    act = (got["flags"] & 1) != 0
+    ids = got["id"][act]
+    for f in ("last_state_change_step", "scheduled_polymerization", "n_active_interactions"):
+        assert np.array_equal(got[f][act], m[f][ids]), f
