@@ -69,23 +69,37 @@ def run(kind, seed, steps):
     return observables(pc, mc, org_p, org_m, cfg.sim_size)
 
 
+def save(path, seeds, rows, steps):
+    out = {k: np.array([r[k] for r in rows]) for k in rows[0]}
+    np.savez_compressed(path, seeds=np.array(seeds), steps=steps, n=N, nm=NM, r_max=R_MAX, bins=BINS, **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", default="1-16")
     ap.add_argument("--steps", type=int, default=STEPS)
     ap.add_argument("--out", default=OUT)
+    ap.add_argument("--append", action="store_true", help="keep the members already in --out, add the others")
     a = ap.parse_args()
     lo, _, hi = a.seeds.partition("-")
     seeds = list(range(int(lo), int(hi or lo) + 1))
     set_threads(max_threads())
-    rows = []
+    done, rows = [], []
+    if a.append and os.path.exists(a.out):
+        d = np.load(a.out)
+        assert int(d["steps"]) == a.steps
+        done = [int(x) for x in d["seeds"]]
+        rows = [{k: d[k][i] for k in d.files if k not in ("seeds", "steps", "n", "nm", "r_max", "bins")}
+                for i in range(len(done))]
     for s in seeds:
+        if s in done:
+            continue
         t0 = time.time()
         rows.append(run("port64", s, a.steps))
+        done.append(s)
         print(f"seed {s}: {time.time() - t0:.0f} s, msd_p {rows[-1]['msd_p']:.4f} msd_m {rows[-1]['msd_m']:.4f}",
               flush=True)
-    out = {k: np.array([r[k] for r in rows]) for k in rows[0]}
-    np.savez_compressed(a.out, seeds=np.array(seeds), steps=a.steps, n=N, nm=NM, r_max=R_MAX, bins=BINS, **out)
+        save(a.out, done, rows, a.steps)  # after every member: an interrupted run keeps what it made
 
 
 if __name__ == "__main__":
