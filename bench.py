@@ -231,18 +231,24 @@ def sub_box(workload, frac):
                 sim_size=float(cfg0.sim_size * frac ** (1.0 / 3.0)))
 
 
-def cpu_sample(args, reps=1, warmup=0):
-    """Times the CPU oracle on a same-density sub-box of the workload:
-    `warmup` untimed steps, then `reps` timed steps."""
-    from oracle import engine as oengine
-    # every host thread this process may run on (a launcher's OMP_NUM_THREADS=1 does not apply: rank 0
-    # runs the CPU leg alone)
+def host_threads():
+    """Every host thread this process may run on (a launcher's OMP_NUM_THREADS=1
+    does not apply: rank 0 runs the CPU leg alone)."""
     try:
-        oengine.set_threads(len(os.sched_getaffinity(0)))
+        return len(os.sched_getaffinity(0))
     except (AttributeError, OSError):
-        oengine.set_threads(os.cpu_count() or 1)
-    frac = args.cpu_fraction
-    cfg = scenes.measured_config(args.workload, **sub_box(args.workload, frac))
+        return os.cpu_count() or 1
+
+
+def cpu_sample(args, reps=1, warmup=0, threads=None, frac=None, workload=None):
+    """Times the CPU oracle on a same-density sub-box of the workload:
+    `warmup` untimed steps, then `reps` timed steps, on `threads` host threads
+    (default: all)."""
+    from oracle import engine as oengine
+    oengine.set_threads(threads or host_threads())
+    frac = args.cpu_fraction if frac is None else frac
+    workload = workload or args.workload
+    cfg = scenes.measured_config(workload, **sub_box(workload, frac))
     n, nm, box = cfg.num_particles, cfg.num_metabolic_particles, cfg.sim_size
     rng = np.random.default_rng(cfg.seed)
     types, rules = scenes.baseline_types(), scenes.workload_rules()
@@ -259,9 +265,24 @@ def cpu_sample(args, reps=1, warmup=0):
     dt = time.perf_counter() - t0
     e.close()
     rate = (n + nm) * reps / dt
-    sample = (f"{reps} step(s) (after {warmup} untimed) of a {frac:.4g}-volume sub-box at the workload's "
+    sample = (f"{reps} step(s) (after {warmup} untimed) of a {frac:.4g}-volume sub-box of {workload} at its "
               f"density ({n} + {nm} items, {box:.1f} nm), {dt:.1f} s")
     return rate, threads, sample
+
+
+def cpu_single_core(args):
+    """The CPU oracle on one host thread: 2 steps of a 1/64-volume sub-box."""
+    rate, _, sample = cpu_sample(args, reps=2, threads=1, frac=1.0 / 64)
+    return {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+
+
+def cpu_small_full(args):
+    """The small workload (65,536 + 131,072 items, 200 nm periodic, seed 1) run
+    in full on the CPU oracle: all 200 of its steps on every host thread."""
+    cfg = scenes.measured_config("plain_small")
+    rate, threads, sample = cpu_sample(args, reps=cfg.steps, threads=host_threads(), frac=1.0, workload="plain_small")
+    return {"metric": METRIC, "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "workload": "plain_small", "sample": sample}
 
 
 def batched_sample(args, native, torch):
@@ -326,11 +347,25 @@ def batched_sample(args, native, torch):
         alone_items += (n + nm) * k
         s1.close()
     alone = alone_items / alone_s
+    # one large cell of the replicas' mean composition (mix (2, 2, 1, 1) / 6, metabolic x2) at their
+    # density: the single-instance rate the batch's per-item rate compares with
+    n1 = 2_097_152
+    c1 = scenes.measured_config("plain_small", num_particles=n1, num_metabolic_particles=2 * n1,
+                                sim_size=float(200.0 * (n1 / 65536.0) ** (1.0 / 3.0)), seed=3, grid_cell_size=cell)
+    s1 = native.Simulation(c1, types, rules)
+    s1.generate_uniform(n1, 2 * n1, kinds, (2 / 6, 2 / 6, 1 / 6, 1 / 6), 3)
+    s1.prepare()
+    single_mix = 3 * n1 * args.batch_steps / timed_steps(s1, args.batch_steps)
+    s1.close()
     return {"replicas": len(specs), "particles": sum(x[0] for x in specs),
             "metabolic_particles": sum(x[1] for x in specs), "steps": args.batch_steps, "value": batched,
             "unit": UNIT, "ms_per_step": 1e3 * batched_s / args.batch_steps, "state_finite": finite,
             "one_at_a_time": alone, "one_at_a_time_sample": f"{len(specs[::8])} replicas (every 8th), {k} steps each",
             "speedup": batched / alone,
+            "single_instance_same_mix": {"value": single_mix, "unit": UNIT,
+                                         "cell": f"{n1} particles + {2 * n1} metabolic, mix (2,2,1,1)/6, the "
+                                                 "replicas' density, one sim"},
+            "vs_single_instance_same_mix": batched / single_mix,
             "form": "one batched sim: one launch per phase over all replicas, replica in the high key bits, "
                     "graph-captured step",
             "sizes": "particles log-uniform in [2048, 262144] (seed 3), metabolic x2, cubes at 65,536 per "
@@ -387,48 +422,71 @@ def serving_sample(args):
 def vesicle_sample(args, native, torch):
     """The crowded vesicle case (900 nm box with reflecting walls: 2 M lipids on a 400 nm
     bilayer shell, 6 M interior particles, 50 k 20-particle lattice complexes,
-    32 M metabolic items; counts scaled by --vesicle-scale), generated on the
-    device: particle-steps/s over --vesicle-steps steps after a warm-up step,
-    and the same with 4 replicas stepping together when the device has room
-    for them.  Wall clock with the device synchronised on both sides."""
+    32 M metabolic items, the measured workloads' A + B binding; counts scaled
+    by --vesicle-scale), generated on the device.  One instance: particle-steps/s
+    over --vesicle-steps steps after a warm-up step, with the step time at the
+    start and the end and the items whose lists overflowed (they take the
+    neighbourhood-scan paths).  Four replicas (seeds 5..8) on the device at
+    once, each with the 4-byte metabolic pair entries (the 16-byte pool of a
+    gas this dense would not leave room for four), stepped in turn for
+    --vesicle-replica-steps steps.  Wall clock with the device synchronised on
+    both sides."""
     cfg, groups, nm = scenes.vesicle_workload(args.vesicle_scale)
     items = cfg.num_particles + nm
-    types, rules = scenes.baseline_types(), scenes.baseline_rules()
+    types, rules = scenes.baseline_types(), scenes.workload_rules()
     torch.cuda.synchronize()
 
-    def make(seed):
-        s = native.Simulation(cfg, types, rules)
+    def make(c, seed):
+        s = native.Simulation(c, types, rules)
         s.generate_scene(groups, nm, seed)
         s.prepare()
         s.step(1)  # warm-up: captures the step graphs
         s.sync()
         return s
 
-    sims = [make(cfg.seed)]
+    one = make(cfg, cfg.seed)
     k = args.vesicle_steps
-    t0 = time.perf_counter()
-    sims[0].step(k)
-    sims[0].sync()
-    one = items * k / (time.perf_counter() - t0)
+    times = []
+    for _ in range(k):
+        t0 = time.perf_counter()
+        one.step(1)
+        one.sync()
+        times.append(time.perf_counter() - t0)
+    ep, em = one.export_state()
+    finite = bool(np.isfinite(ep["pos"][(ep["flags"] & 1) != 0]).all()
+                  and np.isfinite(em["pos"][(em["flags"] & 1) != 0]).all())
     out = {"scale": args.vesicle_scale, "particles": cfg.num_particles, "metabolic_particles": nm,
-           "box_nm": cfg.sim_size, "walls": "reflecting", "steps": k, "value": one, "unit": UNIT,
+           "box_nm": cfg.sim_size, "walls": "reflecting", "steps": k, "value": items * k / sum(times), "unit": UNIT,
+           "ms_per_step_first_last": [round(1e3 * times[0], 1), round(1e3 * times[-1], 1)],
+           "list_overflows_at_end": dict(zip(("particle", "metabolic", "lipid_metabolic", "diffusion"),
+                                             one.list_overflows())),
+           "device_bytes": one.device_bytes(), "state_finite": finite,
+           "complexify": "pair claim, A + B bind at probability %g per step" % scenes.WORKLOAD_BIND_PROBABILITY,
            "scene": "2 leaflets r=400/396 nm (lipids uniform on each sphere), dummy/A/B 70/15/15 in the ball "
                     "r<390 nm, 20-site lattice complexes (3 nm, tree of chain bonds) in r<384 nm, metabolic "
                     "uniform in the box; generated on the device (sc_generate_scene), seed 5",
-           "timing": "wall clock, device synchronised before and after"}
+           "timing": "wall clock per step, device synchronised"}
+    one.close()
+    ks = args.vesicle_replica_steps
+    lean = scenes.vesicle_workload(args.vesicle_scale, metabolic_pairs=0)[0]
+    sims = []
     try:
-        for r in range(1, 4):
-            sims.append(make(cfg.seed + r))
+        for r in range(4):
+            sims.append(make(lean, cfg.seed + r))
     except native.ScError as e:  # the device has no room for four
         out["replicas4"] = {"not_run": f"replica {len(sims) + 1} of 4 could not be created: {e}"}
-    if len(sims) == 4:
+    if len(sims) == 4 and ks > 0:
         t0 = time.perf_counter()
-        for _ in range(k):
+        for _ in range(ks):
             for s in sims:
                 s.step(1)
         for s in sims:
             s.sync()
-        out["replicas4"] = {"value": 4 * items * k / (time.perf_counter() - t0), "unit": UNIT}
+        out["replicas4"] = {"value": 4 * items * ks / (time.perf_counter() - t0), "unit": UNIT, "steps": ks,
+                            "device_bytes_each": [s.device_bytes() for s in sims],
+                            "form": "four sims on the device at once, each step of each enqueued in turn "
+                                    "(graph launches on their own streams)",
+                            "metabolic_pairs": "4-byte entries"}
     for s in sims:
         s.close()
     return out
@@ -572,6 +630,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         sim.step(1)
     sim.sync()
+    footprint = sim.device_bytes()
 
     # device-resident timing
     launches0 = sim.counters().kernel_launches
@@ -656,6 +715,7 @@ def run_ours(args):
     line = None
     if rank == 0:
         cpu_rate, cpu_threads, cpu_desc = cpu_sample(args, reps=2) if not args.no_cpu else (None, 0, "skipped")
+        cpu_one = cpu_single_core(args) if not args.no_cpu else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -683,8 +743,10 @@ def run_ours(args):
                                "diffusion": pairs[3]},
             "phase_ms_per_launch": phase_ms, "phase_share_of_step": share,
             "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
-                             "sample": cpu_desc},
+                             "sample": cpu_desc, "single_core": cpu_one},
             "state_finite": finite, "bonds_per_particle": bbar,
+            "device_bytes": {"sim": footprint, "per_item": footprint / (N + Nm),
+                             "note": "sc_device_bytes after the warm-up steps: state, lists and pools"},
             "clocks": clocks.summary(),
             "gpu_launches": launches,
             "batched": batched,
@@ -717,7 +779,9 @@ def main():
     ap.add_argument("--serve-horizon", type=int, default=150, help="longest request horizon (steps)")
     ap.add_argument("--vesicle-scale", type=float, default=1.0,
                     help="count scale of the vesicle sample (0: skip it)")
-    ap.add_argument("--vesicle-steps", type=int, default=6)
+    ap.add_argument("--vesicle-steps", type=int, default=100)
+    ap.add_argument("--vesicle-replica-steps", type=int, default=25,
+                    help="steps of each of the four vesicle replicas")
     ap.add_argument("--metabolic-pairs", type=int, default=1, choices=[0, 1],
                     help="metabolic relaxation pairs: 0 4-byte entries (geometry per sub-iteration), "
                          "1 16-byte entries with the geometry frozen per step")
@@ -725,8 +789,12 @@ def main():
                     help="steps of the reference's CUDA step timed beside this build's (0: skip)")
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="run a same-density sub-box of this volume fraction (small cases for profiling)")
+    ap.add_argument("--cpu-small-full", action="store_true",
+                    help="only run the small workload in full (200 steps) on the CPU oracle and print its line")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.cpu_small_full:
+        print(json.dumps(cpu_small_full(args)))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -221,21 +221,24 @@ def vesicle_groups(box, shell_r=400.0, lipids=2_000_000, interior=6_000_000, com
     ]
 
 
-def vesicle_workload(scale=1.0):
+def vesicle_workload(scale=1.0, **overrides):
     """The crowded vesicle stress case (900 nm box with reflecting walls, 2 M
     lipids on a 400 nm bilayer shell, 6 M interior particles, 50 k 20-particle complexes,
     32 M metabolic items, seed 5), every count scaled by `scale` and every
-    length by its cube root.  Returns (config, groups, metabolic count)."""
+    length by its cube root, with the measured workloads' A + B binding
+    (workload_rules: probability 0.1 per step, pair claim).  Returns
+    (config, groups, metabolic count)."""
     s = scale ** (1.0 / 3.0)
     box = 900.0 * s
     groups = vesicle_groups(box, shell_r=400.0 * s, lipids=int(2_000_000 * scale), interior=int(6_000_000 * scale),
                             complexes=int(50_000 * scale))
     n = abi.scene_particles(groups)
     nm = int(32_000_000 * scale)
-    cfg = abi.make_config(num_particles=n, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
-                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5,
-                          steps=1000, periodic=0, walls=1)
-    return cfg, groups, nm
+    kw = dict(num_particles=n, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
+              max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5, steps=1000,
+              periodic=0, walls=1, **WORKLOAD_EXTENSIONS)
+    kw.update(overrides)
+    return abi.make_config(**kw), groups, nm
 
 
 def build_workload(name, **overrides):
