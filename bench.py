@@ -20,11 +20,18 @@ in a 635 nm box, 6 nm cells, seeded synthetic state (no dataset exists).
   roofline  the dominant kernel's algorithmic bytes per launch over its
             measured launch time, against the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (oracle/scport.cpp, OpenMP on all host cores)
-            timed on a same-density sub-box of the workload.
-``--impl reference`` times that CPU implementation alone (the reference has
-no CPU path of its own and its GPU build cannot be made on this machine).
-Under torchrun, every rank runs an independent replica (the path does not
-shard); value is the sum over ranks of items per step over the slowest rank.
+            timed on a same-density sub-box of the workload, and on one core;
+  reference_cuda  the reference's own CUDA step (its kernels compiled for
+            sm_103a, main.cu's launch sequence, CUB's sort of whole structs)
+            timed on the same GPU and state beside this build's step;
+  batched / serving / vesicle  the batched replica cells, the request loop
+            and the crowded vesicle case (docstrings of their samples).
+``--impl reference`` times the CPU implementation alone (the reference has no
+CPU path of its own; its CUDA step is the reference_cuda entry above).
+``--cpu-small-full`` runs the small workload in full (200 steps) on the CPU
+oracle.  Under torchrun, every rank runs an independent replica (the path
+does not shard); value is the sum over ranks of items per step over the
+slowest rank.
 """
 import argparse
 import ctypes
@@ -468,27 +475,30 @@ def vesicle_sample(args, native, torch):
            "timing": "wall clock per step, device synchronised"}
     one.close()
     ks = args.vesicle_replica_steps
-    lean = scenes.vesicle_workload(args.vesicle_scale, metabolic_pairs=0)[0]
-    sims = []
-    try:
-        for r in range(4):
-            sims.append(make(lean, cfg.seed + r))
-    except native.ScError as e:  # the device has no room for four
-        out["replicas4"] = {"not_run": f"replica {len(sims) + 1} of 4 could not be created: {e}"}
-    if len(sims) == 4 and ks > 0:
-        t0 = time.perf_counter()
-        for _ in range(ks):
-            for s in sims:
-                s.step(1)
-        for s in sims:
-            s.sync()
-        out["replicas4"] = {"value": 4 * items * ks / (time.perf_counter() - t0), "unit": UNIT, "steps": ks,
-                            "device_bytes_each": [s.device_bytes() for s in sims],
-                            "form": "four sims on the device at once, each step of each enqueued in turn "
-                                    "(graph launches on their own streams)",
-                            "metabolic_pairs": "4-byte entries"}
-    for s in sims:
-        s.close()
+    if ks > 0:
+        lean = scenes.vesicle_workload(args.vesicle_scale, metabolic_pairs=0)[0]
+        seeds = [cfg.seed + r for r in range(4)]
+        reps = [abi.Replica(cfg.num_particles, nm, cfg.sim_size, 0, sd) for sd in seeds]
+        try:
+            b = native.Simulation(lean, types, rules, replicas=reps)
+        except native.ScError as e:  # the device has no room for four
+            out["replicas4"] = {"not_run": f"a batch of 4 replicas could not be created: {e}"}
+        else:
+            b.generate_scene_batch(groups, nm, seeds)
+            b.prepare()
+            b.step(1)  # warm-up: captures the step graph
+            b.sync()
+            t0 = time.perf_counter()
+            b.step(ks)
+            b.sync()
+            dt = time.perf_counter() - t0
+            ok = all(np.isfinite(b.export_replica(r)[0]["pos"]).all() for r in range(4))
+            out["replicas4"] = {"value": 4 * items * ks / dt, "unit": UNIT, "steps": ks,
+                                "ms_per_step": 1e3 * dt / ks, "device_bytes": b.device_bytes(), "state_finite": ok,
+                                "form": "one batched sim of 4 replicas (seeds 5..8): one launch per phase over "
+                                        "all of them, graph-captured step",
+                                "metabolic_pairs": "4-byte entries"}
+            b.close()
     return out
 
 

@@ -497,6 +497,13 @@ typedef struct sc_scene_group {
 /* Fills the sim with the groups' particles (their total must fit its
  * capacity) and nm metabolic particles; counters as sc_generate_uniform. */
 int sc_generate_scene(sc_sim *sim, const sc_scene_group *groups, int32_t n_groups, int32_t nm, uint64_t seed);
+/* Batched sims: every replica r gets the groups' particles and nm metabolic
+ * particles as sc_generate_scene with seeds[r] gives a sim of its own (the
+ * groups' coordinates are the same in every replica's box); the replicas'
+ * particle and metabolic capacities must hold them.  Records are generated
+ * one replica at a time, so the staging memory is one replica's. */
+int sc_generate_scene_batch(sc_sim *sim, const sc_scene_group *groups, int32_t n_groups, int32_t nm,
+                            const uint64_t *seeds);
 
 /* ---- observables (no counterpart in the reference) ----
  * Ensemble quantities reduced on the device in double precision, in a fixed

@@ -100,11 +100,13 @@ __global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int c
     F.dbg[i] = rd4(r, 240);
 }
 
+// Slots [0, cap) of F (records i < n from aos, the rest empty); `base` is the
+// load slot of slot 0 (F shifted to a batch replica's first slot).
 __global__ void k_unpack_metabolic(const uint8_t *__restrict__ aos, int n, int cap, int SP, MFields F, int *cLscs,
-                                   int *cSpoly, int *cNb, int *cBonds) {
+                                   int *cSpoly, int *cNb, int *cBonds, int base = 0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap) return;
-    F.orig[i] = i;
+    F.orig[i] = base + i;
     if (i >= n) {
         F.pos[i] = F.vel[i] = F.rot[i] = F.angvel[i] = F.posnoise[i] = F.angnoise[i] = F.dbg[i] = make_float4(0, 0, 0, 0);
         F.info[i] = make_int4(0, 0, 0, 0);
@@ -1540,6 +1542,107 @@ int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups,
                 k_gen_scene<<<nb_of(G.count), SC_THREADS, 0, s->st>>>(s->staging, G, per, box, seed);
         }
     });
+}
+
+// A batch's field views from slot o on.
+static PFields shift_p(PFields f, size_t o) {
+    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
+    f.state += o; f.lscs += o; f.spoly += o; f.nb += o; f.bonds += 24 * o;
+    return f;
+}
+static MFields shift_m(MFields f, size_t o, size_t q) {
+    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
+    f.state += o; f.met += o * q; f.orig += o;
+    return f;
+}
+
+int sc_generate_scene_batch(sc_sim *s, const sc_scene_group *groups, int32_t n_groups, int32_t nm,
+                            const uint64_t *seeds) {
+    if (!s || !seeds) return set_err(s, SC_E_INVALID, "null argument");
+    if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
+    enter(s);
+    const int R = (int)s->reps.size();
+    if (n_groups < 0 || (n_groups > 0 && !groups) || nm < 0) return set_err(s, SC_E_INVALID, "bad group list");
+    std::vector<sc_gen_group> gg((size_t)std::max(n_groups, 1));
+    const char *why = "";
+    const int64_t total = sc_gen_prepare(groups, n_groups, s->types.data(), (int32_t)s->types.size(), gg.data(), &why);
+    if (total < 0) return set_err(s, SC_E_INVALID, why);
+    const int n = (int)total;
+    std::vector<int> offP(R + 1, 0), offM(R + 1, 0);
+    for (int r = 0; r < R; r++) {
+        if (n > s->reps[r].num_particles || nm > s->reps[r].num_metabolic_particles)
+            return set_err(s, SC_E_INVALID, "replica " + std::to_string(r) + ": scene larger than its capacity");
+        offP[r + 1] = offP[r] + n;
+        offM[r + 1] = offM[r] + nm;
+    }
+    if (nm > 0 && (int)s->types.size() <= SC_PARTICLE_TYPE_METABOLIC)
+        return set_err(s, SC_E_INVALID, "the type table has no metabolic particle type (1000)");
+    const int N = s->P.N, Nm = s->P.Nm;
+    int rc = ensure_staging(s, std::max<size_t>(std::max((size_t)n * sizeof(sc_particle),
+                                                         (size_t)nm * sizeof(sc_metabolic_particle)), 16));
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    B.invalidateLists();
+    s->P.binned = 0;
+    s->P.mAllActive = 0;
+    s->P.lipidValid = 0;
+    for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
+    for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
+    const size_t Q = (size_t)s->P.SP / 4;
+    const sc_type_info *mt = nm > 0 ? &s->types[SC_PARTICLE_TYPE_METABOLIC] : nullptr;
+    bool uniform = true;
+    int lscs0 = 0, spoly0 = 0;
+    for (int r = 0; r < R; r++) {
+        const float box = s->reps[r].sim_size;
+        // replica r's records, as sc_generate_scene writes them for a sim of its own
+        for (int32_t g = 0; g < n_groups; g++) {
+            const sc_gen_group &G = gg[(size_t)g];
+            const int per = (G.kind == SC_SCENE_COMPLEXES || G.kind == SC_SCENE_WRAPPED_CHAINS) ? G.unit : 1;
+            if (G.count > 0)
+                k_gen_scene<<<nb_of(G.count), SC_THREADS, 0, s->st>>>(s->staging, G, per, box, seeds[r]);
+        }
+        if (n > 0)
+            k_unpack_particles<<<nb_of(n), SC_THREADS, 0, s->st>>>(s->staging, n, n, shift_p(B.p[0], (size_t)offP[r]));
+        if (nm > 0) {
+            k_gen_metabolic<<<nb_of(nm), SC_THREADS, 0, s->st>>>(s->staging, nm, box, s->cfg.num_metabolites,
+                                                                 mt->radius, mt->hydrophobic, seeds[r]);
+            if ((rc = mc_prepare(s, nm))) return rc;
+            // generated metabolic records all share one value of each untouched field
+            if (r == 0) {
+                uniform = B.mcUniform;
+                lscs0 = B.mcLscs0;
+                spoly0 = B.mcSpoly0;
+            }
+            if (!B.mcUniform || !uniform || B.mcLscs0 != lscs0 || B.mcSpoly0 != spoly0)
+                return set_err(s, SC_E_INVALID, "generated metabolic records differ between replicas");
+            k_unpack_metabolic<<<nb_of(nm), SC_THREADS, 0, s->st>>>(
+                s->staging, nm, nm, s->P.SP, shift_m(B.m[0], (size_t)offM[r], Q), nullptr, nullptr, nullptr, nullptr,
+                offM[r]);
+        }
+        // the staging buffer is rewritten by the next replica
+        SC_CK(s, cudaStreamSynchronize(s->st));
+        if ((rc = check_launch(s))) return rc;
+    }
+    // the slots past the last replica's items are empty
+    if (N > offP[R])
+        k_unpack_particles<<<nb_of(N - offP[R]), SC_THREADS, 0, s->st>>>(s->staging, 0, N - offP[R],
+                                                                         shift_p(B.p[0], (size_t)offP[R]));
+    if (Nm > offM[R])
+        k_unpack_metabolic<<<nb_of(Nm - offM[R]), SC_THREADS, 0, s->st>>>(
+            s->staging, 0, Nm - offM[R], s->P.SP, shift_m(B.m[0], (size_t)offM[R], Q), nullptr, nullptr, nullptr,
+            nullptr, offM[R]);
+    if (nm == 0) B.mcUniform = true;
+    ScCounters c;
+    memset(&c, 0, sizeof c);
+    c.nActive = offP[R];
+    c.lastActive = offP[R] - 1;
+    c.nActiveM = offM[R];
+    SC_CK(s, cudaMemcpyAsync(B.ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    SC_CK(s, cudaStreamSynchronize(s->st));
+    if ((rc = check_launch(s))) return rc;
+    release_staging(s);
+    s->loaded = true;
+    return set_batch_reps(s, offP, offM);
 }
 
 int sc_mark_positions(sc_sim *s) {

@@ -61,6 +61,7 @@ _SIGS = {
     "sc_load_batch": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32]),
     "sc_export_replica": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "sc_generate_batch": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32, _P]),
+    "sc_generate_scene_batch": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
 }
 
 # Every symbol include/spatialcell.h declares.
@@ -253,6 +254,16 @@ class Simulation:
                                  np.zeros(0, abi.SCENE_GROUP_DTYPE), abi.SCENE_GROUP_DTYPE)
         _check(self.L.sc_generate_scene(self.h, abi.ptr(g) if len(g) else None, len(g), nm, seed), self.h,
                "sc_generate_scene")
+
+    def generate_scene_batch(self, groups, nm, seeds):
+        """Fills a batched sim on the device (sc_generate_scene_batch): every
+        replica r gets the scene groups' particles and nm metabolic particles,
+        seeded by seeds[r]."""
+        g = np.ascontiguousarray(np.concatenate([np.atleast_1d(x) for x in groups]) if len(groups) else
+                                 np.zeros(0, abi.SCENE_GROUP_DTYPE), abi.SCENE_GROUP_DTYPE)
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        _check(self.L.sc_generate_scene_batch(self.h, abi.ptr(g) if len(g) else None, len(g), nm, abi.ptr(sd)),
+               self.h, "sc_generate_scene_batch")
 
     def prepare(self):
         _check(self.L.sc_prepare(self.h), self.h, "sc_prepare")

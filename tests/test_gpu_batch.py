@@ -109,3 +109,36 @@ def test_generated_batch_equals_generated_solo_sims(product):
                           what=f"generated replica {r}")
         solo.close()
     batch.close()
+
+
+@pytest.mark.gpu
+def test_scene_batch_replicas_equal_their_own_sims(product):
+    """A batch of structured scenes (sc_generate_scene_batch): each replica
+    -- generated one replica at a time into its own slots, then stepped with
+    the others -- equals a sim of its own with sc_generate_scene and that seed."""
+    box = 120.0
+    groups = scenes.vesicle_groups(box, shell_r=50.0, lipids=2000, interior=3000, complexes=20, complex_size=20)
+    n = abi.scene_particles(groups)
+    nm = 4000
+    seeds = [5, 9, 11]
+    cfg = abi.make_config(num_particles=n, num_metabolic_particles=nm, sim_size=box, grid_cell_size=6.0,
+                          max_interaction_distance=5.5, max_diffusion_distance=6.0, num_metabolites=8, seed=5,
+                          periodic=0, walls=1, pair_claim=1, rule_probabilities=1, noise_coordination_steps=4,
+                          relaxation_steps=6, metabolite_diffusion_steps=3)
+    types, rules = scenes.baseline_types(), scenes.workload_rules()
+    replicas = [abi.Replica(n + 16 * r, nm + 8, box, 0, sd) for r, sd in enumerate(seeds)]
+    batch = product.Simulation(cfg, types, rules, replicas=replicas)
+    batch.generate_scene_batch(groups, nm, seeds)
+    batch.prepare()
+    batch.step(2)
+    for r, sd in enumerate(seeds):
+        c = abi.config_from_bytes(bytes(cfg))
+        c.num_particles, c.num_metabolic_particles, c.seed = n + 16 * r, nm + 8, sd
+        solo = product.Simulation(c, types, rules)
+        solo.generate_scene(groups, nm, sd)
+        solo.prepare()
+        solo.step(2)
+        assert_same_state(batch.export_replica(r), solo.export_state(), species=cfg.num_metabolites,
+                          what=f"scene replica {r}")
+        solo.close()
+    batch.close()
