@@ -56,12 +56,12 @@ struct ScBuffers {
     int *permM, *permLM, *permD;  // count-ordered list position -> item
     uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
     int *ovfPP, *ovfM;            // overflowed items
-    int *warpOffM;                // metabolic pair pool: first entry of every warp's region
+    long long *warpOffM;          // metabolic pair pool: first entry of every warp's region
     int *workP;                   // particle work list (the items complexify scans)
     unsigned long long *claimP;   // pair-claim keys, one per particle slot (sc_config.pair_claim)
     size_t poolCapM;              // entries the metabolic pair pool (listM) holds
     int poolEntryWords;           // 4-byte words per metabolic pool entry: 1 (lean) or 4 (with geometry)
-    int *warpOffLM;               // lipid-metabolic pair pool: the same
+    long long *warpOffLM;         // lipid-metabolic pair pool: the same
     uint8_t *lipidP;              // per sorted particle slot: active lipid (after each particle sort)
     bool validPP, validM, validLM, validD;
     void invalidateLists() { validPP = validM = validLM = validD = false; }

@@ -74,7 +74,11 @@ __global__ void k_gen_metabolic(uint8_t *aos, int nm, float box, int species, fl
                          box, species, radius, hydrophobic, seed);
 }
 
-__global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int cap, PFields F) {
+// Slots [0, cap) of F (records i < n from aos, the rest empty).  With `bad`,
+// the lowest record index (plus base) whose interaction count is outside
+// 0..8 is recorded there by atomicMin.
+__global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int cap, PFields F, int *bad = nullptr,
+                                   int base = 0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap) return;
     if (i >= n) {
@@ -94,6 +98,7 @@ __global__ void k_unpack_particles(const uint8_t *__restrict__ aos, int n, int c
     F.angvel[i] = rd4(r, 96);
     F.angnoise[i] = rd4(r, 112);
     int nb = rdi(r, 128);
+    if (bad && (nb < 0 || nb > SC_MAX_ACTIVE_INTERACTIONS)) atomicMin(bad, base + i);
     F.nb[i] = nb;
     for (int k = 0; k < 24; k++) F.bonds[(size_t)i * 24 + k] = k < 3 * min(max(nb, 0), 8) ? rdi(r, 132 + 4 * k) : 0;
     F.spoly[i] = rdi(r, 228);
@@ -147,6 +152,13 @@ __global__ void k_mc_scan(const uint8_t *__restrict__ aos, int n, int *mixed) {
     if (i >= n) return;
     const uint8_t *r = aos + (size_t)i * 304;
     if (rdi(r, 128) != 0 || rdi(r, 16) != rdi(aos, 16) || rdi(r, 228) != rdi(aos, 228)) *mixed = 1;
+}
+// The same test against given values (records loaded chunk by chunk).
+__global__ void k_mc_scan_ref(const uint8_t *__restrict__ aos, int n, int lscs0, int spoly0, int *mixed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t *r = aos + (size_t)i * 304;
+    if (rdi(r, 128) != 0 || rdi(r, 16) != lscs0 || rdi(r, 228) != spoly0) *mixed = 1;
 }
 
 __device__ __forceinline__ void wr4(uint8_t *r, int off, float4 v) { *(float4 *)(r + off) = v; }
@@ -889,7 +901,7 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
     const int poolEntryWords = P.metabLean ? 1 : 4;
     size_t poolWords = sc_list_words(SC_LIST_M, (int)Nm);
     if (P.tileCapM == 0) poolWords = std::min(poolWords, sc_list_words(kPoolStart * poolEntryWords, (int)Nm));
-    if ((rc = dalloc(s, &B.mcFlag, 1)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
+    if ((rc = dalloc(s, &B.mcFlag, 4)) || (rc = dalloc(s, &B.hist, 4 * 256)) ||
         (rc = dalloc(s, &B.lookback, (size_t)passes * sc_sort_lookback_words((int)std::max(N, Nm)))) ||
         (rc = dalloc(s, &B.cellStartP, (size_t)P.cells + 1)) || (rc = dalloc(s, &B.cellStartM, (size_t)P.cells + 1)) ||
         (rc = dalloc(s, &B.polyList, N)) || (rc = dalloc(s, &B.polyRank, N)) || (rc = dalloc(s, &B.polyPmi, N)) ||
@@ -914,7 +926,7 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
     }
     B.invalidateLists();
     B.poolEntryWords = poolEntryWords;
-    B.poolCapM = std::min<size_t>(poolWords / B.poolEntryWords, (size_t)INT_MAX - 1024);
+    B.poolCapM = poolWords / B.poolEntryWords;
     // pool_per_item = n >= 0 starts the metabolic pair pool at n entries per item
     if (cfg->pool_per_item >= 0)
         B.poolCapM = std::min(B.poolCapM, (size_t)cfg->pool_per_item * (size_t)std::max<int64_t>(Nm, 1));
@@ -991,6 +1003,23 @@ static int mc_prepare(sc_sim *s, int nm) {
     return SC_OK;
 }
 
+// Field views from slot o on (a chunk of a load, a batch replica's slots).
+static PFields shift_p(PFields f, size_t o) {
+    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
+    f.state += o; f.lscs += o; f.spoly += o; f.nb += o; f.bonds += 24 * o;
+    return f;
+}
+static MFields shift_m(MFields f, size_t o, size_t q) {
+    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
+    f.state += o; f.met += o * q; f.orig += o;
+    return f;
+}
+
+// Records cross into the device through one staging slot, a chunk at a time
+// (copy, then unpack into the chunk's slots), so a load holds kStageBytes of
+// staging whatever the state's size.
+const size_t kStageBytes = (size_t)64 << 20;
+
 int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_metabolic_particle *metabolic,
                   int32_t nm, int32_t step, int32_t next_particle_id) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
@@ -998,29 +1027,72 @@ int sc_load_state(sc_sim *s, const sc_particle *particles, int32_t n, const sc_m
     const int N = s->P.N, Nm = s->P.Nm;
     if (n < 0 || nm < 0 || n > N || nm > Nm || (n > 0 && !particles) || (nm > 0 && !metabolic))
         return set_err(s, SC_E_INVALID, "state larger than the capacity or missing");
-    for (int i = 0; i < n; i++)
-        if (particles[i].n_active_interactions < 0 || particles[i].n_active_interactions > SC_MAX_ACTIVE_INTERACTIONS)
-            return set_err(s, SC_E_INVALID, "particle " + std::to_string(i) + " has more than 8 interactions");
-    size_t bytes = std::max((size_t)n * sizeof(sc_particle), (size_t)nm * sizeof(sc_metabolic_particle));
-    int rc = ensure_staging(s, std::max<size_t>(bytes, 16));
+    int rc = ensure_staging(s, kStageBytes);
     if (rc) return rc;
     ScBuffers &B = s->B;
     B.invalidateLists();
+    s->loaded = false;
     s->P.binned = 0;
     s->P.mAllActive = 0;
     s->P.lipidValid = 0;
     for (int k = 0; k < FP_COUNT; k++) B.cp[k] = 0;
     for (int k = 0; k < FM_COUNT; k++) B.cm[k] = 0;
-    if (N > 0) {
-        if (n) SC_CK(s, cudaMemcpyAsync(s->staging, particles, (size_t)n * sizeof(sc_particle), cudaMemcpyHostToDevice, s->st));
-        k_unpack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, n, N, B.p[0]);
+    // mcFlag: [0] a metabolic record differs from the first, [1] the lowest
+    // particle index with an interaction count outside 0..8
+    const int flags0[2] = {0, INT_MAX};
+    SC_CK(s, cudaMemcpyAsync(B.mcFlag, flags0, sizeof flags0, cudaMemcpyHostToDevice, s->st));
+    const uint8_t *hp = reinterpret_cast<const uint8_t *>(particles);
+    const int perP = (int)(kStageBytes / sizeof(sc_particle));
+    for (int i0 = 0; i0 < n; i0 += perP) {
+        const int cnt = std::min(perP, n - i0);
+        SC_CK(s, cudaMemcpyAsync(s->staging, hp + (size_t)i0 * sizeof(sc_particle), (size_t)cnt * sizeof(sc_particle),
+                                 cudaMemcpyHostToDevice, s->st));
+        k_unpack_particles<<<nb_of(cnt), SC_THREADS, 0, s->st>>>(s->staging, cnt, cnt, shift_p(B.p[0], (size_t)i0),
+                                                                 B.mcFlag + 1, i0);
     }
-    if (Nm > 0) {
-        if (nm)
-            SC_CK(s, cudaMemcpyAsync(s->staging, metabolic, (size_t)nm * sizeof(sc_metabolic_particle),
-                                     cudaMemcpyHostToDevice, s->st));
-        if ((rc = mc_prepare(s, nm))) return rc;
-        k_unpack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, nm, Nm, s->P.SP, B.m[0], MC_MIRRORS(B));
+    if (N > n)
+        k_unpack_particles<<<nb_of(N - n), SC_THREADS, 0, s->st>>>(s->staging, 0, N - n, shift_p(B.p[0], (size_t)n));
+    // metabolic records: unpacked as sharing one value of each untouched field
+    // (every scene here), scanned as they pass; a load that turns out mixed
+    // is unpacked again with per-item copies
+    const uint8_t *hm = reinterpret_cast<const uint8_t *>(metabolic);
+    const int lscs0 = nm > 0 ? metabolic[0].p.last_state_change_step : 0;
+    const int spoly0 = nm > 0 ? metabolic[0].p.scheduled_polymerization : 0;
+    const int perM = (int)(kStageBytes / sizeof(sc_metabolic_particle));
+    const size_t Q = (size_t)s->P.SP / 4;
+    for (int pass = 0; pass < 2; pass++) {
+        const bool mirrors = pass == 1;
+        for (int i0 = 0; i0 < nm; i0 += perM) {
+            const int cnt = std::min(perM, nm - i0);
+            SC_CK(s, cudaMemcpyAsync(s->staging, hm + (size_t)i0 * sizeof(sc_metabolic_particle),
+                                     (size_t)cnt * sizeof(sc_metabolic_particle), cudaMemcpyHostToDevice, s->st));
+            if (!mirrors)
+                k_mc_scan_ref<<<nb_of(cnt), SC_THREADS, 0, s->st>>>(s->staging, cnt, lscs0, spoly0, B.mcFlag);
+            k_unpack_metabolic<<<nb_of(cnt), SC_THREADS, 0, s->st>>>(
+                s->staging, cnt, cnt, s->P.SP, shift_m(B.m[0], (size_t)i0, Q), mirrors ? B.mcLscs + i0 : nullptr,
+                mirrors ? B.mcSpoly + i0 : nullptr, mirrors ? B.mcNb + i0 : nullptr,
+                mirrors ? B.mcBonds + (size_t)i0 * 24 : nullptr, i0);
+        }
+        if (Nm > nm)
+            k_unpack_metabolic<<<nb_of(Nm - nm), SC_THREADS, 0, s->st>>>(
+                s->staging, 0, Nm - nm, s->P.SP, shift_m(B.m[0], (size_t)nm, Q), mirrors ? B.mcLscs + nm : nullptr,
+                mirrors ? B.mcSpoly + nm : nullptr, mirrors ? B.mcNb + nm : nullptr,
+                mirrors ? B.mcBonds + (size_t)nm * 24 : nullptr, nm);
+        int flags[2] = {0, INT_MAX};
+        SC_CK(s, cudaMemcpyAsync(flags, B.mcFlag, sizeof flags, cudaMemcpyDeviceToHost, s->st));
+        SC_CK(s, cudaStreamSynchronize(s->st));
+        if ((rc = check_launch(s))) return rc;
+        if (flags[1] != INT_MAX)
+            return set_err(s, SC_E_INVALID, "particle " + std::to_string(flags[1]) + " has more than 8 interactions");
+        if (mirrors || !flags[0]) {
+            B.mcUniform = !mirrors;
+            B.mcLscs0 = lscs0;
+            B.mcSpoly0 = spoly0;
+            break;
+        }
+        if (!B.mcLscs && ((rc = dalloc(s, &B.mcLscs, (size_t)Nm)) || (rc = dalloc(s, &B.mcSpoly, (size_t)Nm)) ||
+                          (rc = dalloc(s, &B.mcNb, (size_t)Nm)) || (rc = dalloc(s, &B.mcBonds, (size_t)Nm * 24))))
+            return rc;
     }
     ScCounters c;
     memset(&c, 0, sizeof c);
@@ -1113,9 +1185,8 @@ static int grow_pools(sc_sim *s) {
     ScBuffers &B = s->B;
     unsigned long long need = 0;
     SC_CK(s, cudaMemcpy(&need, &B.ctr->poolM, sizeof need, cudaMemcpyDeviceToHost));
-    const size_t most = (size_t)INT_MAX - 1024;  // pool offsets are 32-bit
-    if (need <= B.poolCapM || B.poolCapM >= most) return SC_OK;
-    const size_t cap = std::min<size_t>((size_t)need + (size_t)need / 4 + 1024, most);
+    if (need <= B.poolCapM) return SC_OK;
+    const size_t cap = (size_t)need + (size_t)need / 4 + 1024;
     uint32_t *grown = nullptr;
     int rc = dalloc(s, &grown, cap * B.poolEntryWords);
     if (rc) {  // no room: keep the pool (the overflowing blocks keep scanning)
@@ -1542,18 +1613,6 @@ int sc_generate_scene(sc_sim *s, const sc_scene_group *groups, int32_t n_groups,
                 k_gen_scene<<<nb_of(G.count), SC_THREADS, 0, s->st>>>(s->staging, G, per, box, seed);
         }
     });
-}
-
-// A batch's field views from slot o on.
-static PFields shift_p(PFields f, size_t o) {
-    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
-    f.state += o; f.lscs += o; f.spoly += o; f.nb += o; f.bonds += 24 * o;
-    return f;
-}
-static MFields shift_m(MFields f, size_t o, size_t q) {
-    f.pos += o; f.vel += o; f.rot += o; f.angvel += o; f.posnoise += o; f.angnoise += o; f.dbg += o; f.info += o;
-    f.state += o; f.met += o * q; f.orig += o;
-    return f;
 }
 
 int sc_generate_scene_batch(sc_sim *s, const sc_scene_group *groups, int32_t n_groups, int32_t nm,

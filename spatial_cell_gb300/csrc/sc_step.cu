@@ -858,7 +858,7 @@ __device__ __forceinline__ void relax_class_item(const ScParams &P0, const Relax
 // lanes walk about as many bond terms of the same kind (items with more
 // bonds would otherwise hold back the rest of their warp).
 template <int MODE, bool BATCH>
-__global__ void __launch_bounds__(SC_THREADS) k_relax(ScParams P, RelaxArgs A) {
+__global__ void __launch_bounds__(SC_THREADS, MODE == 0 ? 2 : 4) k_relax(ScParams P, RelaxArgs A) {
     const int n = A.classCount[MODE];
     const int *__restrict__ idx = A.classIdx + (size_t)MODE * A.L.cap;
     if (MODE == 0) {
@@ -973,12 +973,12 @@ struct PoolSlot {
 };
 template <int K, class T>
 __device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, int c, T *__restrict__ pool,
-                                              int poolCap, unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                              long long poolCap, unsigned long long *__restrict__ poolUsed, long long *__restrict__ warpOff,
                                               int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                               int *__restrict__ ovf, int *__restrict__ ovfCount,
                                               const int *__restrict__ items = nullptr) {
     __shared__ int s_n[SC_THREADS / 32];
-    __shared__ int s_base;
+    __shared__ long long s_base;
     const int b0 = blockIdx.x * SC_THREADS, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     int src, cs;
     count_rank<K>(valid, c, &src, &cs);
@@ -994,14 +994,14 @@ __device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, 
         for (int w = 0; w < SC_THREADS / 32; w++) total += s_n[w] * 32;
         // 64-bit demand: it keeps counting what blocks ask for past the pool
         const unsigned long long base = total ? atomicAdd(poolUsed, (unsigned long long)total) : 0ull;
-        s_base = base + (unsigned long long)total <= (unsigned long long)poolCap ? (int)base : -1;
+        s_base = base + (unsigned long long)total <= (unsigned long long)poolCap ? (long long)base : -1ll;
     }
     __syncthreads();
     if (s_base < 0 && cs > 0) {
         ovfl = true;
         n = 0;
     }
-    int off = s_base;
+    long long off = s_base;
     for (int w = 0; w < warp; w++) off += s_n[w] * 32;
     const int g = b0 + t;
     if (g < cap) {
@@ -1034,8 +1034,8 @@ template <bool BATCH>
 __device__ __forceinline__ void emit_m_pairs(const ScParams &P0, bool valid, int c, const uint32_t *scratch,
                                              const int4 *__restrict__ minfo,
                                              const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
-                                             uint4 *__restrict__ pool, int poolCap, unsigned long long *__restrict__ poolUsed,
-                                             int *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
+                                             uint4 *__restrict__ pool, long long poolCap, unsigned long long *__restrict__ poolUsed,
+                                             long long *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
                                              int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const PoolSlot<uint4> S =
         pool_take<SC_LIST_M>(P0, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
@@ -1068,8 +1068,8 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P0, bool valid, int
 // square root and a division per pair) instead of streaming 12 more bytes
 // per pair from HBM.
 __device__ __forceinline__ void emit_m_pairs_lean(const ScParams &P, bool valid, int c, const uint32_t *scratch,
-                                                  uint32_t *__restrict__ pool, int poolCap,
-                                                  unsigned long long *__restrict__ poolUsed, int *__restrict__ warpOff,
+                                                  uint32_t *__restrict__ pool, long long poolCap,
+                                                  unsigned long long *__restrict__ poolUsed, long long *__restrict__ warpOff,
                                                   int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                                   int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const PoolSlot<uint32_t> S =
@@ -1083,9 +1083,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P0, const uint3
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
                                                         const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
-                                                        uint32_t *__restrict__ pool, int poolCap,
+                                                        uint32_t *__restrict__ pool, long long poolCap,
                                                         unsigned long long *__restrict__ poolUsed,
-                                                        int *__restrict__ warpOff, uint32_t *scratch,
+                                                        long long *__restrict__ warpOff, uint32_t *scratch,
                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                                         int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1117,7 +1117,7 @@ struct RelaxMArgs {
     const int4 *__restrict__ pinfo;
     const float4 *__restrict__ pvel;
     const uint4 *__restrict__ pool;     // pairs with their geometry (emit_m_pairs)
-    const int *__restrict__ warpOff;
+    const long long *__restrict__ warpOff;
 };
 
 // The contribution of one colliding neighbour (a metabolic item, or a lipid
@@ -1611,9 +1611,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_lm(ScParams P0, const uint
                                                          const int4 *__restrict__ pinfo,
                                                          const float4 *__restrict__ ppos_,
                                                          const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
-                                                         uint4 *__restrict__ pool, int poolCap,
+                                                         uint4 *__restrict__ pool, long long poolCap,
                                                          unsigned long long *__restrict__ poolUsed,
-                                                         int *__restrict__ warpOff,
+                                                         long long *__restrict__ warpOff,
                                                          uint32_t *scratch, int *__restrict__ cnt,
                                                          int *__restrict__ perm, int cap) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1652,7 +1652,7 @@ template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_partners(
     ScParams P, const uint32_t *__restrict__ cellStartM, const int *__restrict__ nActivePtr,
     const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo, float4 *__restrict__ pvel_,
-    PairList<SC_LIST_LM> L, const uint4 *__restrict__ pool, const int *__restrict__ warpOff,
+    PairList<SC_LIST_LM> L, const uint4 *__restrict__ pool, const long long *__restrict__ warpOff,
     const float4 *__restrict__ mpos, const int4 *__restrict__ minfo, const float4 *__restrict__ mvel) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *nActivePtr) return;
@@ -2744,7 +2744,7 @@ void sc_phase_build_m(ScLaunchCtx &c) {
                           : (c.P.metabLean ? k_build_m<true, false> : k_build_m<false, false>))<<<
                 nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
                 c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info, B.listM,
-                (int)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
+                (long long)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
         }
         (*c.launches)++;
         B.validM = true;
@@ -2795,7 +2795,7 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
         SC_BATCHED(k_build_lm)<<<nblocks(c.P.N), SC_THREADS, 0, c.st>>>(
             c.P, B.cellStartM, B.workP, &B.ctr->workCount, F.info, F.pos, M.pos, M.info,
             reinterpret_cast<uint4 *>(B.listLM),
-            (int)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,
+            (long long)(sc_list_words(SC_LIST_LM, c.P.N) / 4), &B.ctr->poolLM, B.warpOffLM, B.scratchLM, B.cntLM, B.permLM,
             c.P.N);
         (*c.launches)++;
         (*c.launches)++;

@@ -249,3 +249,26 @@ def test_metabolic_fields_no_kernel_touches(product, kind):
     ids = got["id"][act]
     for f in ("last_state_change_step", "scheduled_polymerization", "n_active_interactions"):
         assert np.array_equal(got[f][act], m[f][ids]), f
+
+
+def test_load_rejects_more_than_eight_interactions_and_recovers(product):
+    """sc_load_state refuses a particle with more than 8 interactions (found on
+    the device as the records are unpacked, chunk by chunk) and leaves the sim
+    unloaded; a correct state loads afterwards."""
+    from spatial_cell_gb300.native import ScError
+    cfg, types, rules, p, m, nid = scenes.test_scene(9, n=700, nm=1400, box=38.0)
+    bad = p.copy()
+    bad["n_active_interactions"][123] = 9
+    gpu = product.Simulation(cfg, types, rules)
+    with pytest.raises(ScError, match="particle 123 has more than 8 interactions"):
+        gpu.load_state(bad, m, step=0, next_particle_id=nid)
+    with pytest.raises(ScError):
+        gpu.step(1)
+    gpu.load_state(p, m, step=0, next_particle_id=nid)
+    from oracle.engine import OracleEngine
+    cpu = OracleEngine("port", cfg, types, rules)
+    cpu.load_state(p, m, step=0, next_particle_id=nid)
+    for e in (gpu, cpu):
+        e.prepare()
+        e.step(1)
+    _same(cfg, gpu, cpu, "after a refused load")
