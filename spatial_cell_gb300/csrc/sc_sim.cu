@@ -1187,20 +1187,25 @@ static int grow_pools(sc_sim *s) {
     SC_CK(s, cudaMemcpy(&need, &B.ctr->poolM, sizeof need, cudaMemcpyDeviceToHost));
     if (need <= B.poolCapM) return SC_OK;
     const size_t cap = (size_t)need + (size_t)need / 4 + 1024;
-    uint32_t *grown = nullptr;
-    int rc = dalloc(s, &grown, cap * B.poolEntryWords);
-    if (rc) {  // no room: keep the pool (the overflowing blocks keep scanning)
-        cudaGetLastError();
-        s->err.clear();
-        return SC_OK;
-    }
+    // the old pool goes back to the device's pool first (its lists are
+    // rebuilt anyway), so the new one can take its memory
+    const size_t old = B.poolCapM;
     forget_alloc(s, (void *)B.listM);
     SC_CK(s, cudaFreeAsync(B.listM, s->st));
+    B.listM = nullptr;
+    B.validM = false;
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);  // they hold the old buffer
+    s->graphs.clear();
+    uint32_t *grown = nullptr;
+    int rc = dalloc(s, &grown, cap * B.poolEntryWords);
+    if (rc) {  // no room: a pool of the old size again (the overflowing blocks keep scanning)
+        s->err.clear();
+        if ((rc = dalloc(s, &grown, old * B.poolEntryWords))) return rc;
+        B.listM = grown;
+        return SC_OK;
+    }
     B.listM = grown;
     B.poolCapM = cap;
-    B.validM = false;
-    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
-    s->graphs.clear();
     return SC_OK;
 }
 

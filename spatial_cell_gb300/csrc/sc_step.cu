@@ -1904,7 +1904,7 @@ __device__ __forceinline__ unsigned long long claim_key(sc_f3 delta, int i) {
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(SC_THREADS) k_claim_offer(
+__global__ void __launch_bounds__(SC_THREADS, 3) k_claim_offer(
     ScParams P, const uint32_t *__restrict__ cellStart, const int *__restrict__ work, const int *__restrict__ workCount,
     const float4 *__restrict__ pos, const float4 *__restrict__ rot, const int4 *__restrict__ info,
     const int *__restrict__ state, const int *__restrict__ nbIn, const int *__restrict__ bonds,
