@@ -924,12 +924,6 @@ struct CollisionDistCache {
 // List: per metabolic item, cell by cell, the colliding metabolic items then
 // the colliding lipids (SC_M_FROM_P), as the reference's loops visit them.
 // The M list of metabolic item i, written at position i of `list`.
-// The neighbourhood is walked as one loop over the item's own sequence of
-// slot ranges -- cell by cell in cells27's order, the cell's metabolic range
-// then its lipid range -- so the lanes of a warp, whose items sit in different
-// cells, stay together across range ends instead of waiting at every cell for
-// the lane with the longest range.  The candidates and their order are the
-// per-cell loops' own.
 __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *__restrict__ cellStartM,
                                              const uint32_t *__restrict__ cellStartP, int i,
                                              const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
@@ -939,51 +933,29 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
     const float prad = p4.w, lim = P.maxInt;
-    const int limit = min(SC_LIST_M, P.listLimit);
     CollisionDistCache cm, cp;
-    // the cells of cells27(P, pp, reach(...)), enumerated by one index
-    const Reach R = reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P);
-    const int n = cell_limit(P);
-    const int cx = (int)sc_grid_idx(pp.x, P.cell, n), cy = (int)sc_grid_idx(pp.y, P.cell, n),
-              cz = (int)sc_grid_idx(pp.z, P.cell, n);
-    int x0, x1, y0, y1, z0, z1;
-    if (P.periodic) {
-        x0 = cx + R.xl; x1 = cx + R.xh; y0 = cy + R.yl; y1 = cy + R.yh; z0 = cz + R.zl; z1 = cz + R.zh;
-    } else {
-        x0 = max(cx + R.xl, 0); x1 = min(cx + R.xh, n - 1);
-        y0 = max(cy + R.yl, 0); y1 = min(cy + R.yh, n - 1);
-        z0 = max(cz + R.zl, 0); z1 = min(cz + R.zh, n - 1);
-    }
-    const int ny = y1 - y0 + 1, nz = z1 - z0 + 1, ncell = (x1 - x0 + 1) * ny * nz;
-    int k = -1, ph = 1;
-    uint32_t key = 0, j = 0, e = 0;
-    for (;;) {
-        while (j >= e) {  // the next non-empty range
-            if (ph == 0) {
-                ph = 1;
-                j = cellStartP[key];
-                e = cellStartP[key + 1];
-            } else {
-                if (++k >= ncell) return;
-                const int ix = k / (ny * nz), r = k - ix * (ny * nz), iy = r / nz, iz = r - iy * nz;
-                key = P.periodic ? cell_key(P, wrap_cell(x0 + ix, n), wrap_cell(y0 + iy, n), wrap_cell(z0 + iz, n))
-                                 : cell_key(P, (uint32_t)(x0 + ix), (uint32_t)(y0 + iy), (uint32_t)(z0 + iz));
-                ph = 0;
-                j = cellStartM[key];
-                e = cellStartM[key + 1];
+    cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
+        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
+            if ((int)j == i || !active_m(P, minfo, (int)j)) continue;
+            float4 t4 = mpos[j];
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (cm.collides(prad, t4.w, delta)) {
+                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j;
+                c++;
             }
         }
-        const bool fromP = ph != 0;
-        const int jj = (int)j++;
-        if (fromP ? !active_lipid(P, pinfo, jj) : (jj == i || !active_m(P, minfo, jj))) continue;
-        const float4 t4 = fromP ? ppos_[jj] : mpos[jj];
-        const sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
-        if (outside_cube(delta, lim)) continue;
-        if (fromP ? cp.collides(prad, t4.w, delta) : cm.collides(prad, t4.w, delta)) {
-            if (c < limit) list[sc_list_at(SC_LIST_M, i, c)] = (uint32_t)jj | (fromP ? SC_M_FROM_P : 0u);
-            c++;
+        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
+            if (!active_lipid(P, pinfo, (int)j)) continue;
+            float4 t4 = ppos_[j];
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (cp.collides(prad, t4.w, delta)) {
+                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j | SC_M_FROM_P;
+                c++;
+            }
         }
-    }
+    });
 }
 
 // A pool position for the pairs of one count-ordered list position: the
@@ -2431,58 +2403,16 @@ __device__ __forceinline__ void build_d_item(const ScParams &P, const uint32_t *
     const Imager IM(P, pp, SC_BINNED_M);
     const float lim = P.maxDiff;
     const sc_sqrt_le within = sc_sqrt_le_make(lim);
-    const int limit = min(SC_LIST_D, P.listLimit);
-    // scan27's slot ranges (one per neighbour column, or one per cell of a
-    // column whose z run wraps around the periodic box) walked as one loop,
-    // as build_m_item walks its cells
-    const Reach R = reach(P, pp, lim, SC_BINNED_M);
-    const int n = cell_limit(P);
-    const int cx = (int)sc_grid_idx(pp.x, P.cell, n), cy = (int)sc_grid_idx(pp.y, P.cell, n),
-              cz = (int)sc_grid_idx(pp.z, P.cell, n);
-    int x0, x1, y0, y1, nsub = 1;
-    bool zwrap = false;
-    if (P.periodic) {
-        x0 = cx + R.xl; x1 = cx + R.xh; y0 = cy + R.yl; y1 = cy + R.yh;
-        zwrap = !(cz + R.zl >= 0 && cz + R.zh <= n - 1);
-        if (zwrap) nsub = R.zh - R.zl + 1;
-    } else {
-        x0 = max(cx + R.xl, 0); x1 = min(cx + R.xh, n - 1);
-        y0 = max(cy + R.yl, 0); y1 = min(cy + R.yh, n - 1);
-    }
-    const uint32_t z0 = (uint32_t)max(cz + R.zl, 0), z1 = (uint32_t)min(cz + R.zh, n - 1);
-    const int ny = y1 - y0 + 1, nr = (x1 - x0 + 1) * ny * nsub;
-    int r = -1;
-    uint32_t j = 0, e = 0;
-    for (;;) {
-        while (j >= e) {  // the next non-empty range
-            if (++r >= nr) return;
-            const int col = r / nsub, sub = r - col * nsub, ix = col / ny, iy = col - ix * ny;
-            if (P.periodic) {
-                const uint32_t base = cell_key(P, wrap_cell(x0 + ix, n), wrap_cell(y0 + iy, n), 0);
-                if (zwrap) {
-                    const uint32_t key = base + wrap_cell(cz + R.zl + sub, n);
-                    j = cellStart[key];
-                    e = cellStart[key + 1];
-                } else {
-                    j = cellStart[base + (uint32_t)(cz + R.zl)];
-                    e = cellStart[(base + (uint32_t)(cz + R.zh)) + 1];
-                }
-            } else {
-                const uint32_t base = cell_key(P, (uint32_t)(x0 + ix), (uint32_t)(y0 + iy), 0);
-                j = cellStart[base + z0];
-                e = cellStart[(base + z1) + 1];
-            }
-        }
-        const int jj = (int)j++;
-        if (jj == i || !active_m(P, info, jj)) continue;
-        float4 t4 = pos[jj];
+    scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
+        if (j == i || !active_m(P, info, j)) return;
+        float4 t4 = pos[j];
         sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
-        if (outside_cube(delta, lim)) continue;
+        if (outside_cube(delta, lim)) return;
         if (sc_sqrt_le_test(within, sc_normsq3(delta))) {
-            if (c < limit) list[sc_list_at(SC_LIST_D, i, c)] = (uint32_t)jj;
+            if (c < min(SC_LIST_D, P.listLimit)) list[sc_list_at(SC_LIST_D, i, c)] = (uint32_t)j;
             c++;
         }
-    }
+    });
 }
 
 template <bool BATCH>
