@@ -56,6 +56,14 @@ struct ScBuffers {
     int *permM, *permLM, *permD;  // count-ordered list position -> item
     uint32_t *scratchLM;          // build scratch of the LM list (aliases listD when it fits)
     int *ovfPP, *ovfM;            // overflowed items
+    // The metabolic items whose list overflowed keep their full pair list in
+    // a second pool (16-byte entries as the main one, an item's entries
+    // contiguous): per overflow slot its pair count and first entry (-1: no
+    // room, the item scans its neighbourhood)
+    int *ovfNM;
+    long long *ovfOffM;
+    uint4 *ovfPoolM;
+    size_t ovfPoolCapM;
     long long *warpOffM;          // metabolic pair pool: first entry of every warp's region
     int *workP;                   // particle work list (the items complexify scans)
     unsigned long long *claimP;   // pair-claim keys, one per particle slot (sc_config.pair_claim)

@@ -924,6 +924,36 @@ struct CollisionDistCache {
 // List: per metabolic item, cell by cell, the colliding metabolic items then
 // the colliding lipids (SC_M_FROM_P), as the reference's loops visit them.
 // The M list of metabolic item i, written at position i of `list`.
+// The colliding metabolic items, then lipids, of each neighbour cell of
+// metabolic item i in visiting order, each handed to sink(j, fromP, t4) (j
+// the neighbour's slot, t4 its position and radius; the collision distance is
+// then cached in cm / cp).
+template <class Sink>
+__device__ __forceinline__ void scan_m_item(const ScParams &P, const uint32_t *__restrict__ cellStartM,
+                                            const uint32_t *__restrict__ cellStartP, int i,
+                                            const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
+                                            const float4 *__restrict__ ppos_, const int4 *__restrict__ pinfo,
+                                            const Imager &IM, sc_f3 pp, float prad, CollisionDistCache &cm,
+                                            CollisionDistCache &cp, Sink &&sink) {
+    const float lim = P.maxInt;
+    cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
+        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
+            if ((int)j == i || !active_m(P, minfo, (int)j)) continue;
+            float4 t4 = mpos[j];
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (cm.collides(prad, t4.w, delta)) sink(j, false, t4);
+        }
+        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
+            if (!active_lipid(P, pinfo, (int)j)) continue;
+            float4 t4 = ppos_[j];
+            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, lim)) continue;
+            if (cp.collides(prad, t4.w, delta)) sink(j, true, t4);
+        }
+    });
+}
+
 __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *__restrict__ cellStartM,
                                              const uint32_t *__restrict__ cellStartP, int i,
                                              const float4 *__restrict__ mpos, const int4 *__restrict__ minfo,
@@ -932,30 +962,56 @@ __device__ __forceinline__ void build_m_item(const ScParams &P, const uint32_t *
     float4 p4 = mpos[i];
     const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
     const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
-    const float prad = p4.w, lim = P.maxInt;
     CollisionDistCache cm, cp;
-    cells27(P, pp, reach(P, pp, lim, SC_BINNED_M | SC_BINNED_P), [&](uint32_t key) {
-        for (uint32_t j = cellStartM[key], e = cellStartM[key + 1]; j < e; j++) {
-            if ((int)j == i || !active_m(P, minfo, (int)j)) continue;
-            float4 t4 = mpos[j];
-            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
-            if (outside_cube(delta, lim)) continue;
-            if (cm.collides(prad, t4.w, delta)) {
-                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j;
-                c++;
-            }
+    const int limit = min(SC_LIST_M, P.listLimit);
+    scan_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, IM, pp, p4.w, cm, cp,
+                [&](uint32_t j, bool fromP, float4) {
+                    if (c < limit) list[sc_list_at(SC_LIST_M, i, c)] = fromP ? (j | SC_M_FROM_P) : j;
+                    c++;
+                });
+}
+
+// The full pair lists of the metabolic items whose list overflowed (listed
+// by k_build_m with their pair counts): each takes a contiguous region of
+// the overflow pool by atomicAdd and writes its pairs there in visiting order,
+// 16-byte entries with the frozen geometry as the main pool's; an item the
+// pool has no room for keeps offset -1 (it scans its neighbourhood).  The
+// demand is counted in full for the pool's growth at the next synchronisation.
+template <bool BATCH>
+__global__ void __launch_bounds__(SC_THREADS) k_build_m_ovf(
+    ScParams P0, const uint32_t *__restrict__ cellStartM, const uint32_t *__restrict__ cellStartP,
+    const float4 *__restrict__ mpos, const int4 *__restrict__ minfo, const float4 *__restrict__ ppos_,
+    const int4 *__restrict__ pinfo, const int *__restrict__ ovf, const int *__restrict__ ovfCount,
+    const int *__restrict__ ovfN, long long *__restrict__ ovfOff, uint4 *__restrict__ pool, long long cap,
+    unsigned long long *__restrict__ demand) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
+        const int i = ovf[t], n = ovfN[t];
+        const unsigned long long base = n > 0 ? atomicAdd(demand, (unsigned long long)n) : 0ull;
+        if (n <= 0 || base + (unsigned long long)n > (unsigned long long)cap) {
+            ovfOff[t] = -1;
+            continue;
         }
-        for (uint32_t j = cellStartP[key], e = cellStartP[key + 1]; j < e; j++) {
-            if (!active_lipid(P, pinfo, (int)j)) continue;
-            float4 t4 = ppos_[j];
-            sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
-            if (outside_cube(delta, lim)) continue;
-            if (cp.collides(prad, t4.w, delta)) {
-                if (c < min(SC_LIST_M, P.listLimit)) list[sc_list_at(SC_LIST_M, i, c)] = j | SC_M_FROM_P;
-                c++;
-            }
-        }
-    });
+        ovfOff[t] = (long long)base;
+        ScParams P = P0;
+        rep_apply<BATCH>(P, minfo[i].w);
+        const float4 p4 = mpos[i];
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_M | SC_BINNED_P);
+        const float prad = p4.w;
+        CollisionDistCache cm, cp;
+        uint4 *out = pool + base;
+        int k = 0;
+        scan_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, IM, pp, prad, cm, cp,
+                    [&](uint32_t j, bool fromP, float4 t4) {
+                        if (k >= n) return;
+                        const sc_f3 tpos = IM(sc_make_f3(t4.x, t4.y, t4.z));
+                        const sc_f3 nd = normalize(tpos - pp);
+                        const float cd = fromP ? cp.get(prad, t4.w) : cm.get(prad, t4.w);
+                        const sc_f3 a = tpos - nd * cd;
+                        out[k++] = make_uint4(fromP ? (j | SC_M_FROM_P) : j, __float_as_uint(a.x),
+                                              __float_as_uint(a.y), __float_as_uint(a.z));
+                    });
+    }
 }
 
 // A pool position for the pairs of one count-ordered list position: the
@@ -976,7 +1032,7 @@ __device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, 
                                               long long poolCap, unsigned long long *__restrict__ poolUsed, long long *__restrict__ warpOff,
                                               int *__restrict__ cnt, int *__restrict__ perm, int cap,
                                               int *__restrict__ ovf, int *__restrict__ ovfCount,
-                                              const int *__restrict__ items = nullptr) {
+                                              const int *__restrict__ items = nullptr, int *__restrict__ ovfN = nullptr) {
     __shared__ int s_n[SC_THREADS / 32];
     __shared__ long long s_base;
     const int b0 = blockIdx.x * SC_THREADS, t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -1009,7 +1065,11 @@ __device__ __forceinline__ PoolSlot<T> pool_take(const ScParams &P, bool valid, 
         cnt[g] = ovfl ? INT_MAX : max(cs, 0);
         if (lane == 0) warpOff[g >> 5] = s_base < 0 ? 0 : off;
     }
-    if (ovfl && ovf) ovf[atomicAdd(ovfCount, 1)] = b0 + src;
+    if (ovfl && ovf) {
+        const int t = atomicAdd(ovfCount, 1);
+        ovf[t] = b0 + src;
+        if (ovfN) ovfN[t] = max(cs, 0);  // its full pair count
+    }
     PoolSlot<T> r;
     r.i = cs >= 0 && items ? items[b0 + src] : b0 + src;
     r.n = n;
@@ -1036,9 +1096,10 @@ __device__ __forceinline__ void emit_m_pairs(const ScParams &P0, bool valid, int
                                              const float4 *__restrict__ mpos, const float4 *__restrict__ ppos_,
                                              uint4 *__restrict__ pool, long long poolCap, unsigned long long *__restrict__ poolUsed,
                                              long long *__restrict__ warpOff, int *__restrict__ cnt, int *__restrict__ perm,
-                                             int cap, int *__restrict__ ovf, int *__restrict__ ovfCount) {
-    const PoolSlot<uint4> S =
-        pool_take<SC_LIST_M>(P0, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+                                             int cap, int *__restrict__ ovf, int *__restrict__ ovfCount,
+                                             int *__restrict__ ovfN) {
+    const PoolSlot<uint4> S = pool_take<SC_LIST_M>(P0, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf,
+                                                   ovfCount, nullptr, ovfN);
     if (S.n == 0) return;
     const int i = S.i;
     ScParams P = P0;
@@ -1071,9 +1132,10 @@ __device__ __forceinline__ void emit_m_pairs_lean(const ScParams &P, bool valid,
                                                   uint32_t *__restrict__ pool, long long poolCap,
                                                   unsigned long long *__restrict__ poolUsed, long long *__restrict__ warpOff,
                                                   int *__restrict__ cnt, int *__restrict__ perm, int cap,
-                                                  int *__restrict__ ovf, int *__restrict__ ovfCount) {
-    const PoolSlot<uint32_t> S =
-        pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+                                                  int *__restrict__ ovf, int *__restrict__ ovfCount,
+                                                  int *__restrict__ ovfN) {
+    const PoolSlot<uint32_t> S = pool_take<SC_LIST_M>(P, valid, c, pool, poolCap, poolUsed, warpOff, cnt, perm, cap,
+                                                      ovf, ovfCount, nullptr, ovfN);
     for (int k = 0; k < S.n; k++) S.out[(size_t)k * 32] = scratch[sc_list_at(SC_LIST_M, S.i, k)];
 }
 
@@ -1087,7 +1149,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P0, const uint3
                                                         unsigned long long *__restrict__ poolUsed,
                                                         long long *__restrict__ warpOff, uint32_t *scratch,
                                                         int *__restrict__ cnt, int *__restrict__ perm, int cap,
-                                                        int *__restrict__ ovf, int *__restrict__ ovfCount) {
+                                                        int *__restrict__ ovf, int *__restrict__ ovfCount,
+                                                        int *__restrict__ ovfN) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
@@ -1098,10 +1161,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_m(ScParams P0, const uint3
         if (mi.z & SC_ACTIVE) build_m_item(P, cellStartM, cellStartP, i, mpos, minfo, ppos_, pinfo, scratch, c);
     }
     if (LEAN)
-        emit_m_pairs_lean(P0, valid, c, scratch, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+        emit_m_pairs_lean(P0, valid, c, scratch, pool, poolCap, poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount, ovfN);
     else
         emit_m_pairs<BATCH>(P0, valid, c, scratch, minfo, mpos, ppos_, reinterpret_cast<uint4 *>(pool), poolCap,
-                            poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount);
+                            poolUsed, warpOff, cnt, perm, cap, ovf, ovfCount, ovfN);
 }
 
 
@@ -1293,13 +1356,44 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P0, const 
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
-// The items whose list overflowed (listed by k_build_m), grid-stride.
+// The items whose list overflowed (listed by k_build_m), grid-stride: an
+// item with a region of the overflow pool walks its pairs there as
+// k_relax_metab walks the main pool's (the same terms in the same order);
+// the others scan their neighbourhood.
 template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A,
                                                                      const int *__restrict__ ovf,
-                                                                     const int *__restrict__ ovfCount) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x)
-        relax_metab_scan_item<BATCH>(P, A, ovf[t]);
+                                                                     const int *__restrict__ ovfCount,
+                                                                     const int *__restrict__ ovfN,
+                                                                     const long long *__restrict__ ovfOff,
+                                                                     const uint4 *__restrict__ ovfPool) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
+        const int i = ovf[t];
+        const long long off = ovfOff ? ovfOff[t] : -1;
+        if (off < 0) {
+            relax_metab_scan_item<BATCH>(P, A, i);
+            continue;
+        }
+        if (i < 0) continue;
+        const int4 mi = A.minfo[i];
+        if (!(mi.z & SC_ACTIVE)) continue;
+        const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
+        const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+        const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
+        sc_f3 dV = sc_zero3();
+        float w = 0.0f;
+        const uint4 *e = ovfPool + off;
+        const int n = ovfN[t];
+        for (int k = 0; k < n; k++) {
+            const uint4 E = e[k];
+            const float4 tv = metab_pair_vel(A, E.x);
+            const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
+            const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
+            w += kw;
+            dV += (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
+        }
+        st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+    }
 }
 
 // ---- the same sweep on column-segment tiles (sc_tile.cuh) ---------------------
@@ -2744,7 +2838,14 @@ void sc_phase_build_m(ScLaunchCtx &c) {
                           : (c.P.metabLean ? k_build_m<true, false> : k_build_m<false, false>))<<<
                 nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(
                 c.P, B.cellStartM, B.cellStartP, &B.ctr->nActiveM, M.pos, M.info, F.pos, F.info, B.listM,
-                (long long)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM);
+                (long long)B.poolCapM, &B.ctr->poolM, B.warpOffM, B.listD, B.cntM, B.permM, c.P.Nm, B.ovfM, &B.ctr->ovfM,
+                B.ovfNM);
+            // the overflowed items' full lists
+            cudaMemsetAsync(&B.ctr->poolOvfM, 0, sizeof(B.ctr->poolOvfM), c.st);
+            SC_BATCHED(k_build_m_ovf)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(
+                c.P, B.cellStartM, B.cellStartP, M.pos, M.info, F.pos, F.info, B.ovfM, &B.ctr->ovfM, B.ovfNM,
+                B.ovfOffM, B.ovfPoolM, (long long)B.ovfPoolCapM, &B.ctr->poolOvfM);
+            (*c.launches)++;
         }
         (*c.launches)++;
         B.validM = true;
@@ -2776,8 +2877,8 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
             nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, A);
         (*c.launches)++;
     }
-    SC_BATCHED(k_relax_metab_overflow)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(c.P, A, B.ovfM,
-                                                                                             &B.ctr->ovfM);
+    SC_BATCHED(k_relax_metab_overflow)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(
+        c.P, A, B.ovfM, &B.ctr->ovfM, B.ovfNM, tiles ? nullptr : B.ovfOffM, B.ovfPoolM);
     B.cm[FM_VEL] ^= 1;
     (*c.launches)++;
 }
