@@ -92,8 +92,9 @@ struct ScCounters {
     unsigned long long poolM;   // entries the metabolic list blocks asked of their pool (k_build_m)
     unsigned long long poolLM;  // the same for the lipid-metabolic lists (k_build_lm)
     int workCount;              // items in the particle work list (k_complexify_select)
-    int _pad2;
+    int ovfD;                     // items whose diffusion list overflowed (k_build_d)
     unsigned long long poolOvfM;  // entries the overflowed metabolic items asked of their pool (k_build_m_ovf)
+    unsigned long long poolOvfD;  // the same for the diffusion lists (k_build_d_ovf)
 };
 
 // Relax work classes: 0 bonded items, 1 items with polar (lipid) pairs and no

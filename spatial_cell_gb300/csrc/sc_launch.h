@@ -64,6 +64,13 @@ struct ScBuffers {
     long long *ovfOffM;
     uint4 *ovfPoolM;
     size_t ovfPoolCapM;
+    // the same for the diffusion lists: the overflowed list positions, the
+    // first entry of each one's region by position (-1: it scans), neighbour
+    // slots as entries
+    int *ovfD;
+    long long *ovfOffD;
+    uint32_t *ovfPoolD;
+    size_t ovfPoolCapD;
     long long *warpOffM;          // metabolic pair pool: first entry of every warp's region
     int *workP;                   // particle work list (the items complexify scans)
     unsigned long long *claimP;   // pair-claim keys, one per particle slot (sc_config.pair_claim)

@@ -915,6 +915,7 @@ static int create_sim(const sc_config *cfg_in, const sc_replica *replicas, int32
         (rc = dalloc(s, &B.cntD, Nm)) || (rc = dalloc(s, &B.permM, Nm)) || (rc = dalloc(s, &B.permD, Nm)) ||
         (rc = dalloc(s, &B.permLM, N)) || (rc = dalloc(s, &B.ovfPP, N)) || (rc = dalloc(s, &B.ovfM, Nm)) || (rc = dalloc(s, &B.workP, N)) ||
         (rc = dalloc(s, &B.ovfNM, Nm)) || (rc = dalloc(s, &B.ovfOffM, Nm)) || (rc = dalloc(s, &B.ovfPoolM, 1)) ||
+        (rc = dalloc(s, &B.ovfD, Nm)) || (rc = dalloc(s, &B.ovfOffD, Nm)) || (rc = dalloc(s, &B.ovfPoolD, 1)) ||
         (rc = dalloc(s, &B.claimP, P.pairClaim ? N : 1)) ||
         (rc = dalloc(s, &B.warpOffM, (size_t)Nm / 32 + 1)) || (rc = dalloc(s, &B.warpOffLM, (size_t)N / 32 + 1)) ||
         (rc = dalloc(s, &B.lipidP, N)))
@@ -1182,34 +1183,38 @@ int32_t sc_wait_notices(int64_t *keys, int32_t cap, int32_t timeout_ms) {
 // 1.25x the demand.  Lists of blocks the pool had no room for were scanned
 // instead, so results never depend on the pool's size; step graphs, which
 // hold the old buffer, are dropped.  Called with the sim's streams idle.
-// The overflowed metabolic items' pool grown to its last demand (1.25x), the
-// old one released first; without room it stays as it is.
-static int grow_ovf_pool(sc_sim *s) {
+// An overflow pool (the overflowed metabolic items', or the diffusion
+// lists') grown to its last demand (1.25x), the old one released first;
+// without room it keeps its old size.  Growing drops the lists and the step
+// graphs, which hold the old buffer.
+extern "C++" template <class T>
+int grow_ovf_pool(sc_sim *s, const unsigned long long *demand, T *&pool, size_t &capacity) {
     ScBuffers &B = s->B;
     unsigned long long need = 0;
-    SC_CK(s, cudaMemcpy(&need, &B.ctr->poolOvfM, sizeof need, cudaMemcpyDeviceToHost));
-    if (need <= B.ovfPoolCapM) return SC_OK;
+    SC_CK(s, cudaMemcpy(&need, demand, sizeof need, cudaMemcpyDeviceToHost));
+    if (need <= capacity) return SC_OK;
     const size_t cap = (size_t)need + (size_t)need / 4 + 1024;
-    forget_alloc(s, (void *)B.ovfPoolM);
-    SC_CK(s, cudaFreeAsync(B.ovfPoolM, s->st));
-    B.ovfPoolM = nullptr;
-    B.validM = false;
-    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);  // they hold the old buffer
+    forget_alloc(s, (void *)pool);
+    SC_CK(s, cudaFreeAsync(pool, s->st));
+    pool = nullptr;
+    B.validM = B.validD = false;
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.exec);
     s->graphs.clear();
-    int rc = dalloc(s, &B.ovfPoolM, cap);
+    int rc = dalloc(s, &pool, cap);
     if (rc) {
         s->err.clear();
-        if ((rc = dalloc(s, &B.ovfPoolM, std::max<size_t>(B.ovfPoolCapM, 1)))) return rc;
-        return SC_OK;
+        return dalloc(s, &pool, std::max<size_t>(capacity, 1));
     }
-    B.ovfPoolCapM = cap;
+    capacity = cap;
     return SC_OK;
 }
 
 static int grow_pools(sc_sim *s) {
     ScBuffers &B = s->B;
-    int rc0 = grow_ovf_pool(s);
-    if (rc0) return rc0;
+    int rc0;
+    if ((rc0 = grow_ovf_pool(s, &B.ctr->poolOvfM, B.ovfPoolM, B.ovfPoolCapM)) ||
+        (rc0 = grow_ovf_pool(s, &B.ctr->poolOvfD, B.ovfPoolD, B.ovfPoolCapD)))
+        return rc0;
     unsigned long long need = 0;
     SC_CK(s, cudaMemcpy(&need, &B.ctr->poolM, sizeof need, cudaMemcpyDeviceToHost));
     if (need <= B.poolCapM) return SC_OK;

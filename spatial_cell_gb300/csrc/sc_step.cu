@@ -2514,7 +2514,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
                                                         uint32_t *__restrict__ list, uint32_t *scratch,
-                                                        int *__restrict__ cnt, int *__restrict__ perm, int cap) {
+                                                        int *__restrict__ cnt, int *__restrict__ perm, int cap,
+                                                        int *__restrict__ ovf, int *__restrict__ ovfCount) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < *nActivePtr;
     int c = 0;
@@ -2524,7 +2525,47 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
         rep_apply<BATCH>(Q, in.w);
         if (in.z & SC_ACTIVE) build_d_item(Q, cellStart, i, pos, info, scratch, c);
     }
-    emit_count_ordered<SC_LIST_D>(valid, c, P.listLimit, cap, scratch, list, cnt, perm);
+    emit_count_ordered<SC_LIST_D>(valid, c, P.listLimit, cap, scratch, list, cnt, perm, ovf, ovfCount);
+}
+
+// The full diffusion lists of the overflowed positions (listed by k_build_d;
+// their counts are in cnt): each takes a contiguous region of the overflow
+// pool by atomicAdd and writes its neighbours there in build_d_item's order;
+// a position the pool has no room for keeps offset -1 (it scans).  The demand
+// is counted in full for the pool's growth at the next synchronisation.
+template <bool BATCH>
+__global__ void __launch_bounds__(SC_THREADS) k_build_d_ovf(ScParams P0, const uint32_t *__restrict__ cellStart,
+                                                            const float4 *__restrict__ pos,
+                                                            const int4 *__restrict__ info, const int *__restrict__ ovf,
+                                                            const int *__restrict__ ovfCount, const int *__restrict__ cnt,
+                                                            const int *__restrict__ perm, long long *__restrict__ ovfOff,
+                                                            uint32_t *__restrict__ pool, long long cap,
+                                                            unsigned long long *__restrict__ demand) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
+        const int g = ovf[t], i = perm[g], n = cnt[g];
+        const unsigned long long base = n > 0 ? atomicAdd(demand, (unsigned long long)n) : 0ull;
+        if (i < 0 || n <= 0 || base + (unsigned long long)n > (unsigned long long)cap) {
+            ovfOff[g] = -1;
+            continue;
+        }
+        ovfOff[g] = (long long)base;
+        ScParams P = P0;
+        rep_apply<BATCH>(P, info[i].w);
+        const float4 p4 = pos[i];
+        const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
+        const Imager IM(P, pp, SC_BINNED_M);
+        const float lim = P.maxDiff;
+        const sc_sqrt_le within = sc_sqrt_le_make(lim);
+        uint32_t *out = pool + base;
+        int k = 0;
+        scan27(P, cellStart, pp, reach(P, pp, lim, SC_BINNED_M), [&](int j) {
+            if (j == i || !active_m(P, info, j)) return;
+            const float4 t4 = pos[j];
+            const sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
+            if (outside_cube(delta, lim)) return;
+            if (sc_sqrt_le_test(within, sc_normsq3(delta)) && k < n) out[k++] = (uint32_t)j;
+        });
+    }
 }
 
 template <int SP, bool BATCH>
@@ -2532,7 +2573,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
                                                         const int *__restrict__ nActivePtr,
                                                         const float4 *__restrict__ pos, const int4 *__restrict__ info,
                                                         PairList<SC_LIST_D> L, const float4 *__restrict__ metIn,
-                                                        float4 *__restrict__ metOut) {
+                                                        float4 *__restrict__ metOut, const long long *__restrict__ ovfOff,
+                                                        const uint32_t *__restrict__ ovfPool) {
     constexpr int Q = SP / 4;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;   // list position (count-ordered)
     if (g >= *nActivePtr) return;
@@ -2599,6 +2641,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
             }
             E = En;
         }
+    } else if (ovfOff && ovfOff[g] >= 0) {
+        // an overflowed list kept whole in the overflow pool
+        const uint32_t *__restrict__ e = ovfPool + ovfOff[g];
+        for (int k = 0; k < c; k++) body((int)e[k]);
     } else {
         float4 p4 = pos[i];
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -2997,10 +3043,15 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     MFields M = B.M(), X = B.Mnext();
     if (!B.validD) {
         // the build scratch follows the list in the same buffer
+        cudaMemsetAsync(&B.ctr->ovfD, 0, sizeof(int), c.st);
         SC_BATCHED(k_build_d)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
                                                              B.listD, B.listD + sc_list_words(SC_LIST_D, c.P.Nm),
-                                                             B.cntD, B.permD, c.P.Nm);
-        (*c.launches)++;
+                                                             B.cntD, B.permD, c.P.Nm, B.ovfD, &B.ctr->ovfD);
+        cudaMemsetAsync(&B.ctr->poolOvfD, 0, sizeof(B.ctr->poolOvfD), c.st);
+        SC_BATCHED(k_build_d_ovf)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(
+            c.P, B.cellStartM, M.pos, M.info, B.ovfD, &B.ctr->ovfD, B.cntD, B.permD, B.ovfOffD, B.ovfPoolD,
+            (long long)B.ovfPoolCapD, &B.ctr->poolOvfD);
+        (*c.launches) += 2;
         B.validD = true;
     }
     PairList<SC_LIST_D> L;
@@ -3011,15 +3062,15 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     switch (c.P.SP) {
         case 4:
             (c.P.nRep > 1 ? k_diffuse<4, true> : k_diffuse<4, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                                   L, M.met, X.met);
+                                                                   L, M.met, X.met, B.ovfOffD, B.ovfPoolD);
             break;
         case 8:
             (c.P.nRep > 1 ? k_diffuse<8, true> : k_diffuse<8, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
-                                                                   L, M.met, X.met);
+                                                                   L, M.met, X.met, B.ovfOffD, B.ovfPoolD);
             break;
         default:
             (c.P.nRep > 1 ? k_diffuse<12, true> : k_diffuse<12, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
-                                                                    M.info, L, M.met, X.met);
+                                                                    M.info, L, M.met, X.met, B.ovfOffD, B.ovfPoolD);
             break;
     }
     B.cm[FM_MET] ^= 1;
