@@ -204,6 +204,21 @@ __device__ __forceinline__ sc_f3 ld3(const float4 *p, int i) {
     return sc_make_f3(v.x, v.y, v.z);
 }
 __device__ __forceinline__ void st4(float4 *p, int i, sc_f4 v) { p[i] = make_float4(v.x, v.y, v.z, v.w); }
+
+// A 32-byte row (two float4, 32-byte aligned) in one 256-bit access
+// (ld/st .v8 on the global space, sm_100 and later): a warp's scattered rows
+// then cost one L1 wavefront per row instead of two.  The load is for
+// buffers no thread writes during the kernel.
+__device__ __forceinline__ void ld_row8(const float4 *p, float4 &a, float4 &b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void st_row8(float4 *p, float4 a, float4 b) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
 __device__ __forceinline__ void st3(float4 *p, int i, sc_f3 v, float w) { p[i] = make_float4(v.x, v.y, v.z, w); }
 
 __device__ __forceinline__ int info_state(int w) { return (int)(int8_t)(w & 0xff); }

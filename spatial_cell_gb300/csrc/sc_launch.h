@@ -209,6 +209,7 @@ void sc_phase_relax(ScLaunchCtx &c);
 void sc_phase_relax_metab(ScLaunchCtx &c);
 void sc_phase_build_m(ScLaunchCtx &c);  // the relaxation's metabolic pair list alone
 void sc_phase_relax_partners(ScLaunchCtx &c);
+void sc_phase_build_lm(ScLaunchCtx &c);  // relax_partners' lipid-metabolic pair list alone
 void sc_phase_apply_velocities(ScLaunchCtx &c);
 // prep: the complexify of the start-up sequence (main.cu:324-336, step
 // argument -1); otherwise the step's own, at the device step counter

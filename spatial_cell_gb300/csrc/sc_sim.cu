@@ -186,10 +186,11 @@ __device__ void pack_common(uint8_t *r, int4 in, int state, int lscs, float4 pos
     wr4(r, 240, dbg);
 }
 
-__global__ void k_pack_particles(uint8_t *__restrict__ aos, const int *nActivePtr, int cap, PFields F) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cap) return;
-    uint8_t *r = aos + (size_t)i * 256;
+// Slots [base, end) into records aos[0, end - base).
+__global__ void k_pack_particles(uint8_t *__restrict__ aos, const int *nActivePtr, int base, int end, PFields F) {
+    const int i = base + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    uint8_t *r = aos + (size_t)(i - base) * 256;
     if (i >= *nActivePtr) {
         for (int k = 0; k < 256; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
         return;
@@ -198,12 +199,12 @@ __global__ void k_pack_particles(uint8_t *__restrict__ aos, const int *nActivePt
                 F.angnoise[i], F.nb[i], F.bonds + (size_t)i * 24, F.spoly[i], F.dbg[i]);
 }
 
-__global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePtr, int cap, int SP, MFields F,
-                                 const int *cLscs, const int *cSpoly, const int *cNb, const int *cBonds, int lscs0,
-                                 int spoly0) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cap) return;
-    uint8_t *r = aos + (size_t)i * 304;
+__global__ void k_pack_metabolic(uint8_t *__restrict__ aos, const int *nActivePtr, int base, int end, int SP,
+                                 MFields F, const int *cLscs, const int *cSpoly, const int *cNb, const int *cBonds,
+                                 int lscs0, int spoly0) {
+    const int i = base + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    uint8_t *r = aos + (size_t)(i - base) * 304;
     if (i >= *nActivePtr) {
         for (int k = 0; k < 304; k += 16) *(int4 *)(r + k) = make_int4(0, 0, 0, 0);
         return;
@@ -505,28 +506,26 @@ int run_phase(sc_sim *s, int phase, int arg) {
 // One iteration of the step loop (main.cu:347-661), launched phase by phase.
 int step_direct(sc_sim *s) {
     const sc_config &c = s->cfg;
-    {
-        run_phase(s, SC_PHASE_SORT_PARTICLES, 0);
-        run_phase(s, SC_PHASE_SORT_METABOLIC, 0);
-        run_phase(s, SC_PHASE_MOVE_BROWNIAN, 0);
-        run_phase(s, SC_PHASE_MOVE_BROWNIAN_METAB, 0);
-        for (int j = 0; j < c.noise_coordination_steps; j++) run_phase(s, SC_PHASE_COORDINATE_NOISE, j);
-        run_phase(s, SC_PHASE_APPLY_NOISE, 0);
-        for (int j = 0; j < c.relaxation_steps; j++) {
-            run_phase(s, SC_PHASE_RELAX, j);
-            if (j % 2 == 0) {
-                run_phase(s, SC_PHASE_RELAX_METAB, j);
-                run_phase(s, SC_PHASE_RELAX_PARTNERS, j);
-            }
+    run_phase(s, SC_PHASE_SORT_PARTICLES, 0);
+    run_phase(s, SC_PHASE_SORT_METABOLIC, 0);
+    run_phase(s, SC_PHASE_MOVE_BROWNIAN, 0);
+    run_phase(s, SC_PHASE_MOVE_BROWNIAN_METAB, 0);
+    for (int j = 0; j < c.noise_coordination_steps; j++) run_phase(s, SC_PHASE_COORDINATE_NOISE, j);
+    run_phase(s, SC_PHASE_APPLY_NOISE, 0);
+    for (int j = 0; j < c.relaxation_steps; j++) {
+        run_phase(s, SC_PHASE_RELAX, j);
+        if (j % 2 == 0) {
+            run_phase(s, SC_PHASE_RELAX_METAB, j);
+            run_phase(s, SC_PHASE_RELAX_PARTNERS, j);
         }
-        run_phase(s, SC_PHASE_APPLY_VELOCITIES, 0);
-        run_phase(s, SC_PHASE_COMPLEXIFY, 0);
-        run_phase(s, SC_PHASE_TRANSITION, 0);
-        run_phase(s, SC_PHASE_POLYMERIZE, 0);
-        if (c.propagate_state) run_phase(s, SC_PHASE_PROPAGATE_STATE, 0);
-        for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
-        return run_phase(s, SC_PHASE_END_STEP, 0);
     }
+    run_phase(s, SC_PHASE_APPLY_VELOCITIES, 0);
+    run_phase(s, SC_PHASE_COMPLEXIFY, 0);
+    run_phase(s, SC_PHASE_TRANSITION, 0);
+    run_phase(s, SC_PHASE_POLYMERIZE, 0);
+    if (c.propagate_state) run_phase(s, SC_PHASE_PROPAGATE_STATE, 0);
+    for (int j = 0; j < c.metabolite_diffusion_steps; j++) run_phase(s, SC_PHASE_DIFFUSE, j);
+    return run_phase(s, SC_PHASE_END_STEP, 0);
 }
 
 // The same step as one graph launch: the first step from a given host-side
@@ -1336,29 +1335,51 @@ int sc_device_bytes(const sc_sim *s, int64_t *bytes) {
     return SC_OK;
 }
 
+// The records of slots [0, cap) of one item set, packed chunk by chunk
+// through the staging slot (kStageBytes at most, whatever the state's size):
+// take(first slot, count) runs once a chunk's records are in the slot.
+static int staged_pack(sc_sim *s, bool metabolic, const std::function<int(int, int)> &take) {
+    const int cap = metabolic ? s->P.Nm : s->P.N;
+    if (cap <= 0) return SC_OK;
+    const size_t rec = metabolic ? sizeof(sc_metabolic_particle) : sizeof(sc_particle);
+    const int chunk = (int)std::min<size_t>((size_t)cap, kStageBytes / rec);
+    int rc = ensure_staging(s, (size_t)chunk * rec);
+    if (rc) return rc;
+    ScBuffers &B = s->B;
+    for (int base = 0; base < cap; base += chunk) {
+        const int end = (int)std::min<long long>((long long)base + chunk, cap);
+        if (metabolic)
+            k_pack_metabolic<<<nb_of(end - base), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, base, end,
+                                                                          s->P.SP, B.M(), MC_MIRRORS(B), B.mcLscs0,
+                                                                          B.mcSpoly0);
+        else
+            k_pack_particles<<<nb_of(end - base), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActive, base, end,
+                                                                          B.P());
+        SC_CK(s, cudaStreamSynchronize(s->st));
+        if ((rc = check_launch(s)) || (rc = take(base, end - base))) return rc;
+    }
+    return SC_OK;
+}
+
 int sc_export_state(sc_sim *s, sc_particle *particles, sc_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     enter(s);
-    const int N = s->P.N, Nm = s->P.Nm;
-    int rc = ensure_staging(s, std::max<size_t>(
-                                   std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
-                                   16));
-    if (rc) return rc;
-    ScBuffers &B = s->B;
-    if (particles && N > 0) {
-        k_pack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActive, N, B.P());
-        SC_CK(s, cudaMemcpyAsync(particles, s->staging, (size_t)N * sizeof(sc_particle), cudaMemcpyDeviceToHost, s->st));
-    }
-    if (metabolic && Nm > 0) {
-        SC_CK(s, cudaStreamSynchronize(s->st));
-        k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
-                                                              MC_MIRRORS(B), B.mcLscs0, B.mcSpoly0);
-        SC_CK(s, cudaMemcpyAsync(metabolic, s->staging, (size_t)Nm * sizeof(sc_metabolic_particle),
-                                 cudaMemcpyDeviceToHost, s->st));
-    }
     SC_CK(s, cudaStreamSynchronize(s->st));
+    int rc = SC_OK;
+    if (particles)
+        rc = staged_pack(s, false, [&](int first, int count) {
+            SC_CK(s, cudaMemcpy(particles + first, s->staging, (size_t)count * sizeof(sc_particle),
+                                cudaMemcpyDeviceToHost));
+            return SC_OK;
+        });
+    if (!rc && metabolic)
+        rc = staged_pack(s, true, [&](int first, int count) {
+            SC_CK(s, cudaMemcpy(metabolic + first, s->staging, (size_t)count * sizeof(sc_metabolic_particle),
+                                cudaMemcpyDeviceToHost));
+            return SC_OK;
+        });
     release_staging(s);
-    return check_launch(s);
+    return rc ? rc : check_launch(s);
 }
 
 static int set_batch_reps(sc_sim *s, const std::vector<int> &offP, const std::vector<int> &offM);
@@ -1411,54 +1432,55 @@ static int replica_slots(sc_sim *s, const int4 *info, int cap, int r, std::vecto
     return SC_OK;
 }
 
+// Replica r's records of one item set: its slots' runs (slot order) packed
+// chunk by chunk, each run's part in a chunk copied to its place in `out`
+// (cap records at most; the rest of `out` zero).
+static int export_replica_set(sc_sim *s, int r, bool metabolic, uint8_t *out, size_t cap) {
+    const size_t rec = metabolic ? sizeof(sc_metabolic_particle) : sizeof(sc_particle);
+    memset(out, 0, cap * rec);
+    const int n = metabolic ? s->P.Nm : s->P.N;
+    if (n <= 0) return SC_OK;
+    std::vector<std::pair<int, int>> runs;
+    int rc = replica_slots(s, metabolic ? s->B.M().info : s->B.P().info, n, r, runs);
+    if (rc) return rc;
+    // output position of each run
+    std::vector<size_t> at(runs.size());
+    size_t k = 0;
+    for (size_t u = 0; u < runs.size(); u++) {
+        at[u] = k;
+        k += (size_t)runs[u].second;
+    }
+    size_t u0 = 0;  // first run not yet wholly before the chunk
+    return staged_pack(s, metabolic, [&](int first, int count) {
+        const int last = first + count;
+        while (u0 < runs.size() && runs[u0].first + runs[u0].second <= first) u0++;
+        for (size_t u = u0; u < runs.size() && runs[u].first < last; u++) {
+            const int lo = std::max(first, runs[u].first), hi = std::min(last, runs[u].first + runs[u].second);
+            const size_t dst = at[u] + (size_t)(lo - runs[u].first);
+            if (hi <= lo || dst >= cap) continue;
+            const size_t m = std::min((size_t)(hi - lo), cap - dst);
+            SC_CK(s, cudaMemcpy(out + dst * rec, s->staging + (size_t)(lo - first) * rec, m * rec,
+                                cudaMemcpyDeviceToHost));
+        }
+        return SC_OK;
+    });
+}
+
 int sc_export_replica(sc_sim *s, int32_t r, sc_particle *particles, sc_metabolic_particle *metabolic) {
     if (!s) return set_err(nullptr, SC_E_INVALID, "null sim");
     if (s->reps.empty()) return set_err(s, SC_E_STATE, "not a batched sim");
     if (r < 0 || r >= (int)s->reps.size()) return set_err(s, SC_E_INVALID, "no such replica");
     enter(s);
-    const int N = s->P.N, Nm = s->P.Nm;
-    int rc = ensure_staging(s, std::max<size_t>(
-                                   std::max((size_t)N * sizeof(sc_particle), (size_t)Nm * sizeof(sc_metabolic_particle)),
-                                   16));
-    if (rc) return rc;
-    ScBuffers &B = s->B;
-    std::vector<std::pair<int, int>> runs;
-    if (particles) {
-        const size_t cap = (size_t)s->reps[(size_t)r].num_particles;
-        memset(particles, 0, cap * sizeof(sc_particle));
-        if (N > 0) {
-            k_pack_particles<<<nb_of(N), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActive, N, B.P());
-            SC_CK(s, cudaStreamSynchronize(s->st));
-            if ((rc = replica_slots(s, B.P().info, N, r, runs))) return rc;
-            size_t k = 0;
-            for (auto &run : runs) {
-                const size_t m = std::min((size_t)run.second, cap - std::min(cap, k));
-                if (m) SC_CK(s, cudaMemcpy(particles + k, s->staging + (size_t)run.first * sizeof(sc_particle),
-                                           m * sizeof(sc_particle), cudaMemcpyDeviceToHost));
-                k += m;
-            }
-        }
-    }
-    if (metabolic) {
-        const size_t cap = (size_t)s->reps[(size_t)r].num_metabolic_particles;
-        memset(metabolic, 0, cap * sizeof(sc_metabolic_particle));
-        if (Nm > 0) {
-            k_pack_metabolic<<<nb_of(Nm), SC_THREADS, 0, s->st>>>(s->staging, &B.ctr->nActiveM, Nm, s->P.SP, B.M(),
-                                                                  MC_MIRRORS(B), B.mcLscs0, B.mcSpoly0);
-            SC_CK(s, cudaStreamSynchronize(s->st));
-            if ((rc = replica_slots(s, B.M().info, Nm, r, runs))) return rc;
-            size_t k = 0;
-            for (auto &run : runs) {
-                const size_t m = std::min((size_t)run.second, cap - std::min(cap, k));
-                if (m) SC_CK(s, cudaMemcpy(metabolic + k, s->staging + (size_t)run.first * sizeof(sc_metabolic_particle),
-                                           m * sizeof(sc_metabolic_particle), cudaMemcpyDeviceToHost));
-                k += m;
-            }
-        }
-    }
     SC_CK(s, cudaStreamSynchronize(s->st));
+    int rc = SC_OK;
+    if (particles)
+        rc = export_replica_set(s, r, false, reinterpret_cast<uint8_t *>(particles),
+                                (size_t)s->reps[(size_t)r].num_particles);
+    if (!rc && metabolic)
+        rc = export_replica_set(s, r, true, reinterpret_cast<uint8_t *>(metabolic),
+                                (size_t)s->reps[(size_t)r].num_metabolic_particles);
     release_staging(s);
-    return check_launch(s);
+    return rc ? rc : check_launch(s);
 }
 
 int sc_export_grid(sc_sim *s, int32_t which, uint32_t *ranges, uint32_t *perm) {

@@ -1356,10 +1356,9 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P0, const 
     st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
 }
 
-// The items whose list overflowed (listed by k_build_m), grid-stride: an
-// item with a region of the overflow pool walks its pairs there as
-// k_relax_metab walks the main pool's (the same terms in the same order);
-// the others scan their neighbourhood.
+// The items whose list overflowed (listed by k_build_m) and that the overflow
+// pool had no room for, grid-stride: each scans its neighbourhood
+// (k_relax_metab_pool walks the others).
 template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A,
                                                                      const int *__restrict__ ovf,
@@ -1370,29 +1369,60 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
         const int i = ovf[t];
         const long long off = ovfOff ? ovfOff[t] : -1;
-        if (off < 0) {
-            relax_metab_scan_item<BATCH>(P, A, i);
-            continue;
-        }
-        if (i < 0) continue;
-        const int4 mi = A.minfo[i];
-        if (!(mi.z & SC_ACTIVE)) continue;
+        if (off < 0) relax_metab_scan_item<BATCH>(P, A, i);
+    }
+}
+
+// The overflowed items whose list is kept whole in the overflow pool
+// (k_build_m_ovf), one warp per item: the lanes load 32 entries and the
+// neighbours' velocities at once and each forms its pair's term and weight;
+// lanes 0-2 then add the terms' components and lane 3 the weights in list
+// order from shared memory -- the sums a thread walking the list forms, while
+// a pile-sized list costs one gather latency per 32 pairs.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(RelaxMArgs A, const int *__restrict__ ovf,
+                                                                 const int *__restrict__ ovfCount,
+                                                                 const int *__restrict__ ovfN,
+                                                                 const long long *__restrict__ ovfOff,
+                                                                 const uint4 *__restrict__ ovfPool) {
+    __shared__ float sTerm[SC_THREADS / 32][32][5];   // x, y, z, weight (odd row length: no bank conflicts)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nOvf = *ovfCount;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nOvf; t += (gridDim.x * blockDim.x) >> 5) {
+        const int i = ovf[t];
+        const long long off = ovfOff[t];
+        if (off < 0 || i < 0) continue;   // scanned by k_relax_metab_overflow
+        if (!(A.minfo[i].z & SC_ACTIVE)) continue;
         const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
         const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
         const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
-        sc_f3 dV = sc_zero3();
-        float w = 0.0f;
-        const uint4 *e = ovfPool + off;
+        const uint4 *__restrict__ e = ovfPool + off;
         const int n = ovfN[t];
-        for (int k = 0; k < n; k++) {
-            const uint4 E = e[k];
-            const float4 tv = metab_pair_vel(A, E.x);
-            const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
-            const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
-            w += kw;
-            dV += (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
+        float acc = 0.0f;   // lanes 0-2: dV's components; lane 3: the weight
+        for (int b = 0; b < n; b += 32) {
+            float term[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (b + lane < n) {
+                const uint4 E = e[b + lane];
+                const float4 tv = metab_pair_vel(A, E.x);
+                const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
+                const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
+                const sc_f3 d = (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
+                term[0] = d.x;
+                term[1] = d.y;
+                term[2] = d.z;
+                term[3] = kw;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) sTerm[wid][lane][k] = term[k];
+            __syncwarp();
+            if (lane < 4) {
+                const int m = min(32, n - b);
+                for (int u = 0; u < m; u++) acc += sTerm[wid][u][lane];
+            }
+            __syncwarp();
         }
-        st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+        const float dy = __shfl_sync(0xffffffffu, acc, 1), dz = __shfl_sync(0xffffffffu, acc, 2),
+                    w = __shfl_sync(0xffffffffu, acc, 3);
+        if (lane == 0) st3(A.mvelOut, i, pv + sc_make_f3(acc, dy, dz) / fmaxf(w, 1.0f), v4.w);
     }
 }
 
@@ -2530,7 +2560,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
 
 // The full diffusion lists of the overflowed positions (listed by k_build_d;
 // their counts are in cnt): each takes a contiguous region of the overflow
-// pool by atomicAdd and writes its neighbours there in build_d_item's order;
+// pool (whole 16-byte chunks) by atomicAdd and writes its neighbours there in
+// build_d_item's order;
 // a position the pool has no room for keeps offset -1 (it scans).  The demand
 // is counted in full for the pool's growth at the next synchronisation.
 template <bool BATCH>
@@ -2543,8 +2574,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d_ovf(ScParams P0, const u
                                                             unsigned long long *__restrict__ demand) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
         const int g = ovf[t], i = perm[g], n = cnt[g];
-        const unsigned long long base = n > 0 ? atomicAdd(demand, (unsigned long long)n) : 0ull;
-        if (i < 0 || n <= 0 || base + (unsigned long long)n > (unsigned long long)cap) {
+        // regions are whole 16-byte chunks, so the walk reads four entries per load
+        const unsigned long long n4 = (unsigned long long)((n + 3) & ~3);
+        const unsigned long long base = n > 0 ? atomicAdd(demand, n4) : 0ull;
+        if (i < 0 || n <= 0 || base + n4 > (unsigned long long)cap) {
             ovfOff[g] = -1;
             continue;
         }
@@ -2568,6 +2601,46 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d_ovf(ScParams P0, const u
     }
 }
 
+// An item's amounts, Q float4 per item: eight-amount rows (32 bytes,
+// aligned) in one access.
+template <int Q>
+__device__ __forceinline__ void met_row(const float4 *__restrict__ met, int j, float4 (&v)[Q]) {
+    if (Q == 2) {
+        ld_row8(met + (size_t)j * 2, v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) v[q] = met[(size_t)j * Q + q];
+    }
+}
+template <int SP>
+__device__ __forceinline__ void met_store(float4 *__restrict__ met, int i, const float (&pm)[SP]) {
+    if (SP == 8) {
+        st_row8(met + (size_t)i * 2, make_float4(pm[0], pm[1], pm[2], pm[3]), make_float4(pm[4], pm[5], pm[6], pm[7]));
+    } else {
+#pragma unroll
+        for (int q = 0; q < SP / 4; q++)
+            met[(size_t)i * (SP / 4) + q] = make_float4(pm[4 * q], pm[4 * q + 1], pm[4 * q + 2], pm[4 * q + 3]);
+    }
+}
+// One neighbour's amounts against the item's, the first S of SP amounts
+// (metabolites.cuh:352-431, the exchange of one pair).
+template <int SP>
+__device__ __forceinline__ void diffuse_term(const float4 (&v)[SP / 4], const float (&pm)[SP], float (&dm)[SP],
+                                             int S) {
+#pragma unroll
+    for (int q = 0; q < SP / 4; q++) {
+        const float tm[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int k = 4 * q + c;
+            if (k < S) {
+                const float diff = tm[c] - pm[k];
+                if (sc_diffuse_exceeds(diff)) dm[k] += diff * 0.1f;
+            }
+        }
+    }
+}
+
 template <int SP, bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32_t *__restrict__ cellStart,
                                                         const int *__restrict__ nActivePtr,
@@ -2582,42 +2655,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
     if (i < 0) return;
     if (BATCH) rep_apply<BATCH>(P, info[i].w);
     float pm[SP];
+    {
+        float4 v[Q];
+        met_row<Q>(metIn, i, v);
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-        float4 v = metIn[(size_t)i * Q + q];
-        pm[4 * q] = v.x; pm[4 * q + 1] = v.y; pm[4 * q + 2] = v.z; pm[4 * q + 3] = v.w;
+        for (int q = 0; q < Q; q++) {
+            pm[4 * q] = v[q].x; pm[4 * q + 1] = v[q].y; pm[4 * q + 2] = v[q].z; pm[4 * q + 3] = v[q].w;
+        }
     }
     // after the sort the active items are exactly the binned ones
     const bool act = P.mAllActive ? i < (int)cellStart[P.cells] : (info[i].z & SC_ACTIVE) != 0;
     if (!act) {
-#pragma unroll
-        for (int q = 0; q < Q; q++) metOut[(size_t)i * Q + q] = metIn[(size_t)i * Q + q];
+        met_store<SP>(metOut, i, pm);   // the amounts' bits, unchanged
         return;
     }
     float dm[SP];
 #pragma unroll
     for (int k = 0; k < SP; k++) dm[k] = 0.0f;
     const int S = P.S;
-    auto apply = [&](const float4 *v) {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            float tm[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                int k = 4 * q + c;
-                if (k < S) {
-                    float diff = tm[c] - pm[k];
-                    if (sc_diffuse_exceeds(diff)) dm[k] += diff * 0.1f;
-                }
-            }
-        }
-    };
-    auto body = [&](int j) {
-        float4 v[Q];
-#pragma unroll
-        for (int q = 0; q < Q; q++) v[q] = metIn[(size_t)j * Q + q];
-        apply(v);
-    };
     const int c = L.cnt[g];
     if (c <= min(SC_LIST_D, P.listLimit)) {
         // four entries per list load; their amounts are gathered together and
@@ -2630,21 +2685,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
             float4 v[4][Q];
 #pragma unroll
             for (int kk = 0; kk < 4; kk++)
-                if (k0 + kk < c) {
-#pragma unroll
-                    for (int q = 0; q < Q; q++) v[kk][q] = metIn[(size_t)e[kk] * Q + q];
-                }
+                if (k0 + kk < c) met_row<Q>(metIn, e[kk], v[kk]);
 #pragma unroll
             for (int kk = 0; kk < 4; kk++) {
                 if (k0 + kk >= c) break;
-                apply(v[kk]);
+                diffuse_term<SP>(v[kk], pm, dm, S);
             }
             E = En;
         }
     } else if (ovfOff && ovfOff[g] >= 0) {
-        // an overflowed list kept whole in the overflow pool
-        const uint32_t *__restrict__ e = ovfPool + ovfOff[g];
-        for (int k = 0; k < c; k++) body((int)e[k]);
+        return;   // an overflowed list kept whole in the overflow pool: k_diffuse_pool
     } else {
         float4 p4 = pos[i];
         const sc_f3 pp = sc_make_f3(p4.x, p4.y, p4.z);
@@ -2657,15 +2707,95 @@ __global__ void __launch_bounds__(SC_THREADS) k_diffuse(ScParams P, const uint32
             float4 t4 = pos[j];
             sc_f3 delta = IM(sc_make_f3(t4.x, t4.y, t4.z)) - pp;
             if (outside_cube(delta, lim)) return;
-            if (sc_sqrt_le_test(within, sc_normsq3(delta))) body(j);
+            if (sc_sqrt_le_test(within, sc_normsq3(delta))) {
+                float4 v[Q];
+                met_row<Q>(metIn, j, v);
+                diffuse_term<SP>(v, pm, dm, S);
+            }
         });
     }
 #pragma unroll
     for (int k = 0; k < SP; k++)
         if (k < S) pm[k] += dm[k];
+    met_store<SP>(metOut, i, pm);
+}
+
+// The positions whose overflowed list is kept whole in the overflow pool
+// (k_build_d_ovf), one warp per position: the lanes gather 32 neighbours'
+// amounts at once and each computes its neighbour's terms (zero where the
+// threshold drops the pair; a kept term is never zero), then lane k adds the
+// kept terms of amount k in list order from shared memory -- the sums a
+// thread walking the list forms, term by term, while the list's pile-sized
+// length costs one gather latency per 32 neighbours instead of per 4.
+template <int SP>
+__global__ void __launch_bounds__(SC_THREADS) k_diffuse_pool(ScParams P, const int4 *__restrict__ info,
+                                                             PairList<SC_LIST_D> L, const int *__restrict__ ovf,
+                                                             const int *__restrict__ ovfCount,
+                                                             const long long *__restrict__ ovfOff,
+                                                             const uint32_t *__restrict__ ovfPool,
+                                                             const float4 *__restrict__ metIn,
+                                                             float4 *__restrict__ metOut) {
+    constexpr int Q = SP / 4;
+    __shared__ float sTerm[SC_THREADS / 32][32][SP + 1];   // odd row length: no bank conflicts either way
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int S = P.S;
+    const int n = *ovfCount;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += (gridDim.x * blockDim.x) >> 5) {
+        const int g = ovf[t];
+        const long long off = ovfOff[g];
+        const int i = L.perm[g];
+        if (off < 0 || i < 0) continue;   // scanned by k_diffuse
+        float pm[SP];
+        {
+            float4 v[Q];
+            met_row<Q>(metIn, i, v);
 #pragma unroll
-    for (int q = 0; q < Q; q++)
-        metOut[(size_t)i * Q + q] = make_float4(pm[4 * q], pm[4 * q + 1], pm[4 * q + 2], pm[4 * q + 3]);
+            for (int q = 0; q < Q; q++) {
+                pm[4 * q] = v[q].x; pm[4 * q + 1] = v[q].y; pm[4 * q + 2] = v[q].z; pm[4 * q + 3] = v[q].w;
+            }
+        }
+        // lane k's amount and its running sum
+        float mine = 0.0f, dm = 0.0f;
+#pragma unroll
+        for (int k = 0; k < SP; k++)
+            if (lane == k) mine = pm[k];
+        if (info[i].z & SC_ACTIVE) {
+            const int c = L.cnt[g];
+            const uint32_t *__restrict__ e = ovfPool + off;
+            for (int b = 0; b < c; b += 32) {
+                float term[SP];
+#pragma unroll
+                for (int k = 0; k < SP; k++) term[k] = 0.0f;
+                if (b + lane < c) {
+                    float4 v[Q];
+                    met_row<Q>(metIn, (int)e[b + lane], v);
+#pragma unroll
+                    for (int q = 0; q < Q; q++) {
+                        const float tm[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+                        for (int cc = 0; cc < 4; cc++) {
+                            const int k = 4 * q + cc;
+                            const float diff = tm[cc] - pm[k];
+                            if (k < S && sc_diffuse_exceeds(diff)) term[k] = diff * 0.1f;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < SP; k++) sTerm[wid][lane][k] = term[k];
+                __syncwarp();
+                if (lane < S) {
+                    const int m = min(32, c - b);
+                    for (int u = 0; u < m; u++) {
+                        const float x = sTerm[wid][u][lane];
+                        if (x != 0.0f) dm += x;
+                    }
+                }
+                __syncwarp();
+            }
+            if (lane < S) mine += dm;
+        }
+        if (lane < SP) reinterpret_cast<float *>(metOut)[(size_t)i * SP + lane] = mine;
+    }
 }
 
 // ---- metabolites.cuh:18-88 removeInterferingMetabolicParticles -------------
@@ -2925,11 +3055,17 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     }
     SC_BATCHED(k_relax_metab_overflow)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(
         c.P, A, B.ovfM, &B.ctr->ovfM, B.ovfNM, tiles ? nullptr : B.ovfOffM, B.ovfPoolM);
-    B.cm[FM_VEL] ^= 1;
     (*c.launches)++;
+    if (!tiles) {
+        k_relax_metab_pool<<<std::min(nblocks(c.P.Nm), c.gridCap), SC_THREADS, 0, c.st>>>(
+            A, B.ovfM, &B.ctr->ovfM, B.ovfNM, B.ovfOffM, B.ovfPoolM);
+        (*c.launches)++;
+    }
+    B.cm[FM_VEL] ^= 1;
 }
 
-void sc_phase_relax_partners(ScLaunchCtx &c) {
+// The lipid-metabolic pair list of relax_partners, unless it is already built.
+void sc_phase_build_lm(ScLaunchCtx &c) {
     ScBuffers &B = *c.B;
     if (c.P.N <= 0) return;
     MFields M = B.M();
@@ -2948,6 +3084,14 @@ void sc_phase_relax_partners(ScLaunchCtx &c) {
         (*c.launches)++;
         B.validLM = true;
     }
+}
+
+void sc_phase_relax_partners(ScLaunchCtx &c) {
+    ScBuffers &B = *c.B;
+    if (c.P.N <= 0) return;
+    MFields M = B.M();
+    PFields F = B.P();
+    sc_phase_build_lm(c);
     PairList<SC_LIST_LM> L;
     L.list = B.listLM;
     L.cnt = B.cntLM;
@@ -3059,6 +3203,30 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
     L.cnt = B.cntD;
     L.cap = c.P.Nm;
     L.perm = B.permD;
+    // the positions of the overflow pool run beside the others (on a side
+    // stream when there is one): they write other items and read what the
+    // others read
+    const bool fork = c.side[0] != nullptr;
+    cudaStream_t ps = fork ? c.side[0] : c.st;
+    if (fork) {
+        cudaEventRecord(c.fork, c.st);
+        cudaStreamWaitEvent(ps, c.fork, 0);
+    }
+    const int pg = std::min(nblocks(c.P.Nm), c.gridCap);
+    switch (c.P.SP) {
+        case 4:
+            k_diffuse_pool<4><<<pg, SC_THREADS, 0, ps>>>(c.P, M.info, L, B.ovfD, &B.ctr->ovfD, B.ovfOffD, B.ovfPoolD,
+                                                         M.met, X.met);
+            break;
+        case 8:
+            k_diffuse_pool<8><<<pg, SC_THREADS, 0, ps>>>(c.P, M.info, L, B.ovfD, &B.ctr->ovfD, B.ovfOffD, B.ovfPoolD,
+                                                         M.met, X.met);
+            break;
+        default:
+            k_diffuse_pool<12><<<pg, SC_THREADS, 0, ps>>>(c.P, M.info, L, B.ovfD, &B.ctr->ovfD, B.ovfOffD,
+                                                          B.ovfPoolD, M.met, X.met);
+    }
+    (*c.launches)++;
     switch (c.P.SP) {
         case 4:
             (c.P.nRep > 1 ? k_diffuse<4, true> : k_diffuse<4, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos, M.info,
@@ -3072,6 +3240,10 @@ void sc_phase_diffuse(ScLaunchCtx &c) {
             (c.P.nRep > 1 ? k_diffuse<12, true> : k_diffuse<12, false>)<<<nblocks(c.P.Nm), SC_THREADS, 0, c.st>>>(c.P, B.cellStartM, &B.ctr->nActiveM, M.pos,
                                                                     M.info, L, M.met, X.met, B.ovfOffD, B.ovfPoolD);
             break;
+    }
+    if (fork) {
+        cudaEventRecord(c.join[0], ps);
+        cudaStreamWaitEvent(c.st, c.join[0], 0);
     }
     B.cm[FM_MET] ^= 1;
     (*c.launches)++;
