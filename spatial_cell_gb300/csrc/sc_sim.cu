@@ -1208,12 +1208,22 @@ int grow_ovf_pool(sc_sim *s, const unsigned long long *demand, T *&pool, size_t 
     return SC_OK;
 }
 
+// The main metabolic pool first: when it had no room, whole blocks of
+// ordinary lists overflowed into the overflow pool (at 16 bytes a pair), so
+// that pool's demand is only taken at a synchronisation where the main pool
+// did not grow.
+static int grow_main_pool(sc_sim *s, bool *grew);
 static int grow_pools(sc_sim *s) {
     ScBuffers &B = s->B;
-    int rc0;
-    if ((rc0 = grow_ovf_pool(s, &B.ctr->poolOvfM, B.ovfPoolM, B.ovfPoolCapM)) ||
-        (rc0 = grow_ovf_pool(s, &B.ctr->poolOvfD, B.ovfPoolD, B.ovfPoolCapD)))
-        return rc0;
+    bool grew = false;
+    int rc;
+    if ((rc = grow_main_pool(s, &grew))) return rc;
+    if (!grew && (rc = grow_ovf_pool(s, &B.ctr->poolOvfM, B.ovfPoolM, B.ovfPoolCapM))) return rc;
+    return grow_ovf_pool(s, &B.ctr->poolOvfD, B.ovfPoolD, B.ovfPoolCapD);
+}
+
+static int grow_main_pool(sc_sim *s, bool *grew) {
+    ScBuffers &B = s->B;
     unsigned long long need = 0;
     SC_CK(s, cudaMemcpy(&need, &B.ctr->poolM, sizeof need, cudaMemcpyDeviceToHost));
     if (need <= B.poolCapM) return SC_OK;
@@ -1237,6 +1247,7 @@ static int grow_pools(sc_sim *s) {
     }
     B.listM = grown;
     B.poolCapM = cap;
+    *grew = true;
     return SC_OK;
 }
 
