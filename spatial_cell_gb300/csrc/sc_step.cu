@@ -659,6 +659,142 @@ __device__ __forceinline__ void relax_item(const ScParams &P, const RelaxArgs &A
     if (dbgTouched) st4(A.dbg, i, pdbg);
 }
 
+// A plain particle's relaxation (work class 2: collisions only, list path),
+// with every load that depends on the item alone already issued by the
+// caller (its records, its list count and its first SC_PLAIN_GROUP entries,
+// which lie in its list row whatever the count), so the item waits one
+// memory latency for them and one more for its neighbours.  The terms are
+// relax_item's for this class, in list order.
+__device__ __forceinline__ void relax_plain_item(const ScParams &P, const RelaxArgs &A, int i, float4 v4, float4 r4,
+                                                 float4 a4, float4 p4, int c, const uint32_t (&e0)[SC_PLAIN_GROUP]) {
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, ppos, SC_BINNED_P);
+    const float prad = p4.w;
+    const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
+    sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
+    sc_f3 dV = sc_zero3();
+    const sc_f4 dAV = sc_qid();
+    float w = 0.0f;
+    uint32_t e[SC_PLAIN_GROUP];
+#pragma unroll
+    for (int q = 0; q < SC_PLAIN_GROUP; q++) e[q] = e0[q];
+    for (int k0 = 0; k0 < c; k0 += SC_PLAIN_GROUP) {
+        if (k0 > 0) {
+#pragma unroll
+            for (int q = 0; q < SC_PLAIN_GROUP; q++)
+                e[q] = k0 + q < c ? A.L.list[sc_list_at(SC_LIST_PP, i, k0 + q)] : 0u;
+        }
+        float4 t4[SC_PLAIN_GROUP], tv[SC_PLAIN_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_PLAIN_GROUP; q++) {
+            t4[q] = make_float4(0, 0, 0, 0);
+            tv[q] = t4[q];
+            if (k0 + q < c) {
+                const int j = (int)(e[q] & SC_PP_INDEX);
+                t4[q] = A.pos[j];
+                tv[q] = A.velIn[j];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SC_PLAIN_GROUP; q++) {
+            if (k0 + q < c && (e[q] & SC_PP_COLLIDE)) {
+                // dynamics.cuh:775-786
+                const sc_f3 tpos = IM(sc_make_f3(t4[q].x, t4[q].y, t4[q].z));
+                const float trad = t4[q].w;
+                sc_f3 nd = normalize(tpos - ppos);
+                float cd = prad + trad;
+                sc_f3 tvel = sc_make_f3(tv[q].x, tv[q].y, tv[q].z);
+                w += 1.0f;
+                dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+            }
+        }
+    }
+    sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
+    pav = sc_qmul(sc_slerp(sc_qid(), dAV, 1.0f / fmaxf(w, 1.0f)), pav);
+    st3(A.velOut, i, nv, v4.w);
+    A.rotOut[i] = r4;
+    st4(A.avOut, i, pav);
+}
+
+// A polar particle's relaxation (work class 1: polar and collision pairs,
+// list path): relax_item's terms for this class in list order, with the
+// entries of SC_POLAR_GROUP pairs, then their neighbours' positions,
+// velocities and (polar pairs) rotations, loaded together.
+#define SC_POLAR_GROUP 2
+__device__ __forceinline__ void relax_polar_item(const ScParams &P, const RelaxArgs &A, int i, int4 in, float4 v4,
+                                                 float4 r4, float4 a4, float4 p4, int c) {
+    const sc_f3 ppos = sc_make_f3(p4.x, p4.y, p4.z);
+    const Imager IM(P, ppos, SC_BINNED_P);
+    const float prad = p4.w;
+    const sc_f3 pvel = sc_make_f3(v4.x, v4.y, v4.z);
+    const sc_f4 prot = sc_make_f4(r4.x, r4.y, r4.z, r4.w);
+    sc_f4 pav = sc_make_f4(a4.x, a4.y, a4.z, a4.w);
+    const int phydro = (int)(int8_t)(in.w & 0xff);
+    (void)phydro;
+    sc_f3 dV = sc_zero3();
+    const sc_f4 dAV = sc_qid();
+    sc_f3 phobPos = sc_zero3();
+    float phobSum = 0.0f;
+    float w = 0.0f;
+    const sc_f3 up = sc_rotate(sc_up(), prot);
+    const sc_f3 nextUp = sc_rotate(up, pav);
+    for (int k0 = 0; k0 < c; k0 += SC_POLAR_GROUP) {
+        uint32_t e[SC_POLAR_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_POLAR_GROUP; q++) e[q] = k0 + q < c ? A.L.list[sc_list_at(SC_LIST_PP, i, k0 + q)] : 0u;
+        float4 t4[SC_POLAR_GROUP], tv[SC_POLAR_GROUP], tr[SC_POLAR_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_POLAR_GROUP; q++) {
+            t4[q] = make_float4(0, 0, 0, 0);
+            tv[q] = t4[q];
+            tr[q] = t4[q];
+            if (k0 + q < c) {
+                const int j = (int)(e[q] & SC_PP_INDEX);
+                t4[q] = A.pos[j];
+                if (e[q] & (SC_PP_POLAR | SC_PP_COLLIDE)) tv[q] = A.velIn[j];
+                if (e[q] & SC_PP_POLAR) tr[q] = A.rotIn[j];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SC_POLAR_GROUP; q++) {
+            if (k0 + q >= c) break;
+            const uint32_t fl = e[q];
+            const sc_f3 tpos = IM(sc_make_f3(t4[q].x, t4[q].y, t4[q].z));
+            const float trad = t4[q].w;
+            const sc_f3 tvel = sc_make_f3(tv[q].x, tv[q].y, tv[q].z);
+            if (fl & SC_PP_POLAR) {
+                // dynamics.cuh:478-582: polar (lipid) head / tail attraction
+                sc_f3 nextTup = sc_rotate(sc_rotate(sc_up(), sc_make_f4(tr[q].x, tr[q].y, tr[q].z, tr[q].w)), pav);
+                sc_f3 pPV = -nextUp * prad + ppos + pvel;
+                sc_f3 tpPV = -nextTup * trad + tpos + tvel;
+                float Lr = length(tpPV - pPV) / (prad + trad);
+                float attr = sc_polar_attr(Lr);
+                w += 1.0f;
+                dV += (tpPV - pPV) * 0.05f * attr * 1.0f;
+                float pap = sc_powf(fminf(1.0f / fmaxf(Lr, 1e-6f), 10.0f) / 10.0f, 0.2f);
+                phobSum += pap;
+                phobPos += tpPV * pap;
+            }
+            if (fl & SC_PP_COLLIDE) {
+                // dynamics.cuh:775-786: soft collision with a non-partner
+                sc_f3 nd = normalize(tpos - ppos);
+                float cd = prad + trad;
+                w += 1.0f;
+                dV += (tpos - nd * cd + tvel - (ppos + pvel)) * 0.9f * trad / (prad + trad) * 1.0f;
+            }
+        }
+    }
+    sc_f3 nv = pvel + dV / fmaxf(w, 1.0f);
+    pav = sc_qmul(sc_slerp(sc_qid(), dAV, 1.0f / fmaxf(w, 1.0f)), pav);
+    if (phobSum > 0.0f) {
+        sc_f3 dir = normalize(phobPos / phobSum - (ppos + nv));
+        pav = sc_slerp(pav, sc_quat_from_to(-up, dir), 0.2f);
+    }
+    st3(A.velOut, i, nv, v4.w);
+    A.rotOut[i] = r4;
+    st4(A.avOut, i, pav);
+}
+
 // A bonded particle's relaxation (work class 0, list path).  The pose terms
 // of its rule and chain bonds do not depend on the running sums, so they are
 // evaluated first, from its bond matches (k_build_pp records them in the
@@ -834,6 +970,25 @@ __device__ __forceinline__ void relax_bonded_item(const ScParams &P, const Relax
 // items with a test bond, are left to k_relax_overflow).
 template <int MODE, bool BATCH>
 __device__ __forceinline__ void relax_class_item(const ScParams &P0, const RelaxArgs &A, int i) {
+    if (MODE == 2) {
+        const int4 in = A.info[i];
+        const float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i], p4 = A.pos[i];
+        const int c = A.L.cnt[i];
+        uint32_t e0[SC_PLAIN_GROUP];
+#pragma unroll
+        for (int q = 0; q < SC_PLAIN_GROUP; q++) e0[q] = A.L.list[sc_list_at(SC_LIST_PP, i, q)];
+        if (!(in.z & SC_ACTIVE)) {
+            A.velOut[i] = v4;
+            A.rotOut[i] = r4;
+            A.avOut[i] = a4;
+            return;
+        }
+        ScParams P = P0;
+        rep_apply<BATCH>(P, in.w);
+        if (c > min(SC_LIST_PP, P.listLimit)) return;
+        relax_plain_item(P, A, i, v4, r4, a4, p4, c, e0);
+        return;
+    }
     int4 in = A.info[i];
     float4 v4 = A.velIn[i], r4 = A.rotIn[i], a4 = A.avIn[i];
     if (!(in.z & SC_ACTIVE)) {
@@ -848,7 +1003,7 @@ __device__ __forceinline__ void relax_class_item(const ScParams &P0, const Relax
     if (MODE == 0) {
         if (!(A.matchN[i] & SC_MATCH_INORDER)) relax_bonded_item(P, A, i, in, v4, r4, a4);
     } else {
-        relax_item<false, MODE>(P, A, i, in, v4, r4, a4);
+        relax_polar_item(P, A, i, in, v4, r4, a4, A.pos[i], A.L.cnt[i]);
     }
 }
 
