@@ -1514,8 +1514,13 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P0, const 
 // Lists of the overflow pool longer than this are walked by a whole warp,
 // shorter ones by one thread (both in k_relax_metab_pool): a list that
 // overflowed because the main pool had no room for its block is of ordinary
-// length, one of a wall pile holds hundreds to thousands of pairs.
+// length, one of a wall pile holds hundreds to thousands of pairs.  With the
+// list capacity capped (pair_list_limit, the tests' way into the overflow
+// paths) the bound is four times the cap, so ordinary lists take both walks.
 #define SC_POOL_WARP_MIN 192
+__device__ __forceinline__ int pool_warp_min(const ScParams &P) {
+    return P.listLimit < SC_POOL_WARP_MIN / 4 ? 4 * P.listLimit : SC_POOL_WARP_MIN;
+}
 
 // The items whose list overflowed (listed by k_build_m) and that the overflow
 // pool had no room for, grid-stride: each scans its neighbourhood
@@ -1540,7 +1545,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
 // weight; lanes 0-2 add the terms' components and lane 3 the weights in list
 // order from shared memory -- the sums a thread walking the list forms, while
 // a pile-sized list costs one gather latency per 32 pairs.
-__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(RelaxMArgs A, const int *__restrict__ ovf,
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, RelaxMArgs A, const int *__restrict__ ovf,
                                                                  const int *__restrict__ ovfCount,
                                                                  const int *__restrict__ ovfN,
                                                                  const long long *__restrict__ ovfOff,
@@ -1548,6 +1553,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(RelaxMArgs A, c
     __shared__ float sTerm[SC_THREADS / 32][32][5];   // x, y, z, weight (odd row length: no bank conflicts)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nOvf = *ovfCount;
+    const int warpMin = pool_warp_min(P);
     for (int t0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; t0 < nOvf;
          t0 += ((gridDim.x * blockDim.x) >> 5) * 32) {
         const int t = t0 + lane;
@@ -1559,7 +1565,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(RelaxMArgs A, c
             n = ovfN[t];
         }
         const bool mine = off >= 0 && i >= 0 && (A.minfo[i].z & SC_ACTIVE);
-        if (mine && n <= SC_POOL_WARP_MIN) {
+        if (mine && n <= warpMin) {
             const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
             const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
             const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
@@ -1594,7 +1600,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(RelaxMArgs A, c
             }
             st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
         }
-        unsigned longs = __ballot_sync(0xffffffffu, mine && n > SC_POOL_WARP_MIN);
+        unsigned longs = __ballot_sync(0xffffffffu, mine && n > warpMin);
         while (longs) {
             const int src = __ffs(longs) - 1;
             longs &= longs - 1;
@@ -3266,7 +3272,7 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
     (*c.launches)++;
     if (!tiles) {
         k_relax_metab_pool<<<std::min(nblocks(c.P.Nm), c.gridCap), SC_THREADS, 0, c.st>>>(
-            A, B.ovfM, &B.ctr->ovfM, B.ovfNM, B.ovfOffM, B.ovfPoolM);
+            c.P, A, B.ovfM, &B.ctr->ovfM, B.ovfNM, B.ovfOffM, B.ovfPoolM);
         (*c.launches)++;
     }
     B.cm[FM_VEL] ^= 1;

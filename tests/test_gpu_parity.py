@@ -120,8 +120,10 @@ def test_deterministic(product):
                           (9, 1, 0, 0), (12, 0, 0, 0), (3, 1, 0, 1), (9, 0, 0, 1)])
 def test_pair_list_overflow_paths(product, limit, periodic, tiles, pairs):
     """Items whose pair list overflows are handled by scanning their
-    neighbourhood; with the list capacity capped, both paths run side by side
-    and must still match the oracle bit for bit."""
+    neighbourhood, or, once the overflow pools have grown to their demand at a
+    synchronisation, by walking their whole lists there (a thread per short
+    list, a warp per long one); with the list capacity capped, the paths run
+    side by side and must still match the oracle bit for bit."""
     scene = scenes.test_scene(8, n=900, nm=1800, box=42.0, periodic=periodic)
     scene[0].pair_list_limit = limit
     scene[0].tiles = tiles
@@ -131,6 +133,10 @@ def test_pair_list_overflow_paths(product, limit, periodic, tiles, pairs):
         e.prepare()
         e.step(2)
     _same(cfg, gpu, cpu, f"2 steps with pair lists capped at {limit}")
+    gpu.sync()  # the overflow pools grow to their demand
+    for e in (gpu, cpu):
+        e.step(2)
+    _same(cfg, gpu, cpu, f"2 more steps on the grown overflow pools, lists capped at {limit}")
 
 
 @pytest.mark.parametrize("streams", [1, 3])
