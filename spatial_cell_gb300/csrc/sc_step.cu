@@ -2774,10 +2774,10 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d(ScParams P, const uint32
 
 // The full diffusion lists of the overflowed positions (listed by k_build_d;
 // their counts are in cnt): each takes a contiguous region of the overflow
-// pool (whole 16-byte chunks) by atomicAdd and writes its neighbours there in
-// build_d_item's order;
-// a position the pool has no room for keeps offset -1 (it scans).  The demand
-// is counted in full for the pool's growth at the next synchronisation.
+// pool by atomicAdd and writes its neighbours there in build_d_item's order,
+// for k_diffuse_pool; a position the pool has no room for keeps offset -1 (it
+// scans).  The demand is counted in full for the pool's growth at the next
+// synchronisation.
 template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_build_d_ovf(ScParams P0, const uint32_t *__restrict__ cellStart,
                                                             const float4 *__restrict__ pos,
@@ -2788,7 +2788,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_build_d_ovf(ScParams P0, const u
                                                             unsigned long long *__restrict__ demand) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
         const int g = ovf[t], i = perm[g], n = cnt[g];
-        // regions are whole 16-byte chunks, so the walk reads four entries per load
+        // regions start on 16-byte boundaries (whole chunks of four entries)
         const unsigned long long n4 = (unsigned long long)((n + 3) & ~3);
         const unsigned long long base = n > 0 ? atomicAdd(demand, n4) : 0ull;
         if (i < 0 || n <= 0 || base + n4 > (unsigned long long)cap) {
