@@ -1513,11 +1513,12 @@ __device__ __forceinline__ void relax_metab_scan_item(const ScParams &P0, const 
 
 // Lists of the overflow pool longer than this are walked by a whole warp,
 // shorter ones by one thread (both in k_relax_metab_pool): a list that
-// overflowed because the main pool had no room for its block is of ordinary
-// length, one of a wall pile holds hundreds to thousands of pairs.  With the
-// list capacity capped (pair_list_limit, the tests' way into the overflow
-// paths) the bound is four times the cap, so ordinary lists take both walks.
-#define SC_POOL_WARP_MIN 192
+// overflowed because the main pool had no room for its block fits the list
+// capacity, one that outgrew the capacity (a wall pile's) holds hundreds to
+// thousands of pairs.  With the list capacity capped (pair_list_limit, the
+// tests' way into the overflow paths) the bound is four times the cap, so
+// ordinary lists take both walks.
+#define SC_POOL_WARP_MIN SC_LIST_M
 __device__ __forceinline__ int pool_warp_min(const ScParams &P) {
     return P.listLimit < SC_POOL_WARP_MIN / 4 ? 4 * P.listLimit : SC_POOL_WARP_MIN;
 }
@@ -1537,14 +1538,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P,
 }
 
 // The overflowed items whose list is kept whole in the overflow pool
-// (k_build_m_ovf), 32 at a time per warp.  Each lane walks a short list
-// itself, as k_relax_metab walks the main pool (the same terms in the same
-// order, SC_METAB_GROUP pairs in flight).  The long lists of the 32 are then
-// walked by the whole warp, one after another: the lanes load 32 entries and
-// the neighbours' velocities at once and each forms its pair's term and
-// weight; lanes 0-2 add the terms' components and lane 3 the weights in list
-// order from shared memory -- the sums a thread walking the list forms, while
-// a pile-sized list costs one gather latency per 32 pairs.
+// (k_build_m_ovf).  A short list is walked by one thread, grid-stride over
+// the items, as k_relax_metab walks the main pool (the same terms in the same
+// order, SC_METAB_GROUP pairs in flight).  A long one is walked by a whole
+// warp, warp-stride over the items, so the long lists of a wall pile spread
+// over the device: the lanes load 32 entries and the neighbours' velocities
+// at once and each forms its pair's term and weight; lanes 0-2 add the terms'
+// components and lane 3 the weights in list order from shared memory -- the
+// sums a thread walking the list forms, at one gather latency per 32 pairs.
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, RelaxMArgs A, const int *__restrict__ ovf,
                                                                  const int *__restrict__ ovfCount,
                                                                  const int *__restrict__ ovfN,
@@ -1554,89 +1555,80 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, Rel
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nOvf = *ovfCount;
     const int warpMin = pool_warp_min(P);
-    for (int t0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; t0 < nOvf;
-         t0 += ((gridDim.x * blockDim.x) >> 5) * 32) {
-        const int t = t0 + lane;
-        int i = -1, n = 0;
-        long long off = -1;
-        if (t < nOvf) {
-            i = ovf[t];
-            off = ovfOff[t];
-            n = ovfN[t];
-        }
-        const bool mine = off >= 0 && i >= 0 && (A.minfo[i].z & SC_ACTIVE);
-        if (mine && n <= warpMin) {
-            const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
-            const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
-            const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
-            sc_f3 dV = sc_zero3();
-            float w = 0.0f;
-            const uint4 *__restrict__ e = ovfPool + off;
-            uint4 E[SC_METAB_GROUP];
+    // the short lists, a thread each
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nOvf; t += gridDim.x * blockDim.x) {
+        const int i = ovf[t], n = ovfN[t];
+        const long long off = ovfOff[t];
+        if (off < 0 || i < 0 || n > warpMin || !(A.minfo[i].z & SC_ACTIVE)) continue;
+        const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
+        const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+        const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
+        sc_f3 dV = sc_zero3();
+        float w = 0.0f;
+        const uint4 *__restrict__ e = ovfPool + off;
+        uint4 E[SC_METAB_GROUP];
 #pragma unroll
-            for (int q = 0; q < SC_METAB_GROUP; q++) E[q] = q < n ? e[q] : make_uint4(0, 0, 0, 0);
-            for (int k0 = 0; k0 < n; k0 += SC_METAB_GROUP) {
-                float4 tv[SC_METAB_GROUP];
-                uint4 En[SC_METAB_GROUP];
+        for (int q = 0; q < SC_METAB_GROUP; q++) E[q] = q < n ? e[q] : make_uint4(0, 0, 0, 0);
+        for (int k0 = 0; k0 < n; k0 += SC_METAB_GROUP) {
+            float4 tv[SC_METAB_GROUP];
+            uint4 En[SC_METAB_GROUP];
 #pragma unroll
-                for (int q = 0; q < SC_METAB_GROUP; q++)
-                    tv[q] = k0 + q < n ? metab_pair_vel(A, E[q].x) : make_float4(0, 0, 0, 0);
+            for (int q = 0; q < SC_METAB_GROUP; q++)
+                tv[q] = k0 + q < n ? metab_pair_vel(A, E[q].x) : make_float4(0, 0, 0, 0);
 #pragma unroll
-                for (int q = 0; q < SC_METAB_GROUP; q++) {
-                    const int k = k0 + SC_METAB_GROUP + q;
-                    En[q] = k < n ? e[k] : make_uint4(0, 0, 0, 0);
-                }
-#pragma unroll
-                for (int q = 0; q < SC_METAB_GROUP; q++) {
-                    if (k0 + q < n) {
-                        const float kw = (E[q].x & SC_M_FROM_P) ? 2.0f : 1.0f;
-                        const sc_f3 a = sc_make_f3(__uint_as_float(E[q].y), __uint_as_float(E[q].z),
-                                                   __uint_as_float(E[q].w));
-                        w += kw;
-                        dV += (a + sc_make_f3(tv[q].x, tv[q].y, tv[q].z) - ppv) * 0.9f * kw;
-                    }
-                    E[q] = En[q];
-                }
+            for (int q = 0; q < SC_METAB_GROUP; q++) {
+                const int k = k0 + SC_METAB_GROUP + q;
+                En[q] = k < n ? e[k] : make_uint4(0, 0, 0, 0);
             }
-            st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
-        }
-        unsigned longs = __ballot_sync(0xffffffffu, mine && n > warpMin);
-        while (longs) {
-            const int src = __ffs(longs) - 1;
-            longs &= longs - 1;
-            const int li = __shfl_sync(0xffffffffu, i, src), ln = __shfl_sync(0xffffffffu, n, src);
-            const long long loff = __shfl_sync(0xffffffffu, off, src);
-            const float4 v4 = A.mvelIn[li], p4 = A.mpos[li];
-            const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
-            const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
-            const uint4 *__restrict__ e = ovfPool + loff;
-            float acc = 0.0f;   // lanes 0-2: dV's components; lane 3: the weight
-            for (int b = 0; b < ln; b += 32) {
-                float term[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                if (b + lane < ln) {
-                    const uint4 E = e[b + lane];
-                    const float4 tv = metab_pair_vel(A, E.x);
-                    const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
-                    const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
-                    const sc_f3 d = (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
-                    term[0] = d.x;
-                    term[1] = d.y;
-                    term[2] = d.z;
-                    term[3] = kw;
-                }
 #pragma unroll
-                for (int k = 0; k < 4; k++) sTerm[wid][lane][k] = term[k];
-                __syncwarp();
-                if (lane < 4) {
-                    const int m = min(32, ln - b);
-                    for (int u = 0; u < m; u++) acc += sTerm[wid][u][lane];
+            for (int q = 0; q < SC_METAB_GROUP; q++) {
+                if (k0 + q < n) {
+                    const float kw = (E[q].x & SC_M_FROM_P) ? 2.0f : 1.0f;
+                    const sc_f3 a = sc_make_f3(__uint_as_float(E[q].y), __uint_as_float(E[q].z),
+                                               __uint_as_float(E[q].w));
+                    w += kw;
+                    dV += (a + sc_make_f3(tv[q].x, tv[q].y, tv[q].z) - ppv) * 0.9f * kw;
                 }
-                __syncwarp();
+                E[q] = En[q];
             }
-            const float dy = __shfl_sync(0xffffffffu, acc, 1), dz = __shfl_sync(0xffffffffu, acc, 2),
-                        w = __shfl_sync(0xffffffffu, acc, 3);
-            if (lane == 0) st3(A.mvelOut, li, pv + sc_make_f3(acc, dy, dz) / fmaxf(w, 1.0f), v4.w);
         }
+        st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
+    }
+    // the long lists, a warp each
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nOvf; t += (gridDim.x * blockDim.x) >> 5) {
+        const int i = ovf[t], n = ovfN[t];
+        const long long off = ovfOff[t];
+        if (off < 0 || i < 0 || n <= warpMin || !(A.minfo[i].z & SC_ACTIVE)) continue;   // warp-uniform
+        const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
+        const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
+        const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
+        const uint4 *__restrict__ e = ovfPool + off;
+        float acc = 0.0f;   // lanes 0-2: dV's components; lane 3: the weight
+        for (int b = 0; b < n; b += 32) {
+            float term[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (b + lane < n) {
+                const uint4 E = e[b + lane];
+                const float4 tv = metab_pair_vel(A, E.x);
+                const float kw = (E.x & SC_M_FROM_P) ? 2.0f : 1.0f;
+                const sc_f3 a = sc_make_f3(__uint_as_float(E.y), __uint_as_float(E.z), __uint_as_float(E.w));
+                const sc_f3 d = (a + sc_make_f3(tv.x, tv.y, tv.z) - ppv) * 0.9f * kw;
+                term[0] = d.x;
+                term[1] = d.y;
+                term[2] = d.z;
+                term[3] = kw;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) sTerm[wid][lane][k] = term[k];
+            __syncwarp();
+            if (lane < 4) {
+                const int m = min(32, n - b);
+                for (int u = 0; u < m; u++) acc += sTerm[wid][u][lane];
+            }
+            __syncwarp();
+        }
+        const float dy = __shfl_sync(0xffffffffu, acc, 1), dz = __shfl_sync(0xffffffffu, acc, 2),
+                    w = __shfl_sync(0xffffffffu, acc, 3);
+        if (lane == 0) st3(A.mvelOut, i, pv + sc_make_f3(acc, dy, dz) / fmaxf(w, 1.0f), v4.w);
     }
 }
 
