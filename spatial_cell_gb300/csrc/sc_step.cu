@@ -1523,43 +1523,28 @@ __device__ __forceinline__ int pool_warp_min(const ScParams &P) {
     return P.listLimit < SC_POOL_WARP_MIN / 4 ? 4 * P.listLimit : SC_POOL_WARP_MIN;
 }
 
-// The items whose list overflowed (listed by k_build_m) and that the overflow
-// pool had no room for, grid-stride: each scans its neighbourhood
-// (k_relax_metab_pool walks the others).
+// The items whose list overflowed (listed by k_build_m), a thread each,
+// grid-stride: an item the overflow pool had no room for scans its
+// neighbourhood; one whose region there is short walks it as k_relax_metab
+// walks the main pool (the same terms in the same order, SC_METAB_GROUP pairs
+// in flight); the long regions are k_relax_metab_pool's.
 template <bool BATCH>
 __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_overflow(ScParams P, RelaxMArgs A,
                                                                      const int *__restrict__ ovf,
                                                                      const int *__restrict__ ovfCount,
-                                                                     const long long *__restrict__ ovfOff) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
-        const long long off = ovfOff ? ovfOff[t] : -1;
-        if (off < 0) relax_metab_scan_item<BATCH>(P, A, ovf[t]);
-    }
-}
-
-// The overflowed items whose list is kept whole in the overflow pool
-// (k_build_m_ovf).  A short list is walked by one thread, grid-stride over
-// the items, as k_relax_metab walks the main pool (the same terms in the same
-// order, SC_METAB_GROUP pairs in flight).  A long one is walked by a whole
-// warp, warp-stride over the items, so the long lists of a wall pile spread
-// over the device: the lanes load 32 entries and the neighbours' velocities
-// at once and each forms its pair's term and weight; lanes 0-2 add the terms'
-// components and lane 3 the weights in list order from shared memory -- the
-// sums a thread walking the list forms, at one gather latency per 32 pairs.
-__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, RelaxMArgs A, const int *__restrict__ ovf,
-                                                                 const int *__restrict__ ovfCount,
-                                                                 const int *__restrict__ ovfN,
-                                                                 const long long *__restrict__ ovfOff,
-                                                                 const uint4 *__restrict__ ovfPool) {
-    __shared__ float sTerm[SC_THREADS / 32][32][5];   // x, y, z, weight (odd row length: no bank conflicts)
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nOvf = *ovfCount;
+                                                                     const int *__restrict__ ovfN,
+                                                                     const long long *__restrict__ ovfOff,
+                                                                     const uint4 *__restrict__ ovfPool) {
     const int warpMin = pool_warp_min(P);
-    // the short lists, a thread each
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nOvf; t += gridDim.x * blockDim.x) {
-        const int i = ovf[t], n = ovfN[t];
-        const long long off = ovfOff[t];
-        if (off < 0 || i < 0 || n > warpMin || !(A.minfo[i].z & SC_ACTIVE)) continue;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < *ovfCount; t += gridDim.x * blockDim.x) {
+        const int i = ovf[t];
+        const long long off = ovfOff ? ovfOff[t] : -1;
+        if (off < 0) {
+            relax_metab_scan_item<BATCH>(P, A, i);
+            continue;
+        }
+        const int n = ovfN[t];
+        if (i < 0 || n > warpMin || !(A.minfo[i].z & SC_ACTIVE)) continue;
         const float4 v4 = A.mvelIn[i], p4 = A.mpos[i];
         const sc_f3 pv = sc_make_f3(v4.x, v4.y, v4.z);
         const sc_f3 ppv = sc_make_f3(p4.x, p4.y, p4.z) + pv;
@@ -1594,7 +1579,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, Rel
         }
         st3(A.mvelOut, i, pv + dV / fmaxf(w, 1.0f), v4.w);
     }
-    // the long lists, a warp each
+}
+
+// The overflowed items whose list is kept whole in the overflow pool
+// (k_build_m_ovf) and is longer than pool_warp_min, a warp each, warp-stride
+// over the items so the long lists of a wall pile spread over the device:
+// the lanes load 32 entries and the neighbours' velocities at once and each
+// forms its pair's term and weight; lanes 0-2 add the terms' components and
+// lane 3 the weights in list order from shared memory -- the sums a thread
+// walking the list forms, at one gather latency per 32 pairs.
+__global__ void __launch_bounds__(SC_THREADS) k_relax_metab_pool(ScParams P, RelaxMArgs A, const int *__restrict__ ovf,
+                                                                 const int *__restrict__ ovfCount,
+                                                                 const int *__restrict__ ovfN,
+                                                                 const long long *__restrict__ ovfOff,
+                                                                 const uint4 *__restrict__ ovfPool) {
+    __shared__ float sTerm[SC_THREADS / 32][32][5];   // x, y, z, weight (odd row length: no bank conflicts)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nOvf = *ovfCount;
+    const int warpMin = pool_warp_min(P);
     for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nOvf; t += (gridDim.x * blockDim.x) >> 5) {
         const int i = ovf[t], n = ovfN[t];
         const long long off = ovfOff[t];
@@ -3260,7 +3262,7 @@ void sc_phase_relax_metab(ScLaunchCtx &c) {
         (*c.launches)++;
     }
     SC_BATCHED(k_relax_metab_overflow)<<<std::min(nblocks(c.P.Nm), c.gridCap / 4), SC_THREADS, 0, c.st>>>(
-        c.P, A, B.ovfM, &B.ctr->ovfM, tiles ? nullptr : B.ovfOffM);
+        c.P, A, B.ovfM, &B.ctr->ovfM, B.ovfNM, tiles ? nullptr : B.ovfOffM, B.ovfPoolM);
     (*c.launches)++;
     if (!tiles) {
         k_relax_metab_pool<<<std::min(nblocks(c.P.Nm), c.gridCap), SC_THREADS, 0, c.st>>>(
